@@ -1,0 +1,350 @@
+"""Benchmark: path segments/s of the RTIOW path tracer on GB300.
+
+Default workload (`--config c2`): the RTIOW final scene (485 spheres, seed 0),
+1920x1080, 256 spp, max depth 50, FP32 Kahan accumulation, rendered by the
+plain single-scene wavefront method.  One step = one full render (Draw) of
+that image.  Inputs are synthetic (the seeded scene generator); the working
+set of the ray queues (>1.5 GB) is far larger than L2, so no explicit L2
+flush is done between steps.
+
+Reported keys (one JSON line on rank 0):
+  value      segments/s with the scene resident (device-timed, CUDA events)
+  e2e        the same metric through the public C ABI from host memory:
+             scene upload + LBVH build + render + image download per step
+  roofline   the traversal kernel's algorithmic bytes per launch / its
+             event-timed duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU port (oracle) on a bounded row sample of the workload
+
+`--impl reference` times the reference's path-tracing algorithm on the host
+cores (the CPU port, all threads) on the same config and prints its line.
+With torchrun (N>1) each rank renders its own replica (no collective on the
+data path); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    "c1": dict(workload="RTIOW final scene, 400x225, 16 spp, depth 50, plain wavefront", scene="rtiow",
+               W=400, H=225, spp=16, depth=50, eye=(13, 2, 3)),
+    "c2": dict(workload="RTIOW final scene, 1920x1080, 256 spp, depth 50, plain wavefront", scene="rtiow",
+               W=1920, H=1080, spp=256, depth=50, eye=(13, 2, 3)),
+    "c3": dict(workload="1M-sphere scene (200x20x200 box), 1920x1080, 64 spp, depth 50, plain wavefront",
+               scene="random1m", W=1920, H=1080, spp=64, depth=50, eye=(60, 15, 60)),
+}
+METRIC = "path segments/s on 1 GB300 (batched/served vs plain); p50/p99 render latency"
+UNIT = "segments/s"
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_scene(venu, kind):
+    if kind == "rtiow":
+        return venu.generate_rtiow(0)
+    if kind == "random1m":
+        return venu.generate_random(1_000_000, 1)
+    raise ValueError(kind)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if n_gpus > 0 else "gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
+    """Times the CPU port on a bounded row sample sized to ~target_s seconds."""
+    from oracle import pyoracle
+
+    mode = pyoracle.MODE_GB300 if mode is None else mode
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    r0 = H // 2
+    rows, spp_s = 2, min(spp, 4)
+    t0 = time.perf_counter()
+    res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
+                   rows=(r0, r0 + rows))
+    dt = time.perf_counter() - t0
+    rate = res["segments"] / max(dt, 1e-9)
+    # scale rows to the target time
+    rows = int(max(2, min(H - r0, rows * target_s / max(dt, 1e-3))))
+    t0 = time.perf_counter()
+    res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
+                   rows=(r0, r0 + rows))
+    dt = time.perf_counter() - t0
+    rate = res["segments"] / dt
+    sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
+    return rate, dt, sample, res["segments"]
+
+
+def run_reference(args, cfg, world, rank):
+    if rank != 0:
+        return
+    from oracle import pyoracle
+
+    pyoracle.build()
+    O = pyoracle.Oracle()
+    import venusaur_gb300 as venu
+
+    spheres = make_scene(venu, cfg["scene"])
+    cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, cfg["W"] / cfg["H"], 0.1, 10.0)
+    nt = os.cpu_count() or 1
+    times, segs = [], 0
+    for i in range(args.warmup + args.steps):
+        rate, dt, sample, s = cpu_sample(O, spheres, cam, cfg, nt, target_s=max(2.0, 20.0 / max(1, args.steps)))
+        if i >= args.warmup:
+            times.append(dt)
+            segs += s
+    value = segs / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded RTIOW generator)",
+        "config": {"workload": cfg["workload"], "cpu_sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="venu", choices=["venu", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--max-paths", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    world, rank, local, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, cfg, world, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    import venusaur_gb300 as venu
+    from venusaur_gb300 import build as vb
+
+    vb.build()
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    spheres = make_scene(venu, cfg["scene"])
+    cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    stream = torch.cuda.current_stream()
+    ds = venu.DeviceScene(spheres)
+    wf = venu.Wavefront(args.max_paths, profile=True)
+    accum = venu.new_accum(W, H)
+    img8 = torch.zeros((H * W, 4), dtype=torch.uint8, device="cuda")
+
+    def step(i):
+        wf.render(ds, cam, W, H, spp, accum, subframe=1 + i, max_depth=depth, reset=True, image8=img8)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    segs = 0
+    trav_ms = 0.0
+    trav_n = 0
+    launches = 0
+    e0.record(stream)
+    for i in range(args.steps):
+        step(args.warmup + i)
+        if i == 0:
+            pass
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    # per-step stats are those of the last render; every step renders the
+    # same workload (only the seed differs), so counts are per step
+    st = wf.stats()
+    segs_step = st["segments"]
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    total_segs = segs_step * args.steps * world
+    value = total_segs / (ms / 1000.0)
+    launches = st["kernel_launches"] * args.steps
+
+    # --- roofline of the traversal kernel: counting pass for bytes ---------
+    wfc = venu.Wavefront(args.max_paths, count=True)
+    acc2 = venu.new_accum(W, H)
+    wfc.render(ds, cam, W, H, spp, acc2, subframe=1 + args.warmup + args.steps - 1, max_depth=depth, reset=True)
+    torch.cuda.synchronize()
+    sc = wfc.stats()
+    del acc2
+    nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
+    # algorithmic bytes of the traversal stage per render: 32 B per node
+    # record visited, 16 B per sphere tested, 32 B ray read + 8 B hit write
+    trav_bytes = nodes * 32 + sph * 16 + sc["segments"] * (32 + 8)
+    per_launch_bytes = trav_bytes / max(1, st["traverse_launches"])
+    avg_launch_ms = st["traverse_ms"] / max(1, st["traverse_launches"])
+    achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
+    peak, peak_kind = load_peaks()
+    # FP32 issue view (per segment, SURVEY-style estimate): 20 flop/node, 25/sphere
+    trav_flops = nodes * 20 + sph * 25
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+        "peak_kind": peak_kind, "traffic": None, "kernel": "k_traverse",
+        "bytes_per_segment": trav_bytes / max(1, sc["segments"]),
+        "nodes_per_segment": nodes / max(1, sc["segments"]), "spheres_per_segment": sph / max(1, sc["segments"]),
+        "traverse_share": st["traverse_ms"] / max(1e-9, ms / args.steps),
+        "fp32_tflops": trav_flops / (st["traverse_ms"] / 1000.0) / 1e12,
+    }
+
+    # --- end-to-end through the C ABI from host memory ----------------------
+    import ctypes as C
+
+    from venusaur_gb300._lib import RenderOpts, check, lib, ptr
+
+    host_sph = torch.from_numpy(spheres.view(np.uint8)).pin_memory()
+    host_img = torch.empty((H * W, 4), dtype=torch.uint8).pin_memory()
+    wf_plain = venu.Wavefront(args.max_paths)
+    cam_np = np.ascontiguousarray(cam)
+    h = C.c_void_p(stream.cuda_stream)
+
+    def e2e_step(i):
+        sc_h = C.c_void_p()
+        check(lib().venu_scene_create(ptr(host_sph), len(spheres), h, C.byref(sc_h)))
+        o = RenderOpts(W, H, spp, 1 + i, depth, 1)
+        check(lib().venu_render(wf_plain.handle, sc_h, ptr(cam_np), C.byref(o), ptr(accum), None, ptr(img8), h))
+        host_img.copy_(img8, non_blocking=True)
+        torch.cuda.synchronize()
+        lib().venu_scene_destroy(sc_h)
+
+    e2e_step(0)
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        e2e_step(i + 1)
+    t1 = time.perf_counter()
+    e2e_s = t1 - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": total_segs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(spheres.nbytes),
+           "d2h_bytes_per_step": int(H * W * 4), "ms_per_step": 1000 * e2e_s / args.steps}
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded RTIOW scene generator)",
+        "config": {"workload": cfg["workload"], "width": W, "height": H, "spp": spp, "max_depth": depth,
+                   "spheres": int(len(spheres)), "method": "plain single-scene wavefront",
+                   "l2": "working set (ray queues > 1.5 GB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "segments_per_step": segs_step, "paths_per_step": st["paths"]},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": e2e,
+        "roofline": roofline,
+    }
+    if not args.no_cpu:
+        from oracle import pyoracle
+
+        pyoracle.build()
+        O = pyoracle.Oracle()
+        nt = os.cpu_count() or 1
+        rate, dt, sample, _ = cpu_sample(O, spheres, cam, cfg, nt)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample,
+                                "seconds": dt}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+/*
+ * venu.h -- C ABI of the Venusaur-GB300 path tracer (libvenusaur_gb300.so).
+ *
+ * A drop-in for the reference's OptiX hot path: the LBVH replaces
+ * Renderer::BuildAccelerationStructures, venu_render replaces the
+ * Renderer::Draw -> optixLaunch -> __raygen__rg/__intersection__/
+ * __closesthit__/__miss__ chain.  Citations are relative to the reference
+ * project root (TienYoung/Venusaur).
+ *
+ * Conventions:
+ *  - plain C types only; every call returns a venu_status (no exceptions
+ *    cross the ABI); venu_last_error() gives the message of the last failure
+ *    on the calling thread;
+ *  - device pointers are CUDA device addresses on the current device;
+ *    `stream` is a cudaStream_t passed as void* (NULL = legacy stream);
+ *  - handles are thread-compatible, not thread-safe: one thread per handle
+ *    at a time;
+ *  - the library has no CPU fallback: without a usable sm_103 device every
+ *    GPU entry point returns VENU_ERR_NO_DEVICE.
+ */
+#ifndef VENU_H
+#define VENU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VENU_API __attribute__((visibility("default")))
+#else
+#define VENU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum venu_status {
+    VENU_OK = 0,
+    VENU_ERR_INVALID = 1,    /* bad argument */
+    VENU_ERR_CUDA = 2,       /* CUDA runtime error */
+    VENU_ERR_OOM = 3,        /* device allocation failed or over budget */
+    VENU_ERR_NO_DEVICE = 4,  /* no CUDA device / not sm_103 */
+    VENU_ERR_STACK = 5,      /* traversal stack overflow (reported, never expected) */
+    VENU_ERR_TIMEOUT = 6,    /* a bounded device wait gave up */
+    VENU_ERR_CANCELLED = 7,  /* job cancelled (server) */
+    VENU_ERR_TOO_LARGE = 8,  /* size beyond a stated limit */
+    VENU_ERR_NOT_READY = 9   /* result not available yet (server poll) */
+} venu_status;
+
+/* Material::Type (Core/material.h:8-13). */
+typedef enum venu_material_type {
+    VENU_LAMBERTIAN = 0,
+    VENU_METAL = 1,
+    VENU_DIELECTRIC = 2
+} venu_material_type;
+
+/* Sphere(center, radius, Material(type, albedo, fuzz, ir))
+ * (Core/sphere.h:8-13, Core/material.h:16-19); 48 bytes. */
+typedef struct venu_sphere {
+    float center[3];
+    float radius;
+    float albedo[3];
+    float fuzz;
+    float ir;
+    uint32_t material; /* venu_material_type */
+    uint32_t pad[2];
+} venu_sphere;
+
+/* Camera fields of Params (Core/RayTracer.h:10-14): origin, the U/V/W frame
+ * of Camera::UVWFrame (Core/Camera.cpp:16-37) and the lens radius
+ * (Core/camera.h:20). */
+typedef struct venu_camera {
+    float origin[3];
+    float u[3];
+    float v[3];
+    float w[3];
+    float lens_radius;
+} venu_camera;
+
+/* Per-call render parameters (Params width/height/samples_per_pixel/
+ * subframe_index, Core/RayTracer.h:6-9; Core/RayTracer.cu:172 max_depth). */
+typedef struct venu_render_opts {
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples_per_pixel;
+    uint32_t subframe_index; /* seeds tea<4>(pixel, subframe_index) */
+    uint32_t max_depth;      /* ray casts per path, >= 1 (reference: 4) */
+    uint32_t flags;          /* VENU_FLAG_* */
+} venu_render_opts;
+
+#define VENU_FLAG_RESET_ACCUM 1u /* zero the accumulator first (camera change) */
+
+/* Accumulator layout: 8 floats per pixel {sum.r, sum.g, sum.b, n,
+ * comp.r, comp.g, comp.b, 0} -- a Kahan-compensated running sum of path
+ * radiance over every sample since the last reset. */
+#define VENU_ACCUM_FLOATS_PER_PIXEL 8
+
+typedef struct venu_scene venu_scene;
+typedef struct venu_renderer venu_renderer;
+
+typedef struct venu_scene_info {
+    uint32_t num_spheres;
+    uint32_t num_nodes;      /* internal LBVH nodes (num_spheres - 1) */
+    uint64_t device_bytes;   /* resident bytes owned by the scene */
+    float bounds[6];         /* centroid bounds used for Morton quantisation */
+    float build_ms;          /* device time of the last LBVH build */
+} venu_scene_info;
+
+typedef struct venu_render_stats {
+    uint64_t segments;       /* ray casts of the last render (primary + bounces) */
+    uint64_t paths;          /* paths of the last render (W*H*spp) */
+    uint32_t waves;          /* waves of the last render */
+    uint32_t kernel_launches;/* kernels launched by the last render */
+    uint64_t nodes_visited;  /* counting renders only (VENU_RENDERER_COUNT) */
+    uint64_t spheres_tested; /* counting renders only */
+    float traverse_ms;       /* profiling renders only (VENU_RENDERER_PROFILE): */
+    float shade_ms;          /*   summed CUDA-event times of each kernel's launches */
+    uint32_t traverse_launches;
+    uint32_t shade_launches;
+} venu_render_stats;
+
+/* ---- errors / device -------------------------------------------------- */
+VENU_API const char* venu_last_error(void);
+/* Checks that the current device is usable (sm_103, kernels load). */
+VENU_API venu_status venu_device_check(int* sm_count_out, int* cc_major_out, int* cc_minor_out);
+
+/* ---- host-side scene and camera helpers ------------------------------ */
+/* The RTIOW final scene (Core/Scene.h:13-80) from a seeded generator with a
+ * fixed draw order; returns the sphere count (<= 488) and writes up to cap. */
+VENU_API uint32_t venu_scene_generate_rtiow(uint32_t seed, venu_sphere* out, uint32_t cap);
+/* Ground sphere plus n-1 random spheres: centers uniform in [box_lo, box_hi],
+ * radii log-uniform in [rmin, rmax], materials 80/15/5 as Core/Scene.h:28-64. */
+VENU_API venu_status venu_scene_generate_random(uint32_t n, uint32_t seed, const float box_lo[3],
+                                       const float box_hi[3], float rmin, float rmax,
+                                       venu_sphere* out);
+/* Camera(origin, vfov, aspect, aperture, focal) + SetForward(lookat - origin)
+ * + UVWFrame (Core/camera.h:14, Core/Camera.cpp:24-37, Core/Core.cpp:355). */
+VENU_API void venu_camera_look_at(const float eye[3], const float lookat[3], float vfov_deg, float aspect,
+                         float aperture, float focal, venu_camera* out);
+/* Camera::UpdateUVW (Core/Camera.cpp:27-37) for a unit forward vector. */
+VENU_API void venu_camera_frame(const float eye[3], const float forward[3], float vfov_deg, float aspect,
+                       float aperture, float focal, venu_camera* out);
+
+/* ---- scene: LBVH build (replaces Renderer::BuildAccelerationStructures,
+ *      Core/Renderer.h:160-255, and CreateSBT's per-sphere records,
+ *      Core/Renderer.h:452-520) ------------------------------------------ */
+/* Uploads `n` spheres from host memory and builds the LBVH on the device
+ * (Morton30, radix sort, Karras hierarchy, refit).  Blocks until built. */
+VENU_API venu_status venu_scene_create(const venu_sphere* spheres_host, uint32_t n, void* stream,
+                              venu_scene** out);
+/* Same, from spheres already in device memory. */
+VENU_API venu_status venu_scene_create_device(const venu_sphere* spheres_dev, uint32_t n, void* stream,
+                                     venu_scene** out);
+VENU_API venu_status venu_scene_info_get(const venu_scene* scene, venu_scene_info* out);
+/* Copies the built LBVH to host buffers (any may be NULL): sorted Morton
+ * codes [n], sorted original ids [n], internal nodes [(n-1) x 32 bytes:
+ * lo[3], left, hi[3], right; child >= 0 internal, child|0x80000000 leaf slot]. */
+VENU_API venu_status venu_scene_export_bvh(const venu_scene* scene, uint32_t* morton, uint32_t* ids,
+                                  void* nodes);
+VENU_API venu_status venu_scene_destroy(venu_scene* scene);
+
+/* ---- closest hit for arbitrary rays (optixTrace without programs) ----- */
+/* rays_dev: n x 6 floats (origin, direction).  Writes, per ray, the hit
+ * distance t (tmax on a miss), the original sphere index (-1 on a miss) and
+ * front = 1 when the ray hits the outside (set_face_normal,
+ * Core/RayTracer.cu:219-224). */
+VENU_API venu_status venu_trace(const venu_scene* scene, const float* rays_dev, uint32_t n, float tmin,
+                       float tmax, float* t_dev, int32_t* id_dev, uint32_t* front_dev,
+                       void* stream);
+
+/* ---- renderer: the plain single-scene wavefront method ---------------- */
+#define VENU_RENDERER_COUNT 1u   /* count nodes visited / spheres tested */
+#define VENU_RENDERER_PROFILE 2u /* CUDA events around every traverse / shade launch */
+
+/* max_paths: paths in flight per wave (0 = default 8 Mi). */
+VENU_API venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, venu_renderer** out);
+/* One Renderer::Draw: spp samples per pixel for every pixel, added to the
+ * accumulator (VENU_ACCUM_FLOATS_PER_PIXEL floats per pixel, device), then
+ * the running mean written to image_f (RGBA32F, may be NULL) and image8
+ * (sRGB RGBA8 as Core/RayTracer.cu:16-47, may be NULL).  Asynchronous on
+ * `stream`; statistics are final once the stream has been synchronised. */
+VENU_API venu_status venu_render(venu_renderer* r, const venu_scene* scene, const venu_camera* camera,
+                        const venu_render_opts* opts, float* accum_dev, float* image_f_dev,
+                        uint8_t* image8_dev, void* stream);
+VENU_API venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* out);
+VENU_API venu_status venu_renderer_destroy(venu_renderer* r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VENU_H */

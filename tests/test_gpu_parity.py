@@ -1,0 +1,226 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Bars:
+  * LBVH (Morton codes, sorted order, Karras topology, node boxes): bit-exact;
+  * closest hit for arbitrary rays: bit-exact against the oracle's FP32
+    traversal; sphere id equal and t within 1e-5 relative of the FP64
+    brute-force oracle for well-conditioned rays (not within ~0.6 degrees of
+    tangency, no second sphere within 1e-4 relative);
+  * rendering: the accumulator (Kahan sums, sample counts), the float image
+    and the segment count are bit-exact against the oracle's GB300 arithmetic,
+    at several wave shapes; sRGB bytes within 1 (powf differs by an ulp
+    between the device and host libm).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+def _dev_scene(venu, spheres):
+    return venu.DeviceScene(spheres)
+
+
+def test_device_is_sm103(venu, cuda):
+    import ctypes as C
+
+    sms, ma, mi = C.c_int(), C.c_int(), C.c_int()
+    st = venu.lib().venu_device_check(C.byref(sms), C.byref(ma), C.byref(mi))
+    assert st == 0, venu.lib().venu_last_error()
+    assert (ma.value, mi.value) == (10, 3)
+    assert sms.value >= 100
+
+
+@pytest.mark.parametrize("case", ["rtiow", "n1", "n2", "n3", "rand1k", "rand100k", "dups"])
+def test_lbvh_bit_exact(venu, oracle, cuda, case):
+    if case == "rtiow":
+        sp = oracle.scene_rtiow(0)
+    elif case.startswith("n"):
+        sp = oracle.scene_rtiow(1)[: int(case[1:])]
+    elif case == "rand1k":
+        sp = oracle.scene_random(1000, 1)
+    elif case == "rand100k":
+        sp = oracle.scene_random(100_000, 2)
+    else:
+        sp = oracle.scene_random(3000, 4)
+        sp["center"][100:900] = sp["center"][100]  # many equal Morton codes
+    ds = _dev_scene(venu, sp)
+    got = ds.export_bvh()
+    want = oracle.lbvh(sp)
+    assert np.array_equal(got["keys"], want["keys"])
+    assert np.array_equal(got["ids"], want["ids"])
+    assert got["nodes"].tobytes() == want["nodes"].tobytes()
+    info = ds.info()
+    assert info["num_spheres"] == len(sp)
+    assert np.array_equal(info["bounds"], want["bounds"]) or len(sp) == 0
+
+
+def test_lbvh_golden(venu, cuda):
+    g = np.load(GOLDEN)
+    sp = g["scene"].reshape(-1).view(pyoracle.SPHERE_DTYPE)
+    got = _dev_scene(venu, sp).export_bvh()
+    assert np.array_equal(got["keys"], g["bvh_keys"])
+    assert np.array_equal(got["ids"], g["bvh_ids"])
+    assert got["nodes"].view(np.uint8).tobytes() == g["bvh_nodes"].tobytes()
+
+
+def _random_rays(n, seed, lo=(-12, 0.01, -12), hi=(14, 4, 12)):
+    rng = np.random.default_rng(seed)
+    o = np.stack([rng.uniform(lo[i], hi[i], n) for i in range(3)], 1)
+    d = rng.normal(size=(n, 3))
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+@pytest.mark.parametrize("scene", ["rtiow", "rand50k"])
+def test_trace_matches_oracle(venu, oracle, cuda, scene):
+    torch = cuda
+    if scene == "rtiow":
+        sp = oracle.scene_rtiow(0)
+        rays = _random_rays(30000, 5)
+    else:
+        sp = oracle.scene_random(50_000, 6)
+        rays = _random_rays(30000, 7, lo=(-100, 0, -100), hi=(100, 25, 100))
+    ds = _dev_scene(venu, sp)
+    t, idv, front = ds.trace(torch.from_numpy(rays).cuda())
+    t, idv, front = t.cpu().numpy(), idv.cpu().numpy(), front.cpu().numpy()
+    ob, tb, fb, _, _ = oracle.trace_bvh(sp, rays)
+    assert np.array_equal(idv, ob)
+    assert np.array_equal(t.view(np.uint32), tb.view(np.uint32))
+    assert np.array_equal(front.astype(np.uint32), fb)
+    # FP64 brute force: closest sphere and 1e-5 relative t
+    id64, t64, disc, t2 = oracle.trace_fp64(sp, rays)
+    well = (id64 >= 0) & (disc > 1e-4) & (t2 > t64 * (1 + 1e-4))
+    assert well.sum() > 1000
+    assert np.array_equal(idv[well], id64[well])
+    rel = np.abs(t[well].astype(np.float64) - t64[well]) / t64[well]
+    assert rel.max() < 1e-5, rel.max()
+    assert ((idv < 0) == (id64 < 0)).mean() > 0.999
+
+
+def test_trace_secondary_rays(venu, oracle, cuda):
+    """Rays leaving sphere surfaces (the hard case for the quadratic)."""
+    torch = cuda
+    sp = oracle.scene_rtiow(0)
+    rays = _random_rays(30000, 8)
+    ds = _dev_scene(venu, sp)
+    t, idv, _ = ds.trace(torch.from_numpy(rays).cuda())
+    t, idv = t.cpu().numpy(), idv.cpu().numpy()
+    h = idv >= 0
+    p = rays[h, :3] + rays[h, 3:] * t[h, None]
+    d = np.random.default_rng(9).normal(size=p.shape)
+    rays2 = np.concatenate([p, d], 1).astype(np.float32)
+    t2, id2, _ = ds.trace(torch.from_numpy(rays2).cuda())
+    t2, id2 = t2.cpu().numpy(), id2.cpu().numpy()
+    ob, tb, _, _, _ = oracle.trace_bvh(sp, rays2)
+    assert np.array_equal(id2, ob) and np.array_equal(t2.view(np.uint32), tb.view(np.uint32))
+    id64, t64, disc, tsec = oracle.trace_fp64(sp, rays2)
+    well = (id64 >= 0) & (disc > 1e-4) & (tsec > t64 * (1 + 1e-4))
+    assert np.array_equal(id2[well], id64[well])
+    assert (np.abs(t2[well].astype(np.float64) - t64[well]) / t64[well]).max() < 1e-5
+
+
+def _render_gpu(venu, cuda, sp, cam, W, H, spp, subframe, depth, max_paths=0, accum=None, reset=True):
+    torch = cuda
+    ds = _dev_scene(venu, sp)
+    wf = venu.Wavefront(max_paths)
+    if accum is None:
+        accum = venu.new_accum(W, H)
+    img_f = torch.zeros((H * W, 4), dtype=torch.float32, device="cuda")
+    img8 = torch.zeros((H * W, 4), dtype=torch.uint8, device="cuda")
+    wf.render(ds, cam, W, H, spp, accum, subframe=subframe, max_depth=depth, reset=reset, image_f=img_f,
+              image8=img8)
+    torch.cuda.synchronize()
+    st = wf.stats()
+    return accum.cpu().numpy(), img_f.cpu().numpy(), img8.cpu().numpy(), st
+
+
+@pytest.mark.parametrize("depth", [1, 4, 50])
+def test_render_bit_exact(venu, oracle, cuda, depth):
+    sp = oracle.scene_rtiow(0)
+    W, H, spp = 48, 27, 4
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    acc, img_f, img8, st = _render_gpu(venu, cuda, sp, cam, W, H, spp, 1, depth)
+    want = oracle.render(sp, cam, W, H, spp, subframe=1, max_depth=depth, mode=pyoracle.MODE_GB300)
+    assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
+    assert np.array_equal(img_f.view(np.uint32), want["image_f"].view(np.uint32))
+    assert np.abs(img8.astype(int) - want["image8"].astype(int)).max() <= 1
+    assert st["segments"] == want["segments"]
+    assert st["paths"] == W * H * spp
+
+
+def test_render_golden(venu, cuda):
+    g = np.load(GOLDEN)
+    sp = g["scene"].reshape(-1).view(pyoracle.SPHERE_DTYPE)
+    cam = g["camera"].view(pyoracle.CAMERA_DTYPE)
+    W, H, spp = (int(x) for x in g["wh_spp"])
+    for depth in (4, 50):
+        acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, spp, 1, depth)
+        assert np.array_equal(acc.view(np.uint32), g[f"gb_d{depth}_accum"].view(np.uint32))
+        assert st["segments"] == int(g[f"gb_d{depth}_segments"][0])
+
+
+@pytest.mark.parametrize("max_paths", [997, 3 * 40 * 30, 40 * 30 * 7 + 5])
+def test_render_wave_shapes(venu, oracle, cuda, max_paths):
+    """Waves of P < npix pixels, of k < spp samples, and a single wave all
+    give the same bits (per-pixel sample order is preserved)."""
+    sp = oracle.scene_rtiow(2)
+    W, H, spp = 40, 30, 7
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, spp, 3, 8, max_paths=max_paths)
+    want = oracle.render(sp, cam, W, H, spp, subframe=3, max_depth=8, mode=pyoracle.MODE_GB300)
+    assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
+    assert st["segments"] == want["segments"]
+
+
+def test_progressive_accumulation(venu, oracle, cuda):
+    """Renderer::Draw twice (subframes 1 and 2) == the oracle accumulating the
+    same subframes into one Kahan buffer."""
+    sp = oracle.scene_rtiow(0)
+    W, H = 32, 20
+    cam_np = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    scene = venu.Scene(spheres=sp)
+    r = venu.Renderer(samples_per_pixel=3, max_depth=6)
+    r.Init(scene)
+    cam = venu.Camera((13, 2, 3), 20.0, W / H, 0.1, 10.0)
+    cam.SetForward(np.float32([0, 0, 0]) - np.float32([13, 2, 3]))
+    assert cam.params().tobytes() == cam_np.tobytes()
+    out = venu.CUDAOutputBuffer(W, H)
+    r.Draw(cam, out)
+    r.Draw(cam, out)
+    acc = r.accum.cpu().numpy()
+    want = oracle.render(sp, cam_np, W, H, 3, subframe=1, max_depth=6, mode=pyoracle.MODE_GB300)
+    want = oracle.render(sp, cam_np, W, H, 3, subframe=2, max_depth=6, mode=pyoracle.MODE_GB300,
+                         accum=want["accum"])
+    assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
+    assert np.array_equal(out.getHostFloat().reshape(-1, 4).view(np.uint32), want["image_f"].view(np.uint32))
+    # camera change resets the accumulation (Core/Renderer.h:37-45)
+    cam.MoveForward(0.1)
+    r.Draw(cam, out)
+    assert float(r.accum[:, 3].max()) == 3.0
+    r.Cleanup()
+
+
+def test_render_random_scene(venu, oracle, cuda):
+    sp = oracle.scene_random(20_000, 12)
+    W, H, spp = 64, 36, 2
+    cam = oracle.camera((60, 15, 60), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, spp, 0, 50)
+    want = oracle.render(sp, cam, W, H, spp, subframe=0, max_depth=50, mode=pyoracle.MODE_GB300)
+    assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
+    assert st["segments"] == want["segments"]
+
+
+def test_empty_and_tiny_scenes(venu, oracle, cuda):
+    W, H = 16, 9
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    for n in (0, 1, 2):
+        sp = oracle.scene_rtiow(0)[:n]
+        acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, 2, 0, 10)
+        want = oracle.render(sp, cam, W, H, 2, subframe=0, max_depth=10, mode=pyoracle.MODE_GB300)
+        assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))

@@ -1,0 +1,166 @@
+"""CPU tests: the oracle against the reference's own code and golden vectors.
+
+The oracle (oracle/venu_oracle.cpp) is pinned two ways:
+  * against tests/golden/golden.npz, made from the reference's Core/random.cuh
+    and Core/RayTracer.cu compiled for the host (tests/golden/make_golden.py);
+  * live against that same reference build (oracle/_ref) where it exists.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return np.load(GOLDEN)
+
+
+def _scene_cam(g):
+    spheres = g["scene"].reshape(-1).view(pyoracle.SPHERE_DTYPE)
+    cam = g["camera"].view(pyoracle.CAMERA_DTYPE)
+    W, H, SPP = (int(x) for x in g["wh_spp"])
+    return spheres, cam, W, H, SPP
+
+
+def test_rng_known_answers(oracle, g):
+    for (a, b), want in zip(g["rng_pairs"], g["rng_tea4"]):
+        assert oracle.tea4(int(a), int(b)) == int(want)
+    vals, states = oracle.rnd_stream(oracle.tea4(0, 1), 256)
+    assert np.array_equal(vals.view(np.uint32), g["rng_rnd"].view(np.uint32))
+    assert np.array_equal(states, g["rng_states"])
+    # the value quoted for tea<4>(0,1) then rnd: LCG state 3617041482, 0.592472672
+    assert int(states[0]) == 3617041482
+    assert abs(float(vals[0]) - 0.592472672) < 1e-9
+
+
+def test_ref_mode_matches_reference_golden(oracle, g):
+    spheres, cam, W, H, SPP = _scene_cam(g)
+    r = oracle.render(spheres, cam, W, H, SPP, subframe=0, max_depth=4, mode=pyoracle.MODE_REF)
+    assert np.array_equal(r["accum"].view(np.uint32), g["ref_s0_accum"].view(np.uint32))
+    assert np.abs(r["image8"].astype(int) - g["ref_s0_image8"].astype(int)).max() <= 1
+    # progressive subframe: lerp with the previous accumulation buffer
+    r3 = oracle.render(spheres, cam, W, H, 2, subframe=3, max_depth=4, mode=pyoracle.MODE_REF,
+                       accum=g["ref_s3_prior"].copy())
+    assert np.array_equal(r3["accum"].view(np.uint32), g["ref_s3_accum"].view(np.uint32))
+
+
+def test_gb300_mode_golden(oracle, g):
+    spheres, cam, W, H, SPP = _scene_cam(g)
+    for depth in (4, 50):
+        r = oracle.render(spheres, cam, W, H, SPP, subframe=1, max_depth=depth, mode=pyoracle.MODE_GB300)
+        assert np.array_equal(r["accum"].view(np.uint32), g[f"gb_d{depth}_accum"].view(np.uint32))
+        assert r["segments"] == int(g[f"gb_d{depth}_segments"][0])
+
+
+def test_lbvh_golden(oracle, g):
+    spheres, *_ = _scene_cam(g)
+    b = oracle.lbvh(spheres)
+    assert np.array_equal(b["keys"], g["bvh_keys"])
+    assert np.array_equal(b["ids"], g["bvh_ids"])
+    assert b["nodes"].view(np.uint8).tobytes() == g["bvh_nodes"].tobytes()
+
+
+@pytest.mark.skipif(not pyoracle.RefBuild.available(), reason="reference build (oracle/_ref) not present")
+def test_ref_mode_matches_reference_live(oracle):
+    R = pyoracle.RefBuild()
+    spheres = oracle.scene_rtiow(3)
+    for (W, H, spp, sub) in ((40, 30, 3, 0), (17, 9, 5, 2)):
+        cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+        prior = np.random.default_rng(W).random((W * H, 4)).astype(np.float32)
+        a = oracle.render(spheres, cam, W, H, spp, subframe=sub, max_depth=4, mode=pyoracle.MODE_REF,
+                          accum=prior.copy())
+        b = R.render(spheres, cam, W, H, spp, subframe=sub, accum=prior.copy())
+        assert np.array_equal(a["accum"].view(np.uint32), b["accum"].view(np.uint32))
+
+
+def test_lbvh_structure(oracle):
+    """Karras invariants: every slot is reached once; boxes contain children."""
+    for n in (2, 3, 7, 100, 2000):
+        sp = oracle.scene_random(n, 11) if n > 2 else oracle.scene_rtiow(0)[:n]
+        b = oracle.lbvh(sp)
+        keys, nodes = b["keys"], b["nodes"]
+        assert np.all(np.diff(keys.astype(np.int64)) >= 0)
+        assert sorted(b["ids"].tolist()) == list(range(n))
+        seen_leaf, seen_int = set(), {0}
+        stack = [0]
+        while stack:
+            i = stack.pop()
+            for c in (int(nodes[i]["left"]), int(nodes[i]["right"])):
+                if c < 0:
+                    seen_leaf.add(c & 0x7FFFFFFF)
+                    k = c & 0x7FFFFFFF
+                    s = sp[b["ids"][k]]
+                    assert np.all(nodes[i]["lo"] <= s["center"] - abs(s["radius"]))
+                    assert np.all(nodes[i]["hi"] >= s["center"] + abs(s["radius"]))
+                else:
+                    seen_int.add(c)
+                    stack.append(c)
+                    assert np.all(nodes[i]["lo"] <= nodes[c]["lo"])
+                    assert np.all(nodes[i]["hi"] >= nodes[c]["hi"])
+        assert seen_leaf == set(range(n)) and seen_int == set(range(n - 1))
+
+
+def test_duplicate_keys_tiebreak(oracle):
+    """Spheres sharing a Morton code keep index order (stable sort)."""
+    sp = oracle.scene_random(64, 5)
+    sp["center"][10:40] = sp["center"][10]
+    b = oracle.lbvh(sp)
+    same = [i for i in b["ids"] if 10 <= i < 40]
+    assert same == sorted(same)
+
+
+def test_bvh_traversal_matches_brute_force(oracle):
+    """FP32 LBVH closest hit vs FP32/FP64 brute force on random rays."""
+    rng = np.random.default_rng(1)
+    sp = oracle.scene_rtiow(0)
+    n = 20000
+    o = np.stack([rng.uniform(-12, 14, n), rng.uniform(0.01, 4, n), rng.uniform(-12, 12, n)], 1)
+    d = rng.normal(size=(n, 3))
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    idb, tb, front, nv, ns = oracle.trace_bvh(sp, rays)
+    id64, t64, disc, t2 = oracle.trace_fp64(sp, rays)
+    well = (id64 >= 0) & (disc > 1e-4) & (t2 > t64 * (1 + 1e-4))
+    assert (idb == id64)[well].all()
+    rel = np.abs(tb[well].astype(np.float64) - t64[well]) / t64[well]
+    assert rel.max() < 1e-5, rel.max()
+    assert ((idb == -1) == (id64 == -1)).mean() > 0.999
+
+
+def test_gb300_vs_ref_same_paths(oracle):
+    """The GB300 arithmetic and the reference arithmetic trace the same paths:
+    at the same seeds > 99% of samples agree within 1e-3, and the
+    image RMSE is far below the seed-to-seed noise.  (subframe 0: the
+    reference lerps subframe k > 0 with the previous buffer.)"""
+    sp = oracle.scene_rtiow(0)
+    W, H = 32, 18
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    a = oracle.render(sp, cam, W, H, 16, subframe=0, max_depth=4, mode=pyoracle.MODE_GB300, want_samples=True)
+    b = oracle.render(sp, cam, W, H, 16, subframe=0, max_depth=4, mode=pyoracle.MODE_REF, want_samples=True)
+    err = np.abs(a["samples"] - b["samples"]).max(axis=2)
+    assert (err <= 1e-3).mean() > 0.99, (err <= 1e-3).mean()
+    rmse = np.sqrt(((a["image_f"][:, :3] - b["accum"][:, :3]) ** 2).mean())
+    c = oracle.render(sp, cam, W, H, 16, subframe=0, max_depth=4, mode=pyoracle.MODE_REF)
+    d = oracle.render(sp, cam, W, H, 16, subframe=5, max_depth=4, mode=pyoracle.MODE_GB300)
+    noise = np.sqrt(((d["image_f"][:, :3] - c["accum"][:, :3]) ** 2).mean())
+    assert rmse < 0.25 * noise, (rmse, noise)
+
+
+def test_scene_generators_match_product(oracle, venu):
+    a = venu.generate_rtiow(0)
+    assert a.tobytes() == oracle.scene_rtiow(0).tobytes()
+    assert len(a) == 485
+    b = venu.generate_random(5000, 9)
+    assert b.tobytes() == oracle.scene_random(5000, 9).tobytes()
+    assert b["radius"][1:].min() >= 0.01 and b["radius"][1:].max() <= 0.5
+    frac = np.bincount(b["material"][1:], minlength=3) / (len(b) - 1)
+    assert abs(frac[0] - 0.8) < 0.03 and abs(frac[1] - 0.15) < 0.03
+
+
+def test_camera_matches_product(oracle, venu):
+    for args in (((13, 2, 3), (0, 0, 0), 20.0, 16 / 9, 0.1, 10.0), ((60, 15, 60), (0, 0, 0), 20.0, 1.0, 0.1, 10.0)):
+        assert venu.Camera.look_at(*args).tobytes() == oracle.camera(*args).tobytes()

@@ -1,0 +1,119 @@
+"""ctypes binding of libvenusaur_gb300.so (the C ABI in include/venu.h).
+
+There is no fallback: if the library is missing or does not load, every
+entry point raises VenuError.  Build it with ``python -c "import
+__graft_entry__ as g; g.build()"`` or ``python venusaur_gb300/build.py``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libvenusaur_gb300.so")
+
+SPHERE_DTYPE = np.dtype([
+    ("center", "<f4", (3,)), ("radius", "<f4"), ("albedo", "<f4", (3,)),
+    ("fuzz", "<f4"), ("ir", "<f4"), ("material", "<u4"), ("pad", "<u4", (2,)),
+])
+CAMERA_DTYPE = np.dtype([
+    ("origin", "<f4", (3,)), ("u", "<f4", (3,)), ("v", "<f4", (3,)),
+    ("w", "<f4", (3,)), ("lens_radius", "<f4"),
+])
+NODE_DTYPE = np.dtype([("lo", "<f4", (3,)), ("left", "<i4"), ("hi", "<f4", (3,)), ("right", "<i4")])
+
+STATUS = {
+    0: "VENU_OK", 1: "VENU_ERR_INVALID", 2: "VENU_ERR_CUDA", 3: "VENU_ERR_OOM",
+    4: "VENU_ERR_NO_DEVICE", 5: "VENU_ERR_STACK", 6: "VENU_ERR_TIMEOUT",
+    7: "VENU_ERR_CANCELLED", 8: "VENU_ERR_TOO_LARGE", 9: "VENU_ERR_NOT_READY",
+}
+FLAG_RESET_ACCUM = 1
+RENDERER_COUNT = 1
+RENDERER_PROFILE = 2
+ACCUM_FLOATS = 8
+
+
+class VenuError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class RenderOpts(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("samples_per_pixel", C.c_uint32),
+                ("subframe_index", C.c_uint32), ("max_depth", C.c_uint32), ("flags", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_spheres", C.c_uint32), ("num_nodes", C.c_uint32), ("device_bytes", C.c_uint64),
+                ("bounds", C.c_float * 6), ("build_ms", C.c_float)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("segments", C.c_uint64), ("paths", C.c_uint64), ("waves", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("nodes_visited", C.c_uint64),
+                ("spheres_tested", C.c_uint64), ("traverse_ms", C.c_float), ("shade_ms", C.c_float),
+                ("traverse_launches", C.c_uint32), ("shade_launches", C.c_uint32)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads the library once; raises VenuError if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise VenuError(4, f"{LIB_PATH} is missing: build the CUDA library first "
+                           "(python venusaur_gb300/build.py)")
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    u32 = C.c_uint32
+    L.venu_last_error.restype = C.c_char_p
+    L.venu_scene_generate_rtiow.restype = u32
+    L.venu_scene_generate_rtiow.argtypes = [u32, vp, u32]
+    L.venu_scene_generate_random.argtypes = [u32, u32, vp, vp, C.c_float, C.c_float, vp]
+    L.venu_camera_look_at.restype = None
+    L.venu_camera_look_at.argtypes = [vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+    L.venu_camera_frame.restype = None
+    L.venu_camera_frame.argtypes = [vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+    L.venu_device_check.argtypes = [vp, vp, vp]
+    L.venu_scene_create.argtypes = [vp, u32, vp, C.POINTER(vp)]
+    L.venu_scene_create_device.argtypes = [vp, u32, vp, C.POINTER(vp)]
+    L.venu_scene_info_get.argtypes = [vp, C.POINTER(SceneInfo)]
+    L.venu_scene_export_bvh.argtypes = [vp, vp, vp, vp]
+    L.venu_scene_destroy.argtypes = [vp]
+    L.venu_trace.argtypes = [vp, vp, u32, C.c_float, C.c_float, vp, vp, vp, vp]
+    L.venu_renderer_create.argtypes = [u32, u32, C.POINTER(vp)]
+    L.venu_render.argtypes = [vp, vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp]
+    L.venu_renderer_stats.argtypes = [vp, C.POINTER(RenderStats)]
+    L.venu_renderer_destroy.argtypes = [vp]
+    for name in ("venu_device_check", "venu_scene_generate_random", "venu_scene_create",
+                 "venu_scene_create_device", "venu_scene_info_get", "venu_scene_export_bvh",
+                 "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
+                 "venu_renderer_stats", "venu_renderer_destroy"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != 0:
+        msg = lib().venu_last_error()
+        raise VenuError(status, msg.decode() if msg else "")
+
+
+def ptr(a) -> C.c_void_p | None:
+    """Address of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    if isinstance(a, int):
+        return C.c_void_p(a)
+    raise TypeError(f"cannot take the address of {type(a)}")

@@ -1,0 +1,410 @@
+"""Python mirror of the reference's Core/ interface over the C ABI.
+
+Names follow the reference (Core/material.h, Core/sphere.h, Core/Scene.h,
+Core/camera.h, Core/CUDAOutputBuffer.h, Core/Renderer.h) so a user of
+Renderer::Init / Draw / Cleanup finds the same calls.  Device memory for the
+output and accumulation buffers is held in torch tensors (plumbing only); all
+compute runs in libvenusaur_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import CAMERA_DTYPE, NODE_DTYPE, SPHERE_DTYPE, RenderOpts, RenderStats, SceneInfo, check, lib, ptr
+
+
+def _torch():
+    import torch  # noqa: PLC0415  (imported lazily: only device buffers need it)
+    return torch
+
+
+def _stream_handle(stream=None):
+    """cudaStream_t of `stream` (default: torch's current stream).  Without a
+    CUDA device this is NULL and the library itself reports the missing
+    device (VENU_ERR_NO_DEVICE)."""
+    if stream is not None:
+        return C.c_void_p(stream.cuda_stream)
+    torch = _torch()
+    if not torch.cuda.is_available():
+        return None
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ---------------------------------------------------------------------------
+# Material / Sphere (Core/material.h:6-33, Core/sphere.h:5-36)
+# ---------------------------------------------------------------------------
+class Material:
+    Lambertian = 0
+    Metal = 1
+    Dielectric = 2
+
+    def __init__(self, type: int, albedo=(0.0, 0.0, 0.0), fuzz: float = 0.0, ir: float = 0.0):
+        self.m_type = int(type)
+        self.m_albedo = tuple(float(np.float32(a)) for a in albedo)
+        self.m_fuzz = float(np.float32(fuzz))
+        self.m_ir = float(np.float32(ir))
+
+    def GetType(self) -> int:
+        return self.m_type
+
+    def GetAlbedo(self):
+        return self.m_albedo
+
+    def GetFuzz(self) -> float:
+        return self.m_fuzz
+
+    def GetIR(self) -> float:
+        return self.m_ir
+
+
+class Sphere:
+    def __init__(self, center, radius: float, material: Material):
+        self.m_center = tuple(float(np.float32(c)) for c in center)
+        self.m_radius = float(np.float32(radius))
+        self.m_material = material
+
+    def GetCenter(self):
+        return self.m_center
+
+    def GetRadius(self) -> float:
+        return self.m_radius
+
+    def GetMaterial(self) -> Material:
+        return self.m_material
+
+    def SetMaterial(self, material: Material) -> None:
+        self.m_material = material
+
+    def GetAABB(self):
+        """Core/sphere.h:17-28, using |radius| (the reference computes it and
+        then ignores it)."""
+        r = abs(self.m_radius)
+        c = self.m_center
+        return (c[0] - r, c[1] - r, c[2] - r, c[0] + r, c[1] + r, c[2] + r)
+
+
+def spheres_to_array(spheres) -> np.ndarray:
+    a = np.zeros(len(spheres), SPHERE_DTYPE)
+    for i, s in enumerate(spheres):
+        m = s.GetMaterial()
+        a[i]["center"] = s.GetCenter()
+        a[i]["radius"] = s.GetRadius()
+        a[i]["albedo"] = m.GetAlbedo()
+        a[i]["fuzz"] = m.GetFuzz()
+        a[i]["ir"] = m.GetIR()
+        a[i]["material"] = m.GetType()
+    return a
+
+
+def array_to_spheres(a: np.ndarray):
+    out = []
+    for r in a:
+        m = Material(int(r["material"]), tuple(r["albedo"]), float(r["fuzz"]), float(r["ir"]))
+        out.append(Sphere(tuple(r["center"]), float(r["radius"]), m))
+    return out
+
+
+def generate_rtiow(seed: int = 0) -> np.ndarray:
+    buf = np.zeros(600, SPHERE_DTYPE)
+    n = lib().venu_scene_generate_rtiow(seed, ptr(buf), len(buf))
+    return buf[:n].copy()
+
+
+def generate_random(n: int, seed: int = 0, box_lo=(-100.0, 0.0, -100.0), box_hi=(100.0, 20.0, 100.0),
+                    rmin: float = 0.01, rmax: float = 0.5) -> np.ndarray:
+    out = np.zeros(n, SPHERE_DTYPE)
+    lo = np.asarray(box_lo, np.float32)
+    hi = np.asarray(box_hi, np.float32)
+    check(lib().venu_scene_generate_random(n, seed, ptr(lo), ptr(hi), rmin, rmax, ptr(out)))
+    return out
+
+
+class Scene:
+    """Core/Scene.h: the default constructor builds the RTIOW final scene."""
+
+    def __init__(self, seed: int = 0, spheres=None):
+        if spheres is None:
+            self.spheres = generate_rtiow(seed)
+        elif isinstance(spheres, np.ndarray):
+            self.spheres = np.ascontiguousarray(spheres, SPHERE_DTYPE)
+        else:
+            self.spheres = spheres_to_array(spheres)
+
+    @classmethod
+    def random(cls, n: int, seed: int = 0, **kw) -> "Scene":
+        return cls(spheres=generate_random(n, seed, **kw))
+
+    @property
+    def m_spheres(self):
+        return array_to_spheres(self.spheres)
+
+    @property
+    def m_aabbs(self) -> np.ndarray:
+        c = self.spheres["center"]
+        r = np.abs(self.spheres["radius"])[:, None]
+        return np.concatenate([c - r, c + r], axis=1)
+
+    @property
+    def m_indices(self) -> np.ndarray:
+        return np.arange(len(self.spheres), dtype=np.uint32)
+
+    def __len__(self) -> int:
+        return len(self.spheres)
+
+
+# ---------------------------------------------------------------------------
+# Camera (Core/camera.h, Core/Camera.cpp)
+# ---------------------------------------------------------------------------
+class Camera:
+    m_defaultForward = (0.0, 0.0, -1.0)
+
+    def __init__(self, origin=(0.0, 0.0, 0.0), vfov: float = 45.0, aspect: float = 1.6,
+                 aperture: float = 0.0, focalLength: float = 1.0):
+        self.m_position = np.asarray(origin, np.float32)
+        self.m_forward = np.asarray(self.m_defaultForward, np.float32)
+        self.m_vfov = np.float32(vfov)
+        self.m_aspect = np.float32(aspect)
+        self.m_aperture = np.float32(aperture)
+        self.m_focalLength = np.float32(focalLength)
+        self.m_changed = True
+
+    def SetForward(self, direction) -> None:
+        d = np.asarray(direction, np.float32)
+        dot = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+        inv = np.float32(1.0) / np.sqrt(dot)
+        self.m_forward = (d * inv).astype(np.float32)
+        self.m_changed = True
+
+    def GetLensRadius(self) -> float:
+        return float(self.m_aperture * np.float32(0.5))
+
+    def GetPosition(self):
+        return self.m_position.copy()
+
+    def GetFocalLength(self) -> float:
+        return float(self.m_focalLength)
+
+    def SetFocalLength(self, length: float) -> None:
+        if self.m_focalLength != np.float32(length):
+            self.m_focalLength = np.float32(length)
+            self.m_changed = True
+
+    def MoveForward(self, speed: float) -> None:
+        self.m_position = (self.m_position + self.m_forward * np.float32(speed)).astype(np.float32)
+        self.m_changed = True
+
+    def Changed(self) -> bool:
+        c = self.m_changed
+        self.m_changed = False
+        return c
+
+    def params(self) -> np.ndarray:
+        """The venu_camera record (Params origin/u/v/w/lens_radius)."""
+        cam = np.zeros(1, CAMERA_DTYPE)
+        e = np.ascontiguousarray(self.m_position, np.float32)
+        f = np.ascontiguousarray(self.m_forward, np.float32)
+        lib().venu_camera_frame(ptr(e), ptr(f), float(self.m_vfov), float(self.m_aspect),
+                                float(self.m_aperture), float(self.m_focalLength), ptr(cam))
+        return cam
+
+    def UVWFrame(self):
+        c = self.params()[0]
+        return c["u"].copy(), c["v"].copy(), c["w"].copy()
+
+    @staticmethod
+    def look_at(eye, lookat, vfov, aspect, aperture, focal) -> np.ndarray:
+        cam = np.zeros(1, CAMERA_DTYPE)
+        e = np.asarray(eye, np.float32)
+        l = np.asarray(lookat, np.float32)
+        lib().venu_camera_look_at(ptr(e), ptr(l), float(vfov), float(aspect), float(aperture),
+                                  float(focal), ptr(cam))
+        return cam
+
+
+# ---------------------------------------------------------------------------
+# Device scene (LBVH) and closest-hit queries
+# ---------------------------------------------------------------------------
+class DeviceScene:
+    """A venu_scene: spheres uploaded and the LBVH built on the device."""
+
+    def __init__(self, spheres, stream=None):
+        arr = spheres.spheres if isinstance(spheres, Scene) else np.ascontiguousarray(spheres, SPHERE_DTYPE)
+        self.spheres = arr
+        h = C.c_void_p()
+        check(lib().venu_scene_create(ptr(arr), len(arr), _stream_handle(stream), C.byref(h)))
+        self.handle = h
+
+    @classmethod
+    def from_device(cls, spheres_dev, n: int, stream=None) -> "DeviceScene":
+        self = cls.__new__(cls)
+        self.spheres = None
+        h = C.c_void_p()
+        check(lib().venu_scene_create_device(ptr(spheres_dev), n, _stream_handle(stream), C.byref(h)))
+        self.handle = h
+        return self
+
+    def info(self) -> dict:
+        si = SceneInfo()
+        check(lib().venu_scene_info_get(self.handle, C.byref(si)))
+        return dict(num_spheres=si.num_spheres, num_nodes=si.num_nodes, device_bytes=si.device_bytes,
+                    bounds=np.array(si.bounds[:], np.float32), build_ms=si.build_ms)
+
+    def export_bvh(self) -> dict:
+        n = self.info()["num_spheres"]
+        keys = np.zeros(n, np.uint32)
+        ids = np.zeros(n, np.uint32)
+        nodes = np.zeros(max(n - 1, 1), NODE_DTYPE)
+        check(lib().venu_scene_export_bvh(self.handle, ptr(keys), ptr(ids), ptr(nodes)))
+        return dict(keys=keys, ids=ids, nodes=nodes[: max(n - 1, 0)])
+
+    def trace(self, rays, tmin: float = 0.001, tmax: float = 1e16, stream=None):
+        """rays: (n, 6) float32 CUDA tensor -> (t, id, front) CUDA tensors."""
+        torch = _torch()
+        rays = rays.contiguous()
+        n = rays.shape[0]
+        t = torch.empty(n, dtype=torch.float32, device=rays.device)
+        idv = torch.empty(n, dtype=torch.int32, device=rays.device)
+        front = torch.empty(n, dtype=torch.int32, device=rays.device)
+        check(lib().venu_trace(self.handle, ptr(rays), n, tmin, tmax, ptr(t), ptr(idv), ptr(front),
+                               _stream_handle(stream)))
+        return t, idv, front
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().venu_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# The plain wavefront renderer
+# ---------------------------------------------------------------------------
+class Wavefront:
+    """A venu_renderer (queues sized for `max_paths` paths per wave)."""
+
+    def __init__(self, max_paths: int = 0, count: bool = False, profile: bool = False):
+        h = C.c_void_p()
+        flags = (_lib.RENDERER_COUNT if count else 0) | (_lib.RENDERER_PROFILE if profile else 0)
+        check(lib().venu_renderer_create(max_paths, flags, C.byref(h)))
+        self.handle = h
+
+    def render(self, scene: DeviceScene, camera: np.ndarray, width: int, height: int, spp: int,
+               accum, subframe: int = 0, max_depth: int = 4, reset: bool = False,
+               image_f=None, image8=None, stream=None) -> None:
+        o = RenderOpts(width, height, spp, subframe, max_depth, _lib.FLAG_RESET_ACCUM if reset else 0)
+        cam = np.ascontiguousarray(camera, CAMERA_DTYPE)
+        check(lib().venu_render(self.handle, scene.handle, ptr(cam), C.byref(o), ptr(accum), ptr(image_f),
+                                ptr(image8), _stream_handle(stream)))
+
+    def stats(self) -> dict:
+        s = RenderStats()
+        check(lib().venu_renderer_stats(self.handle, C.byref(s)))
+        return dict(segments=s.segments, paths=s.paths, waves=s.waves, kernel_launches=s.kernel_launches,
+                    nodes_visited=s.nodes_visited, spheres_tested=s.spheres_tested,
+                    traverse_ms=s.traverse_ms, shade_ms=s.shade_ms, traverse_launches=s.traverse_launches,
+                    shade_launches=s.shade_launches)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().venu_renderer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def new_accum(width: int, height: int, device="cuda"):
+    torch = _torch()
+    return torch.zeros((height * width, _lib.ACCUM_FLOATS), dtype=torch.float32, device=device)
+
+
+# ---------------------------------------------------------------------------
+# CUDAOutputBuffer (CUDA_DEVICE mode) and Renderer (Core/Renderer.h:22-97)
+# ---------------------------------------------------------------------------
+class CUDAOutputBuffer:
+    """Device pixel buffer (Core/CUDAOutputBuffer.h, CUDA_DEVICE mode only:
+    there is no GL interop).  Holds sRGB RGBA8 and linear RGBA32F images."""
+
+    def __init__(self, width: int, height: int, device="cuda"):
+        self.m_device = device
+        self.resize(width, height)
+
+    def resize(self, width: int, height: int) -> None:
+        torch = _torch()
+        self.m_width = max(1, int(width))
+        self.m_height = max(1, int(height))
+        self.pixels = torch.zeros((self.m_height, self.m_width, 4), dtype=torch.uint8, device=self.m_device)
+        self.pixels_f = torch.zeros((self.m_height, self.m_width, 4), dtype=torch.float32, device=self.m_device)
+
+    def width(self) -> int:
+        return self.m_width
+
+    def height(self) -> int:
+        return self.m_height
+
+    def map(self):
+        return self.pixels
+
+    def unmap(self) -> None:
+        _torch().cuda.current_stream().synchronize()
+
+    def getHostPointer(self) -> np.ndarray:
+        return self.pixels.cpu().numpy()
+
+    def getHostFloat(self) -> np.ndarray:
+        return self.pixels_f.cpu().numpy()
+
+
+class Renderer:
+    """Renderer::Init / Draw / Cleanup over the wavefront kernels.
+
+    Draw renders `samples_per_pixel` samples per pixel (16, as
+    Core/Renderer.h:53) seeded with tea<4>(pixel, subframe_index) and adds
+    them to a Kahan-compensated accumulator; a camera change resets it and
+    restarts subframe_index at 1, as Core/Renderer.h:37-54 does.
+    """
+
+    def __init__(self, samples_per_pixel: int = 16, max_depth: int = 4, max_paths: int = 0):
+        self.samples_per_pixel = samples_per_pixel
+        self.max_depth = max_depth
+        self.max_paths = max_paths
+        self.scene = None
+        self.wave = None
+        self.accum = None
+        self.subframe_index = 0
+
+    def Init(self, scene: Scene, ptxSource: str | None = None) -> None:
+        """ptxSource is accepted for signature parity and ignored (no PTX JIT)."""
+        self.scene = DeviceScene(scene)
+        self.wave = Wavefront(self.max_paths)
+
+    def Draw(self, camera: Camera, outputBuffer: CUDAOutputBuffer) -> None:
+        W, H = outputBuffer.width(), outputBuffer.height()
+        reset = False
+        if camera.Changed() or self.accum is None or self.accum.shape[0] != W * H:
+            self.accum = new_accum(W, H, outputBuffer.m_device)
+            self.subframe_index = 0
+            reset = True
+        self.subframe_index += 1
+        self.wave.render(self.scene, camera.params(), W, H, self.samples_per_pixel, self.accum,
+                         subframe=self.subframe_index, max_depth=self.max_depth, reset=reset,
+                         image_f=outputBuffer.pixels_f, image8=outputBuffer.pixels)
+        outputBuffer.unmap()
+
+    def Cleanup(self) -> None:
+        if self.wave is not None:
+            self.wave.close()
+        if self.scene is not None:
+            self.scene.close()
+        self.wave = self.scene = self.accum = None

@@ -1,0 +1,374 @@
+// lbvh.cu -- linear BVH over spheres, built on the device.
+//
+// Replaces Renderer::BuildAccelerationStructures (Core/Renderer.h:160-255):
+//   1. centroid bounds (order-preserving integer atomics: exact min/max),
+//   2. 30-bit Morton codes of the centroids quantised to 10 bits per axis,
+//   3. stable LSD radix sort of (code, original index), 4 passes of 8 bits,
+//      one warp per 512-key tile, stable ranking with __match_any_sync,
+//   4. Karras 2012 hierarchy ("Maximizing Parallelism in the Construction of
+//      BVHs, Octrees, and k-d Trees"), ties on equal codes broken by index,
+//   5. bottom-up refit with per-node arrival counters; leaf boxes are the
+//      sphere AABBs rounded outward (__fsub_rd / __fadd_ru, |radius|),
+//   6. gather of spheres and materials into Morton (slot) order.
+// Every step is integer work or exact float min/max, so the result is
+// bit-identical to a host build of the same algorithm.
+#include "venu_device.cuh"
+#include "venu_internal.h"
+
+#include <vector>
+
+namespace venu {
+namespace {
+
+constexpr int kTileKeys = 512;  // keys per warp tile
+constexpr int kWarpsPerBlock = 8;
+constexpr int kRadixBits = 8;
+constexpr int kBuckets = 1 << kRadixBits;
+
+__device__ __forceinline__ uint32_t f2u(float f) {
+    uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float u2f(uint32_t u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+__global__ void k_bounds(const venu_sphere* __restrict__ s, uint32_t n, uint32_t* __restrict__ bu) {
+    uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0, 0, 0};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            uint32_t u = f2u(s[i].center[a]);
+            lo[a] = min(lo[a], u);
+            hi[a] = max(hi[a], u);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(bu + a, lo[a]);
+            atomicMax(bu + 3 + a, hi[a]);
+        }
+    }
+}
+
+// Karras's bit spreading: bit i of v goes to bit 3i.
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+    v &= 0x3ffu;
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+__device__ __forceinline__ uint32_t quant10(float c, float lo, float ext) {
+    if (!(ext > 0.0f)) return 0;
+    float t = (c - lo) / ext;
+    float f = t * 1024.0f;
+    f = fminf(fmaxf(f, 0.0f), 1023.0f);
+    return (uint32_t)f;
+}
+
+__global__ void k_morton(const venu_sphere* __restrict__ s, uint32_t n, const uint32_t* __restrict__ bu,
+                         float* __restrict__ bounds_out, uint32_t* __restrict__ keys,
+                         uint32_t* __restrict__ vals) {
+    float lo[3], ext[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = u2f(bu[a]);
+        float hi = u2f(bu[3 + a]);
+        ext[a] = hi - lo[a];
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            bounds_out[a] = lo[a];
+            bounds_out[3 + a] = hi;
+        }
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t qx = quant10(s[i].center[0], lo[0], ext[0]);
+        uint32_t qy = quant10(s[i].center[1], lo[1], ext[1]);
+        uint32_t qz = quant10(s[i].center[2], lo[2], ext[2]);
+        keys[i] = (spread10(qx) << 2) | (spread10(qy) << 1) | spread10(qz);
+        vals[i] = i;
+    }
+}
+
+// Per-tile digit histogram, digit-major: hist[d * ntiles + tile].
+__global__ void k_hist(const uint32_t* __restrict__ keys, uint32_t n, int shift, uint32_t ntiles,
+                       uint32_t* __restrict__ hist) {
+    __shared__ uint32_t cnt[kWarpsPerBlock][kBuckets];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tile = blockIdx.x * kWarpsPerBlock + w;
+    for (int d = lane; d < kBuckets; d += 32) cnt[w][d] = 0;
+    __syncwarp();
+    if (tile < ntiles) {
+        for (int j = 0; j < kTileKeys / 32; ++j) {
+            uint32_t idx = tile * kTileKeys + j * 32 + lane;
+            if (idx < n) atomicAdd(&cnt[w][(keys[idx] >> shift) & (kBuckets - 1)], 1u);
+        }
+        __syncwarp();
+        for (int d = lane; d < kBuckets; d += 32) hist[(size_t)d * ntiles + tile] = cnt[w][d];
+    }
+}
+
+// Exclusive scan of `total` counters in place (one block of 1024 threads).
+__global__ void k_scan(uint32_t* __restrict__ a, uint32_t total) {
+    __shared__ uint32_t part[1024];
+    const uint32_t t = threadIdx.x;
+    const uint32_t per = (total + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = t * per, e = min(total, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += a[i];
+    part[t] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        uint32_t v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[t] - sum;  // exclusive prefix of this thread's chunk
+    for (uint32_t i = b; i < e; ++i) {
+        uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
+// Stable scatter: keys of a tile are ranked in tile order within their digit.
+__global__ void k_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t n,
+                          int shift, uint32_t ntiles, const uint32_t* __restrict__ offs,
+                          uint32_t* __restrict__ kout, uint32_t* __restrict__ vout) {
+    __shared__ uint32_t base[kWarpsPerBlock][kBuckets];
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tile = blockIdx.x * kWarpsPerBlock + w;
+    if (tile >= ntiles) return;  // whole warp leaves together
+    for (int d = lane; d < kBuckets; d += 32) base[w][d] = offs[(size_t)d * ntiles + tile];
+    __syncwarp();
+    const uint32_t lt = (1u << lane) - 1u;
+    for (int j = 0; j < kTileKeys / 32; ++j) {
+        uint32_t idx = tile * kTileKeys + j * 32 + lane;
+        bool valid = idx < n;
+        uint32_t k = valid ? kin[idx] : 0u;
+        uint32_t d = valid ? ((k >> shift) & (kBuckets - 1)) : (uint32_t)kBuckets + lane;
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t rank = __popc(peers & lt);
+        uint32_t pos = valid ? base[w][d] + rank : 0u;
+        __syncwarp();
+        if (valid && rank == 0) base[w][d] += __popc(peers);
+        __syncwarp();
+        if (valid) {
+            kout[pos] = k;
+            vout[pos] = vin[idx];
+        }
+    }
+}
+
+__device__ __forceinline__ int delta(const uint32_t* __restrict__ k, int n, int i, int j) {
+    if (j < 0 || j > n - 1) return -1;
+    uint32_t a = k[i], b = k[j];
+    if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+// One thread per internal node i in [0, n-2].
+__global__ void k_karras(const uint32_t* __restrict__ keys, int n, float4* __restrict__ nodes,
+                         int32_t* __restrict__ parent_int, int32_t* __restrict__ parent_leaf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, n, i, i - d);
+    int lmax = 2;
+    while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(keys, n, i, j);
+    int s = 0;
+    int t = l;
+    do {
+        t = (t + 1) >> 1;  // ceil(l/2), ceil(l/4), ..., 1
+        if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + min(d, 0);
+    int left = (min(i, j) == gamma) ? (gamma | kLeaf) : gamma;
+    int right = (max(i, j) == gamma + 1) ? ((gamma + 1) | kLeaf) : gamma + 1;
+    nodes[2 * i].w = __int_as_float(left);
+    nodes[2 * i + 1].w = __int_as_float(right);
+    if (left & kLeaf) parent_leaf[left & ~kLeaf] = i; else parent_int[left] = i;
+    if (right & kLeaf) parent_leaf[right & ~kLeaf] = i; else parent_int[right] = i;
+    if (i == 0) parent_int[0] = -1;
+}
+
+// Leaf boxes + bottom-up refit.  The second thread to arrive at a node
+// computes its box; a __threadfence before each arrival publishes the
+// children's boxes, and they are read back through L2 (__ldcg).
+__global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __restrict__ vals, int n,
+                        float4* nodes, const int32_t* __restrict__ parent_int,
+                        const int32_t* __restrict__ parent_leaf, float4* leafbox,
+                        uint32_t* __restrict__ arrive) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const venu_sphere& sp = s[vals[k]];
+    float r = fabsf(sp.radius);
+    float4 lo = make_float4(__fsub_rd(sp.center[0], r), __fsub_rd(sp.center[1], r), __fsub_rd(sp.center[2], r), 0.0f);
+    float4 hi = make_float4(__fadd_ru(sp.center[0], r), __fadd_ru(sp.center[1], r), __fadd_ru(sp.center[2], r), 0.0f);
+    leafbox[2 * k] = lo;
+    leafbox[2 * k + 1] = hi;
+    int p = parent_leaf[k];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(arrive + p, 1u) == 0u) return;
+        __threadfence();
+        int32_t cl = __float_as_int(__ldcg(&nodes[2 * p].w));
+        int32_t cr = __float_as_int(__ldcg(&nodes[2 * p + 1].w));
+        float4 l0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf)) : __ldcg(nodes + 2 * cl);
+        float4 h0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf) + 1) : __ldcg(nodes + 2 * cl + 1);
+        float4 l1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & ~kLeaf)) : __ldcg(nodes + 2 * cr);
+        float4 h1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & ~kLeaf) + 1) : __ldcg(nodes + 2 * cr + 1);
+        nodes[2 * p] = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), __int_as_float(cl));
+        nodes[2 * p + 1] = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), __int_as_float(cr));
+        p = parent_int[p];
+    }
+}
+
+__global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* __restrict__ vals, uint32_t n,
+                         float4* __restrict__ sph, float4* __restrict__ mat, uint32_t* __restrict__ meta) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t id = vals[k];
+    const venu_sphere& sp = s[id];
+    uint32_t type = sp.material > 2u ? 2u : sp.material;
+    sph[k] = make_float4(sp.center[0], sp.center[1], sp.center[2], sp.radius);
+    float param = type == 1u ? sp.fuzz : (type == 2u ? sp.ir : 0.0f);
+    mat[k] = make_float4(sp.albedo[0], sp.albedo[1], sp.albedo[2], param);
+    meta[k] = id | (type << 30);
+}
+
+inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+}  // namespace
+
+void free_scene(venu_scene* s) {
+    if (!s) return;
+    cudaFree(s->nodes);
+    cudaFree(s->sph);
+    cudaFree(s->mat);
+    cudaFree(s->meta);
+    cudaFree(s->keys);
+    s->nodes = nullptr;
+    s->sph = s->mat = nullptr;
+    s->meta = s->keys = nullptr;
+}
+
+venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t st, venu_scene* S) {
+    S->n = n;
+    if (n == 0) return VENU_OK;
+    if (n > (1u << 30)) {
+        set_error("venu_scene_create: more than 2^30 spheres");
+        return VENU_ERR_TOO_LARGE;
+    }
+    const uint32_t ntiles = cdiv(n, kTileKeys);
+    const size_t hist_n = (size_t)kBuckets * ntiles;
+    // persistent buffers
+    size_t bytes = 0;
+    auto alloc = [&](void** p, size_t b) -> cudaError_t {
+        bytes += b;
+        return cudaMalloc(p, b ? b : 16);
+    };
+    uint32_t nint = n > 1 ? n - 1 : 1;
+    VENU_CUDA(alloc((void**)&S->nodes, sizeof(float4) * 2 * nint));
+    VENU_CUDA(alloc((void**)&S->sph, sizeof(float4) * n));
+    VENU_CUDA(alloc((void**)&S->mat, sizeof(float4) * n));
+    VENU_CUDA(alloc((void**)&S->meta, sizeof(uint32_t) * n));
+    VENU_CUDA(alloc((void**)&S->keys, sizeof(uint32_t) * n));
+    S->bytes = bytes;
+    // scratch
+    uint32_t *bu = nullptr, *keys_alt = nullptr, *vals = nullptr, *vals_alt = nullptr, *hist = nullptr,
+             *arrive = nullptr;
+    int32_t *pint = nullptr, *pleaf = nullptr;
+    float4* leafbox = nullptr;
+    float* bounds_dev = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    venu_status rc = VENU_OK;
+    auto fail = [&](cudaError_t e, const char* what) {
+        rc = cuda_fail(e, what);
+    };
+#define STEP(call)                              \
+    do {                                        \
+        cudaError_t _e = (call);                \
+        if (_e != cudaSuccess) {                \
+            fail(_e, #call);                    \
+            goto done;                          \
+        }                                       \
+    } while (0)
+    STEP(cudaMalloc(&bu, 6 * sizeof(uint32_t) + 6 * sizeof(float)));
+    bounds_dev = reinterpret_cast<float*>(bu + 6);
+    STEP(cudaMalloc(&keys_alt, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&vals, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&vals_alt, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&hist, sizeof(uint32_t) * hist_n));
+    STEP(cudaMalloc(&arrive, sizeof(uint32_t) * nint));
+    STEP(cudaMalloc(&pint, sizeof(int32_t) * nint));
+    STEP(cudaMalloc(&pleaf, sizeof(int32_t) * n));
+    STEP(cudaMalloc(&leafbox, sizeof(float4) * 2 * n));
+    STEP(cudaEventCreate(&e0));
+    STEP(cudaEventCreate(&e1));
+    STEP(cudaEventRecord(e0, st));
+    {
+        const uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+        STEP(cudaMemcpyAsync(bu, init, sizeof(init), cudaMemcpyHostToDevice, st));
+        STEP(cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * nint, st));
+        STEP(cudaMemsetAsync(pleaf, 0xff, sizeof(int32_t) * n, st));
+        STEP(cudaMemsetAsync(pint, 0xff, sizeof(int32_t) * nint, st));
+        const uint32_t blocks = std::min(cdiv(n, 256), (uint32_t)(sm_count() * 8));
+        k_bounds<<<blocks, 256, 0, st>>>(spheres_dev, n, bu);
+        k_morton<<<blocks, 256, 0, st>>>(spheres_dev, n, bu, bounds_dev, S->keys, vals);
+        uint32_t *kin = S->keys, *kout = keys_alt, *vin = vals, *vout = vals_alt;
+        const uint32_t sblocks = cdiv(ntiles, kWarpsPerBlock);
+        for (int shift = 0; shift < 32; shift += kRadixBits) {
+            k_hist<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, n, shift, ntiles, hist);
+            k_scan<<<1, 1024, 0, st>>>(hist, (uint32_t)hist_n);
+            k_scatter<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, vin, n, shift, ntiles, hist, kout, vout);
+            std::swap(kin, kout);
+            std::swap(vin, vout);
+        }
+        // 4 passes: sorted data is back in S->keys / vals.
+        if (n > 1) {
+            k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(S->keys, (int)n, S->nodes, pint, pleaf);
+            k_refit<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, (int)n, S->nodes, pint, pleaf, leafbox, arrive);
+        }
+        k_gather<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, n, S->sph, S->mat, S->meta);
+        STEP(cudaGetLastError());
+        STEP(cudaEventRecord(e1, st));
+        STEP(cudaMemcpyAsync(S->bounds, bounds_dev, 6 * sizeof(float), cudaMemcpyDeviceToHost, st));
+        STEP(cudaStreamSynchronize(st));
+        float ms = 0.0f;
+        STEP(cudaEventElapsedTime(&ms, e0, e1));
+        S->build_ms = ms;
+    }
+#undef STEP
+done:
+    cudaFree(bu);
+    cudaFree(keys_alt);
+    cudaFree(vals);
+    cudaFree(vals_alt);
+    cudaFree(hist);
+    cudaFree(arrive);
+    cudaFree(pint);
+    cudaFree(pleaf);
+    cudaFree(leafbox);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return rc;
+}
+
+}  // namespace venu

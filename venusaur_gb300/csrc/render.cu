@@ -1,0 +1,469 @@
+// render.cu -- the plain single-scene wavefront renderer.
+//
+// Replaces Renderer::Draw (Core/Renderer.h:35-78) and the OptiX programs of
+// Core/RayTracer.cu.  A render call is cut into waves of up to max_paths
+// paths (pixels x a run of consecutive samples).  Per wave:
+//   raygen     one thread per pixel, the wave's samples in order;
+//   bounce b   traverse (closest hit for every queued ray)
+//              shade    (scatter; survivors compacted into the next queue
+//                        with __ballot_sync + a warp prefix, finished paths
+//                        write their radiance to their sample slot);
+//   accumulate one thread per pixel, Kahan-adds the wave's samples in
+//              sample order.
+// A resolve pass writes the running mean (RGBA32F) and sRGB RGBA8.
+// Queue counts live on the device; the host never waits inside a render.
+#include "render_kernels.cuh"
+#include "venu_internal.h"
+
+#include <algorithm>
+#include <vector>
+
+namespace venu {
+
+__global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, uint32_t P, uint32_t s0,
+                         uint32_t k, uint32_t subframe, int max_depth, uint32_t* __restrict__ seeds,
+                         Queue q, uint32_t* __restrict__ cnt, uint32_t* __restrict__ work, int nbounce) {
+    const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl == 0) {
+        cnt[0] = P * k;
+        for (int b = 1; b <= nbounce; ++b) cnt[b] = 0;
+        for (int b = 0; b <= nbounce; ++b) work[b] = 0;
+    }
+    if (pl >= P) return;
+    const DevCamera C = load_camera(cam);
+    const uint32_t pix = p0 + pl;
+    const uint32_t x = pix % W, y = pix / W;
+    uint32_t seed = (s0 == 0) ? tea4(pix, subframe) : seeds[pix];
+    for (uint32_t s = 0; s < k; ++s) {
+        f3 o, d;
+        camera_ray(C, x, y, W, H, seed, o, d);
+        const uint32_t pos = s * P + pl;
+        write_primary(q, pos, o, d, pos, max_depth - 1, seed);
+    }
+    seeds[pix] = seed;
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
+                                                  uint32_t* __restrict__ work, int2* __restrict__ hits,
+                                                  uint32_t* __restrict__ err,
+                                                  unsigned long long* __restrict__ stats) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.pair = reinterpret_cast<int2*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    const uint32_t n = *cnt;
+    const uint32_t lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        if (i < n) {
+            float4 o4 = q.o[i], d4 = q.d[i];
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float t;
+            int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            hits[i] = make_int2(__float_as_int(t), k);
+        }
+    }
+    if (overflow) atomicOr(err, 1u);
+    if (COUNT) {
+        unsigned long long a = K.nodes, b = K.spheres;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+        }
+        if (lane == 0) {
+            atomicAdd(stats + 1, a);
+            atomicAdd(stats + 2, b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
+                                               const uint32_t* __restrict__ cnt_in, Queue qout,
+                                               uint32_t* __restrict__ cnt_out, float4* __restrict__ slots) {
+    const uint32_t n = *cnt_in;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const uint32_t i = base + lane;
+        ShadeOut r;
+        r.cont = false;
+        uint32_t slot = 0;
+        const bool valid = i < n;
+        if (valid) {
+            float4 o4 = qin.o[i], d4 = qin.d[i], t4 = qin.t[i];
+            slot = (uint32_t)__float_as_int(o4.w);
+            r = shade_one(S, o4, d4, t4, hits[i]);
+        }
+        const uint32_t pos = warp_append(r.cont, cnt_out);
+        if (r.cont) {
+            qout.o[pos] = r.o;
+            qout.d[pos] = r.d;
+            qout.t[pos] = r.t;
+        } else if (valid) {
+            slots[slot] = r.result;
+        }
+    }
+}
+
+// Kahan-adds samples [0, k) of pixels [p0, p0+P) from their slots, in order.
+__global__ void k_accumulate(const float4* __restrict__ slots, uint32_t p0, uint32_t P, uint32_t k,
+                             float4* __restrict__ accum) {
+    const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pl >= P) return;
+    const uint32_t pix = p0 + pl;
+    float4 a0 = accum[2 * (size_t)pix], a1 = accum[2 * (size_t)pix + 1];
+    for (uint32_t s = 0; s < k; ++s) kahan_add(a0, a1, slots[(size_t)s * P + pl]);
+    accum[2 * (size_t)pix] = a0;
+    accum[2 * (size_t)pix + 1] = a1;
+}
+
+__global__ void k_resolve(const float4* __restrict__ accum, uint32_t npix, float4* __restrict__ image_f,
+                          uchar4* __restrict__ image8) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    float4 a0 = accum[2 * (size_t)pix];
+    f3 mean = mk(a0.x / a0.w, a0.y / a0.w, a0.z / a0.w);
+    if (image_f) image_f[pix] = make_float4(mean.x, mean.y, mean.z, 1.0f);
+    if (image8) image8[pix] = make_color(mean);
+}
+
+// Arbitrary rays -> closest hit (t, original id, front face).
+__global__ void __launch_bounds__(128) k_trace_rays(SceneView S, const float* __restrict__ rays, uint32_t n,
+                                                    float tmin, float tmax, float* __restrict__ t_out,
+                                                    int32_t* __restrict__ id_out, uint32_t* __restrict__ front_out,
+                                                    uint32_t* __restrict__ err) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.pair = reinterpret_cast<int2*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 o = mk(rays[6 * (size_t)i], rays[6 * (size_t)i + 1], rays[6 * (size_t)i + 2]);
+    f3 d = mk(rays[6 * (size_t)i + 3], rays[6 * (size_t)i + 4], rays[6 * (size_t)i + 5]);
+    RayPre R = prep(o, d);
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    float t;
+    int32_t k = trace_closest<false>(S, R, tmin, tmax, t, sm, threadIdx.x, blockDim.x, overflow, K);
+    if (overflow) atomicOr(err, 1u);
+    if (t_out) t_out[i] = t;
+    uint32_t front = 0;
+    int32_t id = -1;
+    if (k >= 0) {
+        id = (int32_t)(__ldg(S.meta + k) & 0x3fffffffu);
+        float4 sp = __ldg(S.sph + k);
+        f3 p = o + d * t;
+        f3 outward = divs(p - mk(sp.x, sp.y, sp.z), sp.w);
+        front = dot(d, outward) < 0.0f ? 1u : 0u;
+    }
+    if (id_out) id_out[i] = id;
+    if (front_out) front_out[i] = front;
+}
+
+SceneView view_of(const venu_scene* s) {
+    SceneView v;
+    v.nodes = s->nodes;
+    v.sph = s->sph;
+    v.mat = s->mat;
+    v.meta = s->meta;
+    v.n = s->n;
+    return v;
+}
+
+size_t traverse_smem(int block) { return (size_t)block * kShared * (sizeof(int2) + sizeof(float)); }
+
+}  // namespace venu
+
+using namespace venu;
+
+struct venu_renderer {
+    uint32_t Q = 0;
+    uint32_t flags = 0;
+    Queue q[2] = {};
+    int2* hits = nullptr;
+    float4* slots = nullptr;
+    uint32_t* seeds = nullptr;
+    uint32_t seeds_cap = 0;
+    uint32_t* cnt = nullptr;   // [65]
+    uint32_t* work = nullptr;  // [65]
+    uint32_t* err = nullptr;
+    unsigned long long* stats = nullptr;  // segments, nodes, spheres
+    int trav_blocks = 0, shade_blocks = 0;
+    venu_render_stats last = {};
+    // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
+    std::vector<cudaEvent_t> ev;
+    size_t ev_used = 0;
+};
+
+namespace {
+constexpr int kTravBlock = 128;
+constexpr int kShadeBlock = 256;
+constexpr uint32_t kMaxDepth = 64;
+
+// Returns an event pair for the next profiled launch, growing the pool.
+cudaError_t next_events(venu_renderer* r, cudaEvent_t& a, cudaEvent_t& b) {
+    while (r->ev_used + 2 > r->ev.size()) {
+        cudaEvent_t e;
+        cudaError_t err = cudaEventCreate(&e);
+        if (err != cudaSuccess) return err;
+        r->ev.push_back(e);
+    }
+    a = r->ev[r->ev_used];
+    b = r->ev[r->ev_used + 1];
+    r->ev_used += 2;
+    return cudaSuccess;
+}
+
+void free_renderer(venu_renderer* r) {
+    for (cudaEvent_t e : r->ev) cudaEventDestroy(e);
+    r->ev.clear();
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(r->q[i].o);
+        cudaFree(r->q[i].d);
+        cudaFree(r->q[i].t);
+    }
+    cudaFree(r->hits);
+    cudaFree(r->slots);
+    cudaFree(r->seeds);
+    cudaFree(r->cnt);
+    cudaFree(r->work);
+    cudaFree(r->err);
+    cudaFree(r->stats);
+}
+}  // namespace
+
+extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, venu_renderer** out) {
+    if (!out) {
+        set_error("venu_renderer_create: out is NULL");
+        return VENU_ERR_INVALID;
+    }
+    *out = nullptr;
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    if (max_paths == 0) max_paths = 8u << 20;
+    if (max_paths > (1u << 27)) {
+        set_error("venu_renderer_create: max_paths above 2^27");
+        return VENU_ERR_TOO_LARGE;
+    }
+    venu_renderer* r = new venu_renderer();
+    r->Q = max_paths;
+    r->flags = flags;
+    cudaError_t e = cudaSuccess;
+    const size_t Q = max_paths;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].o, sizeof(float4) * Q);
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].d, sizeof(float4) * Q);
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].t, sizeof(float4) * Q);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&r->hits, sizeof(int2) * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&r->slots, sizeof(float4) * Q);
+    if (e == cudaSuccess) e = cudaMalloc(&r->cnt, sizeof(uint32_t) * (kMaxDepth + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&r->work, sizeof(uint32_t) * (kMaxDepth + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&r->err, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMemset(r->err, 0, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(r->stats, 0, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) {
+        const size_t sm = traverse_smem(kTravBlock);
+        e = cudaFuncSetAttribute(k_traverse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        int per_sm = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_traverse<false>, kTravBlock, sm);
+        r->trav_blocks = std::max(1, per_sm) * sm_count();
+        int per_sm2 = 0;
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_shade, kShadeBlock, 0);
+        r->shade_blocks = std::max(1, per_sm2) * sm_count();
+    }
+    if (e != cudaSuccess) {
+        free_renderer(r);
+        delete r;
+        return e == cudaErrorMemoryAllocation ? (set_error("venu_renderer_create: out of device memory"), VENU_ERR_OOM)
+                                              : cuda_fail(e, "venu_renderer_create");
+    }
+    *out = r;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_renderer_destroy(venu_renderer* r) {
+    if (!r) return VENU_OK;
+    free_renderer(r);
+    delete r;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, const venu_camera* camera,
+                                   const venu_render_opts* opts, float* accum_dev, float* image_f_dev,
+                                   uint8_t* image8_dev, void* stream) {
+    if (!r || !scene || !camera || !opts || !accum_dev) {
+        set_error("venu_render: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    const uint32_t W = opts->width, H = opts->height, spp = opts->samples_per_pixel;
+    const uint32_t maxd = opts->max_depth;
+    if (W < 2 || H < 2 || spp == 0 || maxd == 0 || maxd > kMaxDepth) {
+        set_error("venu_render: need width,height >= 2, spp >= 1, 1 <= max_depth <= 64");
+        return VENU_ERR_INVALID;
+    }
+    const uint64_t npix64 = (uint64_t)W * H;
+    if (npix64 > (1u << 30)) {
+        set_error("venu_render: image above 2^30 pixels");
+        return VENU_ERR_TOO_LARGE;
+    }
+    const uint32_t npix = (uint32_t)npix64;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (npix > r->seeds_cap) {
+        cudaFree(r->seeds);
+        r->seeds = nullptr;
+        r->seeds_cap = 0;
+        VENU_CUDA(cudaMalloc(&r->seeds, sizeof(uint32_t) * npix));
+        r->seeds_cap = npix;
+    }
+    if (opts->flags & VENU_FLAG_RESET_ACCUM)
+        VENU_CUDA(cudaMemsetAsync(accum_dev, 0, sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL * npix64, st));
+    VENU_CUDA(cudaMemsetAsync(r->stats, 0, sizeof(unsigned long long) * 4, st));
+    const SceneView S = view_of(scene);
+    const bool count = (r->flags & VENU_RENDERER_COUNT) != 0;
+    const bool prof = (r->flags & VENU_RENDERER_PROFILE) != 0;
+    r->ev_used = 0;
+    std::vector<uint8_t> kinds;  // 0 traverse, 1 shade, per event pair
+    const size_t tsm = traverse_smem(kTravBlock);
+    float4* accum = reinterpret_cast<float4*>(accum_dev);
+    uint32_t launches = 0, waves = 0;
+    // wave shape: all pixels x k samples, or P pixels x 1 sample
+    uint32_t P, k;
+    if (npix <= r->Q) {
+        P = npix;
+        k = std::min(spp, r->Q / npix);
+    } else {
+        P = r->Q;
+        k = 1;
+    }
+    const int nb = (int)maxd;
+    for (uint32_t s0 = 0; s0 < spp; s0 += k) {
+        const uint32_t kk = std::min(k, spp - s0);
+        for (uint32_t p0 = 0; p0 < npix; p0 += P) {
+            const uint32_t PP = std::min(P, npix - p0);
+            k_raygen<<<(PP + 255) / 256, 256, 0, st>>>(*camera, W, H, p0, PP, s0, kk, opts->subframe_index,
+                                                       (int)maxd, r->seeds, r->q[0], r->cnt, r->work, nb);
+            ++launches;
+            for (int b = 0; b < nb; ++b) {
+                const Queue& qi = r->q[b & 1];
+                const Queue& qo = r->q[(b + 1) & 1];
+                cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr, e3 = nullptr;
+                if (prof) {
+                    VENU_CUDA(next_events(r, e0, e1));
+                    VENU_CUDA(next_events(r, e2, e3));
+                    VENU_CUDA(cudaEventRecord(e0, st));
+                }
+                if (count)
+                    k_traverse<true><<<r->trav_blocks, kTravBlock, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
+                                                                             r->err, r->stats);
+                else
+                    k_traverse<false><<<r->trav_blocks, kTravBlock, tsm, st>>>(S, qi, r->cnt + b, r->work + b,
+                                                                              r->hits, r->err, r->stats);
+                if (prof) {
+                    VENU_CUDA(cudaEventRecord(e1, st));
+                    VENU_CUDA(cudaEventRecord(e2, st));
+                }
+                k_shade<<<r->shade_blocks, kShadeBlock, 0, st>>>(S, qi, r->hits, r->cnt + b, qo, r->cnt + b + 1,
+                                                                 r->slots);
+                if (prof) VENU_CUDA(cudaEventRecord(e3, st));
+                launches += 2;
+            }
+            k_accumulate<<<(PP + 255) / 256, 256, 0, st>>>(r->slots, p0, PP, kk, accum);
+            ++launches;
+            ++waves;
+        }
+    }
+    if (image_f_dev || image8_dev) {
+        k_resolve<<<(npix + 255) / 256, 256, 0, st>>>(accum, npix, reinterpret_cast<float4*>(image_f_dev),
+                                                      reinterpret_cast<uchar4*>(image8_dev));
+        ++launches;
+    }
+    VENU_CUDA(cudaGetLastError());
+    (void)kinds;
+    r->last = venu_render_stats{};
+    r->last.paths = (uint64_t)npix * spp;
+    r->last.waves = waves;
+    r->last.kernel_launches = launches;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* out) {
+    if (!r || !out) {
+        set_error("venu_renderer_stats: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    unsigned long long st[4] = {0, 0, 0, 0};
+    uint32_t err = 0;
+    VENU_CUDA(cudaMemcpy(st, r->stats, sizeof(st), cudaMemcpyDeviceToHost));
+    VENU_CUDA(cudaMemcpy(&err, r->err, sizeof(err), cudaMemcpyDeviceToHost));
+    r->last.segments = st[0];
+    r->last.nodes_visited = st[1];
+    r->last.spheres_tested = st[2];
+    // event pairs alternate traverse, shade (4 events per bounce)
+    float tms = 0.0f, sms = 0.0f;
+    uint32_t tn = 0, sn = 0;
+    for (size_t i = 0; i + 3 < r->ev_used; i += 4) {
+        float a = 0.0f, b = 0.0f;
+        VENU_CUDA(cudaEventElapsedTime(&a, r->ev[i], r->ev[i + 1]));
+        VENU_CUDA(cudaEventElapsedTime(&b, r->ev[i + 2], r->ev[i + 3]));
+        tms += a;
+        sms += b;
+        ++tn;
+        ++sn;
+    }
+    r->last.traverse_ms = tms;
+    r->last.shade_ms = sms;
+    r->last.traverse_launches = tn;
+    r->last.shade_launches = sn;
+    *out = r->last;
+    if (err) {
+        set_error("traversal stack overflow (result of at least one ray is incomplete)");
+        return VENU_ERR_STACK;
+    }
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_trace(const venu_scene* scene, const float* rays_dev, uint32_t n, float tmin,
+                                  float tmax, float* t_dev, int32_t* id_dev, uint32_t* front_dev, void* stream) {
+    if (!scene || (!rays_dev && n)) {
+        set_error("venu_trace: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    if (n == 0) return VENU_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t* err = nullptr;
+    VENU_CUDA(cudaMalloc(&err, sizeof(uint32_t)));
+    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(uint32_t), st);
+    const size_t tsm = traverse_smem(kTravBlock);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_trace_rays, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm);
+    if (e == cudaSuccess) {
+        k_trace_rays<<<(n + kTravBlock - 1) / kTravBlock, kTravBlock, tsm, st>>>(view_of(scene), rays_dev, n, tmin,
+                                                                               tmax, t_dev, id_dev, front_dev, err);
+        e = cudaGetLastError();
+    }
+    uint32_t herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(err);
+    if (e != cudaSuccess) return cuda_fail(e, "venu_trace");
+    if (herr) {
+        set_error("venu_trace: traversal stack overflow");
+        return VENU_ERR_STACK;
+    }
+    return VENU_OK;
+}

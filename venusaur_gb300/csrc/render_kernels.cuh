@@ -1,0 +1,135 @@
+// render_kernels.cuh -- wavefront stages shared by the plain single-scene
+// renderer and the batched multi-scene renderer.
+#pragma once
+
+#include "venu_device.cuh"
+
+namespace venu {
+
+// Per-sample camera ray into a queue entry (Core/RayTracer.cu:163-202 up to
+// optixTrace).  The bounce seed is the raygen seed after the sample's jitter
+// and lens draws; the raygen seed continues from that same state to the next
+// sample (the reference copies it into the PRD and never copies it back).
+__device__ __forceinline__ void write_primary(const Queue& q, uint32_t pos, f3 o, f3 d, uint32_t slot,
+                                              int depth, uint32_t seed) {
+    q.o[pos] = make_float4(o.x, o.y, o.z, __int_as_float((int)slot));
+    q.d[pos] = make_float4(d.x, d.y, d.z, __int_as_float(depth));
+    q.t[pos] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
+}
+
+__device__ __forceinline__ DevCamera load_camera(const venu_camera& c) {
+    DevCamera k;
+    k.origin = mk(c.origin[0], c.origin[1], c.origin[2]);
+    k.u = mk(c.u[0], c.u[1], c.u[2]);
+    k.v = mk(c.v[0], c.v[1], c.v[2]);
+    k.w = mk(c.w[0], c.w[1], c.w[2]);
+    k.un = normalize(k.u);
+    k.vn = normalize(k.v);
+    k.lens = c.lens_radius;
+    return k;
+}
+
+struct ShadeOut {
+    bool cont;
+    float4 o, d, t;   // next queue entry when cont
+    float4 result;    // final path radiance when !cont
+};
+
+// One hit/miss record -> scatter (Core/RayTracer.cu:272-449, iterative):
+// forward throughput, black at depth 0 or on metal absorption, sky on miss.
+__device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, float4 d4, float4 t4, int2 h) {
+    ShadeOut out;
+    out.cont = false;
+    f3 o = mk(o4.x, o4.y, o4.z), d = mk(d4.x, d4.y, d4.z);
+    int depth = __float_as_int(d4.w);
+    f3 T = mk(t4.x, t4.y, t4.z);
+    uint32_t seed = __float_as_uint(t4.w);
+    if (h.y < 0) {
+        f3 L = T * sky(d);
+        out.result = make_float4(L.x, L.y, L.z, 0.0f);
+        return out;
+    }
+    if (!(depth > 0)) {
+        out.result = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        return out;
+    }
+    const int k = h.y;
+    const float t = __int_as_float(h.x);
+    float4 sp = __ldg(S.sph + k);
+    float4 m = __ldg(S.mat + k);
+    uint32_t type = __ldg(S.meta + k) >> 30;
+    f3 C = mk(sp.x, sp.y, sp.z);
+    f3 p = o + d * t;
+    f3 outward = divs(p - C, sp.w);
+    bool front = dot(d, outward) < 0.0f;
+    f3 n = front ? outward : -outward;
+    f3 dir;
+    if (type == 0u) {
+        dir = n + normalize(random_in_unit_sphere(seed));
+        if (near_zero(dir)) dir = n;
+        T = T * mk(m.x, m.y, m.z);
+    } else if (type == 1u) {
+        f3 refl = reflect(normalize(d), n);
+        dir = refl + m.w * random_in_unit_sphere(seed);
+        if (!(dot(dir, n) > 0.0f)) {
+            out.result = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            return out;
+        }
+        T = T * mk(m.x, m.y, m.z);
+    } else {
+        float ratio = front ? (1.0f / m.w) : m.w;
+        f3 ud = normalize(d);
+        float cos_t = fminf(dot(-ud, n), 1.0f);
+        float sin_t = sqrtf(1.0f - cos_t * cos_t);
+        bool cannot = ratio * sin_t > 1.0f;
+        if (cannot || reflectance(cos_t, ratio) > rnd(seed))
+            dir = reflect(ud, n);
+        else
+            dir = refract(ud, n, ratio);
+    }
+    out.cont = true;
+    out.o = make_float4(p.x, p.y, p.z, o4.w);
+    out.d = make_float4(dir.x, dir.y, dir.z, __int_as_float(depth - 1));
+    out.t = make_float4(T.x, T.y, T.z, __uint_as_float(seed));
+    return out;
+}
+
+// Warp-aggregated append: one atomic per warp, positions from the ballot.
+__device__ __forceinline__ uint32_t warp_append(bool pred, uint32_t* counter) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t m = __ballot_sync(0xffffffffu, pred);
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+// Kahan-compensated add of one sample into {sum.rgb, n} {comp.rgb, 0}.
+__device__ __forceinline__ void kahan_add(float4& a0, float4& a1, float4 v) {
+    float y, t;
+    y = v.x - a1.x; t = a0.x + y; a1.x = (t - a0.x) - y; a0.x = t;
+    y = v.y - a1.y; t = a0.y + y; a1.y = (t - a0.y) - y; a0.y = t;
+    y = v.z - a1.z; t = a0.z + y; a1.z = (t - a0.z) - y; a0.z = t;
+    a0.w = a0.w + 1.0f;
+}
+
+// Core/RayTracer.cu:16-47: clamp, sRGB (powf with 1/2.4), x*256 truncated.
+__device__ __forceinline__ unsigned char quant8(float x) {
+    x = fmaxf(0.0f, fminf(x, 1.0f));
+    uint32_t q = (uint32_t)(x * 256.0f);
+    return (unsigned char)min(q, 255u);
+}
+__device__ __forceinline__ uchar4 make_color(f3 c) {
+    float v[3] = {fmaxf(0.0f, fminf(c.x, 1.0f)), fmaxf(0.0f, fminf(c.y, 1.0f)), fmaxf(0.0f, fminf(c.z, 1.0f))};
+    const float inv_gamma = 1.0f / 2.4f;
+    unsigned char q[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float p = powf(v[i], inv_gamma);
+        float srgb = v[i] < 0.0031308f ? 12.92f * v[i] : 1.055f * p - 0.055f;
+        q[i] = quant8(srgb);
+    }
+    return make_uchar4(q[0], q[1], q[2], 255);
+}
+
+}  // namespace venu

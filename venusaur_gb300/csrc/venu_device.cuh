@@ -1,0 +1,426 @@
+// venu_device.cuh -- device building blocks of the GB300 path tracer.
+//
+// Arithmetic contract (the library is compiled with -fmad=false): every
+// float operation rounds once as written; fmaf() appears only where written.
+// Camera rays, scattering and the sky follow the reference's device source
+// (Core/RayTracer.cu, Core/vec_math.h) operation by operation; the ray/box
+// and ray/sphere tests are this library's own (robust slab test, stable
+// quadratic with an exactly refined constant term).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/venu.h"
+
+namespace venu {
+
+// ---------------------------------------------------------------------------
+// float3 operations with Core/vec_math.h semantics.
+// ---------------------------------------------------------------------------
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator-(f3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return mk(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Core/vec_math.h:483-487: float3 / float multiplies by the reciprocal.
+__device__ __forceinline__ f3 divs(f3 a, float s) {
+    float inv = 1.0f / s;
+    return a * inv;
+}
+__device__ __forceinline__ f3 normalize(f3 v) {  // Core/vec_math.h:544-549
+    float inv = 1.0f / sqrtf(dot(v, v));
+    return v * inv;
+}
+__device__ __forceinline__ f3 reflect(f3 i, f3 n) { return i - (2.0f * n) * dot(n, i); }
+__device__ __forceinline__ f3 refract(f3 uv, f3 n, float eta) {  // Core/vec_math.h:563-569
+    float cos_theta = fminf(dot(-uv, n), 1.0f);
+    f3 r_perp = eta * (uv + cos_theta * n);
+    f3 r_par = (-sqrtf(fabsf(1.0f - dot(r_perp, r_perp)))) * n;
+    return r_perp + r_par;
+}
+__device__ __forceinline__ f3 lerp3(f3 a, f3 b, float t) { return a + t * (b - a); }
+
+// ---------------------------------------------------------------------------
+// RNG: TEA-4 seed hash and the 24-bit LCG of Core/random.cuh:31-67.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t tea4(uint32_t v0, uint32_t v1) {
+    uint32_t s0 = 0;
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+__device__ __forceinline__ float rnd(uint32_t& s) {
+    s = 1664525u * s + 1013904223u;
+    return (float)(s & 0x00FFFFFFu) / (float)0x01000000;
+}
+// Core/RayTracer.cu:93-97 with min=-1, max=1; draws x, y, z left to right.
+__device__ __forceinline__ float rnd_pm1(uint32_t& s) { return -1.0f + (1.0f - -1.0f) * rnd(s); }
+__device__ __forceinline__ f3 random_in_unit_sphere(uint32_t& s) {  // :117-125
+    for (;;) {
+        float x = rnd_pm1(s);
+        float y = rnd_pm1(s);
+        float z = rnd_pm1(s);
+        f3 p = mk(x, y, z);
+        if (!(dot(p, p) >= 1.0f)) return p;
+    }
+}
+__device__ __forceinline__ f3 random_in_unit_disk(uint32_t& s) {  // :141-149
+    for (;;) {
+        float x = rnd_pm1(s);
+        float y = rnd_pm1(s);
+        f3 p = mk(x, y, 0.0f);
+        if (!(dot(p, p) >= 1.0f)) return p;
+    }
+}
+// Core/RayTracer.cu:8-13; for float x, (double)x < 1e-8 <=> x <= 1e-8f.
+__device__ __forceinline__ bool near_zero(f3 e) {
+    return fabsf(e.x) <= 1e-8f && fabsf(e.y) <= 1e-8f && fabsf(e.z) <= 1e-8f;
+}
+
+// ---------------------------------------------------------------------------
+// Camera (Params fields) with the per-launch constants normalize(U/V).
+// ---------------------------------------------------------------------------
+struct DevCamera {
+    f3 origin, u, v, w, un, vn;
+    float lens;
+};
+
+// Core/RayTracer.cu:151-161,173-177: jitter u, jitter v, then the lens disk.
+__device__ __forceinline__ void camera_ray(const DevCamera& C, uint32_t x, uint32_t y, uint32_t W,
+                                           uint32_t H, uint32_t& seed, f3& o, f3& d) {
+    float r1 = rnd(seed);
+    float s = 2.0f * ((float)x + r1) / (float)(W - 1) - 1.0f;
+    float r2 = rnd(seed);
+    float t = 2.0f * ((float)y + r2) / (float)(H - 1) - 1.0f;
+    f3 rd = C.lens * random_in_unit_disk(seed);
+    f3 offset = C.un * rd.x + C.vn * rd.y;
+    o = C.origin + offset;
+    d = C.w + (s * C.u) * 0.5f + (t * C.v) * 0.5f - offset;
+}
+
+// Core/RayTracer.cu:442-449.  fmaf(0.5, y, 0.5) equals the reference's double
+// 0.5 * (y + 1.0) rounded to float (both are one rounding of the same value).
+__device__ __forceinline__ f3 sky(f3 d) {
+    f3 ud = normalize(d);
+    float t = fmaf(0.5f, ud.y, 0.5f);
+    return lerp3(mk(1.0f, 1.0f, 1.0f), mk(0.5f, 0.7f, 1.0f), t);
+}
+
+// Schlick (Core/RayTracer.cu:373-379) with (1-cos)^5 as an explicit product.
+__device__ __forceinline__ float reflectance(float cosine, float ref_idx) {
+    float r0 = (1.0f - ref_idx) / (1.0f + ref_idx);
+    r0 = r0 * r0;
+    float x = 1.0f - cosine;
+    float x2 = x * x;
+    float x5 = (x2 * x2) * x;
+    return r0 + (1.0f - r0) * x5;
+}
+
+// ---------------------------------------------------------------------------
+// Scene view: LBVH nodes + spheres/materials in Morton (slot) order.
+// ---------------------------------------------------------------------------
+constexpr int32_t kLeaf = (int32_t)0x80000000u;
+constexpr int32_t kNone = 0x7fffffff;
+
+struct SceneView {
+    const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
+    const float4* __restrict__ sph;    // {center, radius} per slot
+    const float4* __restrict__ mat;    // {albedo, fuzz or ir} per slot
+    const uint32_t* __restrict__ meta; // original id | material << 30
+    uint32_t n;
+};
+
+struct RayPre {
+    f3 o, d, inv, noi;  // noi = -(o * inv)
+    float a, inv_a, slack;
+};
+
+__device__ __forceinline__ RayPre prep(f3 o, f3 d) {
+    RayPre R;
+    R.o = o;
+    R.d = d;
+    float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
+    float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
+    float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
+    R.inv = mk(1.0f / dx, 1.0f / dy, 1.0f / dz);
+    float ox = o.x * R.inv.x, oy = o.y * R.inv.y, oz = o.z * R.inv.z;
+    R.noi = mk(-ox, -oy, -oz);
+    float m = fmaxf(fmaxf(fmaxf(0.0f, fabsf(ox)), fabsf(oy)), fabsf(oz));
+    R.slack = m * 4.76837158203125e-07f;  // 2^-21
+    R.a = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+    R.inv_a = 1.0f / R.a;
+    return R;
+}
+
+// Robust slab test: conservative by a relative 2^-20 plus an absolute slack
+// proportional to |o / d|, so rounding never drops a box the ray touches.
+__device__ __forceinline__ bool box_test(const RayPre& R, float4 lo, float4 hi, float tmin,
+                                         float tcap, float& tnear) {
+    float t0x = fmaf(lo.x, R.inv.x, R.noi.x), t1x = fmaf(hi.x, R.inv.x, R.noi.x);
+    float t0y = fmaf(lo.y, R.inv.y, R.noi.y), t1y = fmaf(hi.y, R.inv.y, R.noi.y);
+    float t0z = fmaf(lo.z, R.inv.z, R.noi.z), t1z = fmaf(hi.z, R.inv.z, R.noi.z);
+    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcap));
+    tnear = tn;
+    return tn <= fmaf(tf, 1.00000095367431640625f, R.slack);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bp = s - a;
+    float ap = s - bp;
+    e = (a - ap) + (b - bp);
+}
+
+// Ray/sphere: the discriminant is formed from the perpendicular distance of
+// the centre to the ray line, disc = a (r^2 - |f|^2) with f = h - (h.d/a) d
+// (Haines et al., "Precision Improvements for Ray/Sphere Intersection", Ray
+// Tracing Gems ch. 7), so its error scales with r^2 instead of |h|^2; the
+// roots come from q = -(b + sign(b) sqrt(disc)) as q/a and c/q (no
+// cancellation).  When the origin is close to the surface relative to the
+// radius (|c| < (|h|^2 + r^2)/16), c = |o-C|^2 - r^2 and h are refined with
+// TwoDiff/TwoProduct/TwoSum error terms, so the near root c/q keeps full
+// relative accuracy even for the r = 1000 ground sphere.  Root selection
+// follows Core/RayTracer.cu:248-253: the smaller root in [tmin, tmax], else
+// the larger.
+__device__ __forceinline__ bool sphere_test(const RayPre& R, float4 S, float tmin, float tmax,
+                                            float& tout) {
+    const float r = S.w;
+    float hx = R.o.x - S.x, hy = R.o.y - S.y, hz = R.o.z - S.z;
+    float hb = fmaf(hx, R.d.x, fmaf(hy, R.d.y, hz * R.d.z));
+    float hh = fmaf(hx, hx, fmaf(hy, hy, hz * hz));
+    float r2 = r * r;
+    float c = hh - r2;
+    float discp;
+    if (fabsf(c) < (hh + r2) * 0.0625f) {
+        // exact residuals of h = o - C (TwoDiff)
+        float bvx = R.o.x - hx, bvy = R.o.y - hy, bvz = R.o.z - hz;
+        float ex = (R.o.x - (hx + bvx)) + (bvx - S.x);
+        float ey = (R.o.y - (hy + bvy)) + (bvy - S.y);
+        float ez = (R.o.z - (hz + bvz)) + (bvz - S.z);
+        // c = |h + e|^2 - r^2 from exact squares and compensated sums
+        float px = hx * hx, py = hy * hy, pz = hz * hz;
+        float qx = fmaf(hx, hx, -px), qy = fmaf(hy, hy, -py), qz = fmaf(hz, hz, -pz);
+        float qr = fmaf(r, r, -r2);
+        float s1, e1, s2, e2, s3, e3;
+        two_sum(px, py, s1, e1);
+        two_sum(s1, pz, s2, e2);
+        two_sum(s2, -r2, s3, e3);
+        float lo = (e1 + e2) + e3;
+        lo = lo + ((qx + qy) + qz);
+        lo = lo - qr;
+        float he = fmaf(hx, ex, fmaf(hy, ey, hz * ez));
+        lo = fmaf(2.0f, he, lo);
+        c = s3 + lo;
+        hb = hb + fmaf(ex, R.d.x, fmaf(ey, R.d.y, ez * R.d.z));
+        // f = (h + e) - s d as head + tail, then r^2 - |f|^2 compensated
+        const float s = hb * R.inv_a;
+        float mx = s * R.d.x, my = s * R.d.y, mz = s * R.d.z;
+        float mex = fmaf(s, R.d.x, -mx), mey = fmaf(s, R.d.y, -my), mez = fmaf(s, R.d.z, -mz);
+        float fx, fy, fz, fex, fey, fez;
+        two_sum(hx, -mx, fx, fex);
+        two_sum(hy, -my, fy, fey);
+        two_sum(hz, -mz, fz, fez);
+        float tx = (fex - mex) + ex, ty = (fey - mey) + ey, tz = (fez - mez) + ez;
+        float gx = fx * fx, gy = fy * fy, gz = fz * fz;
+        float gex = fmaf(fx, fx, -gx), gey = fmaf(fy, fy, -gy), gez = fmaf(fz, fz, -gz);
+        float u1, v1, u2, v2, w, we;
+        two_sum(gx, gy, u1, v1);
+        two_sum(u1, gz, u2, v2);
+        two_sum(r2, -u2, w, we);
+        float dl = (we + qr) - (v1 + v2);
+        dl = dl - ((gex + gey) + gez);
+        dl = fmaf(-2.0f, fmaf(fx, tx, fmaf(fy, ty, fz * tz)), dl);
+        discp = w + dl;
+    } else {
+        const float s = hb * R.inv_a;
+        const float fx = fmaf(-s, R.d.x, hx);
+        const float fy = fmaf(-s, R.d.y, hy);
+        const float fz = fmaf(-s, R.d.z, hz);
+        const float ff = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+        discp = fmaf(r, r, -ff);
+    }
+    if (!(discp >= 0.0f)) return false;
+    const float sd = sqrtf(R.a * discp);
+    const float q = -(hb + copysignf(sd, hb));
+    if (q == 0.0f) return false;
+    const float ta = q * R.inv_a;
+    const float tb = c / q;
+    const float t0 = fminf(ta, tb), t1 = fmaxf(ta, tb);
+    if (t0 >= tmin && t0 <= tmax) {
+        tout = t0;
+        return true;
+    }
+    if (t1 >= tmin && t1 <= tmax) {
+        tout = t1;
+        return true;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Closest-hit traversal of the binary LBVH.
+//
+// Children are tested at their parent: internal children by their box (two
+// float4 loads each), leaf children directly by the sphere (one float4).
+// The nearer hit child is descended; the farther one's child pair and entry
+// distance go on a per-thread stack whose top kShared entries live in shared
+// memory (ring buffer, layout [entry][thread] so a warp touches 32 distinct
+// banks) and whose older entries spill to local memory.  Ties on t go to the
+// smaller slot, so the result does not depend on traversal order.
+// ---------------------------------------------------------------------------
+constexpr int kShared = 16;  // shared-memory entries per thread (power of two)
+constexpr int kSpill = 64;   // local-memory entries beyond those
+
+struct StackSmem {
+    int2* pair;  // [kShared][block]
+    float* tn;   // [kShared][block]
+};
+
+struct TraceCounters {
+    uint32_t nodes, spheres;
+};
+
+template <bool COUNT>
+__device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPre& R, float tmin,
+                                                 float tmax, float& t_out, StackSmem sm,
+                                                 uint32_t tid, uint32_t bdim, bool& overflow,
+                                                 TraceCounters& K) {
+    float best_t = tmax;
+    int32_t best = kNone;
+    const uint32_t n = S.n;
+    if (n == 0) {
+        t_out = tmax;
+        return -1;
+    }
+    auto leaf = [&](int32_t k) {
+        float t;
+        if (COUNT) ++K.spheres;
+        float4 sp = __ldg(S.sph + k);
+        if (sphere_test(R, sp, tmin, tmax, t) && (t < best_t || (t == best_t && k < best))) {
+            best_t = t;
+            best = k;
+        }
+    };
+    if (n == 1) {
+        leaf(0);
+    } else {
+        float tn;
+        float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
+        if (COUNT) ++K.nodes;
+        if (box_test(R, rlo, rhi, tmin, best_t, tn)) {
+            int2 spill[kSpill];
+            float spill_tn[kSpill];
+            int sp = 0;
+            int32_t pl = __float_as_int(rlo.w), pr = __float_as_int(rhi.w);
+            for (;;) {
+                bool h0 = false, h1 = false;
+                float tn0 = 0.0f, tn1 = 0.0f;
+                int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
+                if (pl & kLeaf) {
+                    leaf(pl & ~kLeaf);
+                } else {
+                    float4 lo = __ldg(S.nodes + 2 * pl), hi = __ldg(S.nodes + 2 * pl + 1);
+                    if (COUNT) ++K.nodes;
+                    h0 = box_test(R, lo, hi, tmin, best_t, tn0);
+                    c0l = __float_as_int(lo.w);
+                    c0r = __float_as_int(hi.w);
+                }
+                if (pr & kLeaf) {
+                    leaf(pr & ~kLeaf);
+                } else {
+                    float4 lo = __ldg(S.nodes + 2 * pr), hi = __ldg(S.nodes + 2 * pr + 1);
+                    if (COUNT) ++K.nodes;
+                    h1 = box_test(R, lo, hi, tmin, best_t, tn1);
+                    c1l = __float_as_int(lo.w);
+                    c1r = __float_as_int(hi.w);
+                }
+                if (h0 && h1) {
+                    int2 far;
+                    float far_tn;
+                    if (tn1 < tn0) {
+                        far = make_int2(c0l, c0r);
+                        far_tn = tn0;
+                        pl = c1l;
+                        pr = c1r;
+                    } else {
+                        far = make_int2(c1l, c1r);
+                        far_tn = tn1;
+                        pl = c0l;
+                        pr = c0r;
+                    }
+                    // push
+                    const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
+                    if (sp >= kShared) {
+                        const int g = sp - kShared;
+                        if (g >= kSpill) {
+                            overflow = true;
+                            break;
+                        }
+                        spill[g] = sm.pair[j];
+                        spill_tn[g] = sm.tn[j];
+                    }
+                    sm.pair[j] = far;
+                    sm.tn[j] = far_tn;
+                    ++sp;
+                } else if (h0) {
+                    pl = c0l;
+                    pr = c0r;
+                } else if (h1) {
+                    pl = c1l;
+                    pr = c1r;
+                } else {
+                    bool found = false;
+                    while (sp > 0) {
+                        --sp;
+                        const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
+                        int2 e = sm.pair[j];
+                        float etn = sm.tn[j];
+                        if (sp >= kShared) {
+                            sm.pair[j] = spill[sp - kShared];
+                            sm.tn[j] = spill_tn[sp - kShared];
+                        }
+                        if (etn <= best_t) {
+                            pl = e.x;
+                            pr = e.y;
+                            found = true;
+                            break;
+                        }
+                    }
+                    if (!found) break;
+                }
+            }
+        }
+    }
+    if (best == kNone) {
+        t_out = tmax;
+        return -1;
+    }
+    t_out = best_t;
+    return best;
+}
+
+// ---------------------------------------------------------------------------
+// Path state in the wavefront queues (48 bytes per path):
+//   o4 = {origin.xyz, slot (int bits)}
+//   d4 = {direction.xyz, remaining depth (int bits)}
+//   t4 = {throughput.rgb, bounce seed (uint bits)}
+// ---------------------------------------------------------------------------
+struct Queue {
+    float4* o;
+    float4* d;
+    float4* t;
+};
+
+}  // namespace venu

@@ -1,0 +1,43 @@
+// venu_internal.h -- host-side internals shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/venu.h"
+
+namespace venu {
+
+void set_error(const std::string& msg);
+venu_status cuda_fail(cudaError_t e, const char* what);
+
+#define VENU_CUDA(call)                                          \
+    do {                                                         \
+        cudaError_t _e = (call);                                 \
+        if (_e != cudaSuccess) return ::venu::cuda_fail(_e, #call); \
+    } while (0)
+
+venu_status require_device();  // sm_103 device present and kernels loadable
+int sm_count();
+
+}  // namespace venu
+
+struct venu_scene {
+    uint32_t n = 0;
+    float4* nodes = nullptr;   // 2 per internal node
+    float4* sph = nullptr;     // slot order
+    float4* mat = nullptr;
+    uint32_t* meta = nullptr;  // original id | material << 30
+    uint32_t* keys = nullptr;  // sorted Morton codes
+    float bounds[6] = {0, 0, 0, 0, 0, 0};
+    float build_ms = 0.0f;
+    uint64_t bytes = 0;
+};
+
+namespace venu {
+// Builds the LBVH for `n` device spheres into `s` (allocates its buffers).
+venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t stream, venu_scene* s);
+void free_scene(venu_scene* s);
+}  // namespace venu
