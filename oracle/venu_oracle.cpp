@@ -72,25 +72,30 @@ inline float rnd(uint32_t& prev) {  // random.cuh:49-55 (lcg) and :64-67 (rnd)
 // Core/RayTracer.cu:93-97 (random_float with range), left-to-right draws.
 inline float rnd_range(uint32_t& s, float lo, float hi) { return lo + (hi - lo) * rnd(s); }
 // Core/RayTracer.cu:117-125: rejection sampling, x then y then z per try.
+// Capped at 4096 candidates like the CUDA kernels (an unreachable bound at
+// a 52% / 79% acceptance rate that only guarantees termination).
+const int kMaxTries = 4096;
 inline f3 random_in_unit_sphere(uint32_t& s) {
-    for (;;) {
+    f3 p{0, 0, 0};
+    for (int i = 0; i < kMaxTries; ++i) {
         float x = rnd_range(s, -1.0f, 1.0f);
         float y = rnd_range(s, -1.0f, 1.0f);
         float z = rnd_range(s, -1.0f, 1.0f);
-        f3 p = mk(x, y, z);
-        if (dot(p, p) >= 1.0f) continue;
-        return p;
+        p = mk(x, y, z);
+        if (!(dot(p, p) >= 1.0f)) break;
     }
+    return p;
 }
 // Core/RayTracer.cu:141-149
 inline f3 random_in_unit_disk(uint32_t& s) {
-    for (;;) {
+    f3 p{0, 0, 0};
+    for (int i = 0; i < kMaxTries; ++i) {
         float x = rnd_range(s, -1.0f, 1.0f);
         float y = rnd_range(s, -1.0f, 1.0f);
-        f3 p = mk(x, y, 0.0f);
-        if (dot(p, p) >= 1.0f) continue;
-        return p;
+        p = mk(x, y, 0.0f);
+        if (!(dot(p, p) >= 1.0f)) break;
     }
+    return p;
 }
 // Core/RayTracer.cu:8-13: |e_i| < 1e-8 (a double constant) for all i.  For a
 // float x, (double)x < 1e-8 holds exactly when x <= 1e-8f.

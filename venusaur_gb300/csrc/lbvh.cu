@@ -224,12 +224,17 @@ __global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __res
     leafbox[2 * k] = lo;
     leafbox[2 * k + 1] = hi;
     int p = parent_leaf[k];
-    while (p >= 0) {
+    // A Karras tree over unique (code, index) keys is at most 63 levels deep;
+    // the bound only guards against a corrupt parent chain.
+    for (int level = 0; p >= 0 && p < n - 1 && level < 128; ++level) {
         __threadfence();
         if (atomicAdd(arrive + p, 1u) == 0u) return;
         __threadfence();
         int32_t cl = __float_as_int(__ldcg(&nodes[2 * p].w));
         int32_t cr = __float_as_int(__ldcg(&nodes[2 * p + 1].w));
+        const bool ok_l = (cl & kLeaf) ? (cl & ~kLeaf) < n : cl < n - 1;
+        const bool ok_r = (cr & kLeaf) ? (cr & ~kLeaf) < n : cr < n - 1;
+        if (!ok_l || !ok_r) return;
         float4 l0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf)) : __ldcg(nodes + 2 * cl);
         float4 h0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf) + 1) : __ldcg(nodes + 2 * cl + 1);
         float4 l1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & ~kLeaf)) : __ldcg(nodes + 2 * cr);
@@ -272,8 +277,8 @@ void free_scene(venu_scene* s) {
 venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t st, venu_scene* S) {
     S->n = n;
     if (n == 0) return VENU_OK;
-    if (n > (1u << 30)) {
-        set_error("venu_scene_create: more than 2^30 spheres");
+    if (n > (1u << 28)) {
+        set_error("venu_scene_create: more than 2^28 spheres");
         return VENU_ERR_TOO_LARGE;
     }
     const uint32_t ntiles = cdiv(n, kTileKeys);

@@ -65,23 +65,31 @@ __device__ __forceinline__ float rnd(uint32_t& s) {
     return (float)(s & 0x00FFFFFFu) / (float)0x01000000;
 }
 // Core/RayTracer.cu:93-97 with min=-1, max=1; draws x, y, z left to right.
+// The rejection loops stop after kMaxTries candidates (the last one is then
+// kept): an acceptance rate of 52% (sphere) / 79% (disk) makes that bound
+// unreachable in practice, and it guarantees termination on the GPU.
+constexpr int kMaxTries = 4096;
 __device__ __forceinline__ float rnd_pm1(uint32_t& s) { return -1.0f + (1.0f - -1.0f) * rnd(s); }
 __device__ __forceinline__ f3 random_in_unit_sphere(uint32_t& s) {  // :117-125
-    for (;;) {
+    f3 p;
+    for (int i = 0; i < kMaxTries; ++i) {
         float x = rnd_pm1(s);
         float y = rnd_pm1(s);
         float z = rnd_pm1(s);
-        f3 p = mk(x, y, z);
-        if (!(dot(p, p) >= 1.0f)) return p;
+        p = mk(x, y, z);
+        if (!(dot(p, p) >= 1.0f)) break;
     }
+    return p;
 }
 __device__ __forceinline__ f3 random_in_unit_disk(uint32_t& s) {  // :141-149
-    for (;;) {
+    f3 p;
+    for (int i = 0; i < kMaxTries; ++i) {
         float x = rnd_pm1(s);
         float y = rnd_pm1(s);
-        f3 p = mk(x, y, 0.0f);
-        if (!(dot(p, p) >= 1.0f)) return p;
+        p = mk(x, y, 0.0f);
+        if (!(dot(p, p) >= 1.0f)) break;
     }
+    return p;
 }
 // Core/RayTracer.cu:8-13; for float x, (double)x < 1e-8 <=> x <= 1e-8f.
 __device__ __forceinline__ bool near_zero(f3 e) {
@@ -324,7 +332,17 @@ __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPr
             float spill_tn[kSpill];
             int sp = 0;
             int32_t pl = __float_as_int(rlo.w), pr = __float_as_int(rhi.w);
+            // A tree has n-1 internal nodes and each iteration expands the
+            // child pair of a different one; the guard and the index checks
+            // turn a corrupt tree into an error flag instead of a hang.
+            uint32_t guard = 2u * n + 8u;
             for (;;) {
+                if (--guard == 0u || (!(pl & kLeaf) && (uint32_t)pl >= n - 1u) ||
+                    (!(pr & kLeaf) && (uint32_t)pr >= n - 1u) || (uint32_t)(pl & ~kLeaf) >= n ||
+                    (uint32_t)(pr & ~kLeaf) >= n) {
+                    overflow = true;
+                    break;
+                }
                 bool h0 = false, h1 = false;
                 float tn0 = 0.0f, tn1 = 0.0f;
                 int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
