@@ -219,7 +219,10 @@ __global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __res
     if (k >= n) return;
     const venu_sphere& sp = s[vals[k]];
     float r = fabsf(sp.radius);
-    float4 lo = make_float4(__fsub_rd(sp.center[0], r), __fsub_rd(sp.center[1], r), __fsub_rd(sp.center[2], r), 0.0f);
+    // An exactly-zero difference rounds down to -0.0; "+ 0.0f" makes it +0.0
+    // (still a lower bound) so boxes never carry a signed zero.
+    float4 lo = make_float4(__fsub_rd(sp.center[0], r) + 0.0f, __fsub_rd(sp.center[1], r) + 0.0f,
+                            __fsub_rd(sp.center[2], r) + 0.0f, 0.0f);
     float4 hi = make_float4(__fadd_ru(sp.center[0], r), __fadd_ru(sp.center[1], r), __fadd_ru(sp.center[2], r), 0.0f);
     leafbox[2 * k] = lo;
     leafbox[2 * k + 1] = hi;
