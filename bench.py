@@ -141,9 +141,12 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
                    rows=(r0, r0 + rows))
     dt = time.perf_counter() - t0
-    rate = res["segments"] / max(dt, 1e-9)
-    # scale rows to the target time
-    rows = int(max(2, min(H - r0, rows * target_s / max(dt, 1e-3))))
+    # scale rows (up to the lower half of the image), then samples, to the target time
+    grow = target_s / max(dt, 1e-3)
+    new_rows = int(max(2, min(H - r0, rows * grow)))
+    grow /= new_rows / rows
+    rows = new_rows
+    spp_s = int(max(spp_s, min(spp, spp_s * grow)))
     t0 = time.perf_counter()
     res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
                    rows=(r0, r0 + rows))
@@ -211,7 +214,7 @@ def main():
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
-    wf = venu.Wavefront(args.max_paths, profile=True)
+    wf = venu.Wavefront(args.max_paths)
     accum = venu.new_accum(W, H)
     img8 = torch.zeros((H * W, 4), dtype=torch.uint8, device="cuda")
 
@@ -239,8 +242,6 @@ def main():
     e0.record(stream)
     for i in range(args.steps):
         step(args.warmup + i)
-        if i == 0:
-            pass
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
@@ -258,12 +259,23 @@ def main():
     value = total_segs / (ms / 1000.0)
     launches = st["kernel_launches"] * args.steps
 
-    # --- roofline of the traversal kernel: counting pass for bytes ---------
-    wfc = venu.Wavefront(args.max_paths, count=True)
+    # --- roofline of the traversal kernel -----------------------------------
+    # The last timed step is rendered again twice: once with CUDA events
+    # around every traverse/shade launch (per-kernel device time), once with
+    # the counting traversal (nodes visited, spheres tested).  Both are
+    # deterministic replays of the same workload as the timed steps.
+    last_sub = 1 + args.warmup + args.steps - 1
     acc2 = venu.new_accum(W, H)
-    wfc.render(ds, cam, W, H, spp, acc2, subframe=1 + args.warmup + args.steps - 1, max_depth=depth, reset=True)
+    wfp = venu.Wavefront(args.max_paths, profile=True)
+    wfp.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
+    torch.cuda.synchronize()
+    st = wfp.stats()
+    wfp.close()
+    wfc = venu.Wavefront(args.max_paths, count=True)
+    wfc.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
     torch.cuda.synchronize()
     sc = wfc.stats()
+    wfc.close()
     del acc2
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
     # algorithmic bytes of the traversal stage per render: 32 B per node
