@@ -159,6 +159,37 @@ VENU_API venu_status venu_scene_export_bvh(const venu_scene* scene, uint32_t* mo
                                   void* nodes);
 VENU_API venu_status venu_scene_destroy(venu_scene* scene);
 
+/* ---- LBVH build that allocates nothing --------------------------------
+ * No counterpart in the reference (OptiX sizes and allocates its own build
+ * buffers).  For callers that must not allocate device memory: an engine or
+ * server that hands every byte of HBM out from its own pool or budget and
+ * cannot let a library call cudaMalloc behind it, or a per-frame rebuild of
+ * moving spheres that cannot afford the device-wide synchronisation that
+ * cudaMalloc/cudaFree may cause.  It runs the same kernels as
+ * venu_scene_create into buffers the caller owns, asynchronously on
+ * `stream`, and calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Scratch lives in one fixed device array inside the library (about 3.8 MB
+ * for VENU_NOALLOC_MAX_SPHERES spheres), which every GPU that loads the
+ * library holds until the process exits.  n above VENU_NOALLOC_MAX_SPHERES
+ * returns VENU_ERR_TOO_LARGE.  The first call on a device looks up that
+ * array's device address (once per device, with the device current); make
+ * that first call before any stream capture.  All calls share the array and
+ * it keeps the last call's contents: calls whose work overlaps on the GPU
+ * (other streams, other host threads) race and must be serialised.
+ *
+ * Outputs (device, 16-byte aligned where float4):
+ *   nodes_out      (n-1) x 8 floats: {lo.xyz, left} {hi.xyz, right} (n > 1)
+ *   spheres_out    n x 4 floats {center, radius} in Morton slot order
+ *   materials_out  n x 4 floats {albedo, fuzz or ir}
+ *   meta_out       n uint32: original index | material << 30
+ *   morton_out     n uint32: sorted Morton codes
+ * They equal venu_scene_create's LBVH (venu_scene_export_bvh) bit for bit. */
+#define VENU_NOALLOC_MAX_SPHERES 65536u
+VENU_API venu_status venu_lbvh_build_noalloc(const venu_sphere* spheres_dev, uint32_t n, float* nodes_out,
+                                             float* spheres_out, float* materials_out, uint32_t* meta_out,
+                                             uint32_t* morton_out, void* stream);
+
 /* ---- closest hit for arbitrary rays (optixTrace without programs) ----- */
 /* rays_dev: n x 6 floats (origin, direction).  Writes, per ray, the hit
  * distance t (tmax on a miss), the original sphere index (-1 on a miss) and

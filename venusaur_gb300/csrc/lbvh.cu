@@ -15,6 +15,9 @@
 #include "venu_device.cuh"
 #include "venu_internal.h"
 
+#include <algorithm>
+#include <mutex>
+#include <string>
 #include <vector>
 
 namespace venu {
@@ -380,3 +383,132 @@ done:
 }
 
 }  // namespace venu
+
+// ---------------------------------------------------------------------------
+// venu_lbvh_build_noalloc: the same LBVH build into caller-owned buffers,
+// with its scratch in a fixed file-scope device array instead of cudaMalloc.
+// ---------------------------------------------------------------------------
+namespace venu {
+namespace {
+
+constexpr uint32_t kNoAllocMaxSpheres = VENU_NOALLOC_MAX_SPHERES;
+constexpr uint32_t kNoAllocMaxTiles = (kNoAllocMaxSpheres + kTileKeys - 1) / kTileKeys;
+constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kNA = kNoAllocMaxSpheres;
+constexpr size_t kOffBounds = 0;                                      // 6 uint32 + 6 float
+constexpr size_t kOffKeysAlt = al256(kOffBounds + 48);
+constexpr size_t kOffVals = al256(kOffKeysAlt + 4 * kNA);
+constexpr size_t kOffValsAlt = al256(kOffVals + 4 * kNA);
+constexpr size_t kOffHist = al256(kOffValsAlt + 4 * kNA);
+constexpr size_t kOffArrive = al256(kOffHist + 4 * (size_t)kBuckets * kNoAllocMaxTiles);
+constexpr size_t kOffParentInt = al256(kOffArrive + 4 * kNA);
+constexpr size_t kOffParentLeaf = al256(kOffParentInt + 4 * kNA);
+constexpr size_t kOffLeafBox = al256(kOffParentLeaf + 4 * kNA);
+constexpr size_t kNoAllocScratchBytes = al256(kOffLeafBox + 32 * kNA);  // about 3.8 MB
+
+}  // namespace
+}  // namespace venu
+
+// Every GPU that loads the library holds this array until the process exits.
+static __device__ __align__(256) unsigned char g_lbvh_noalloc_scratch[venu::kNoAllocScratchBytes];
+
+namespace venu {
+namespace {
+
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void* g_noalloc_scratch[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The host-side
+// name g_lbvh_noalloc_scratch is only a stand-in: its device address comes
+// from cudaGetSymbolAddress, once per device, with that device current.
+venu_status noalloc_scratch(unsigned char** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "venu_lbvh_build_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("venu_lbvh_build_noalloc: device ordinal out of range");
+        return VENU_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_scratch[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_lbvh_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "venu_lbvh_build_noalloc: cudaGetSymbolAddress");
+        g_noalloc_scratch[dev] = p;
+    }
+    *out = static_cast<unsigned char*>(g_noalloc_scratch[dev]);
+    return VENU_OK;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+}  // namespace venu
+
+extern "C" venu_status venu_lbvh_build_noalloc(const venu_sphere* spheres_dev, uint32_t n, float* nodes_out,
+                                               float* spheres_out, float* materials_out, uint32_t* meta_out,
+                                               uint32_t* morton_out, void* stream) {
+    using namespace venu;
+    if (n > kNoAllocMaxSpheres) {
+        set_error("venu_lbvh_build_noalloc: " + std::to_string(n) + " spheres exceed the limit of " +
+                  std::to_string(kNoAllocMaxSpheres) + " (VENU_NOALLOC_MAX_SPHERES); use venu_scene_create");
+        return VENU_ERR_TOO_LARGE;
+    }
+    if (n == 0) return VENU_OK;
+    if (!spheres_dev || !spheres_out || !materials_out || !meta_out || !morton_out || (n > 1 && !nodes_out)) {
+        set_error("venu_lbvh_build_noalloc: NULL buffer");
+        return VENU_ERR_INVALID;
+    }
+    if (!aligned16(spheres_out) || !aligned16(materials_out) || (n > 1 && !aligned16(nodes_out))) {
+        set_error("venu_lbvh_build_noalloc: nodes/spheres/materials outputs must be 16-byte aligned");
+        return VENU_ERR_INVALID;
+    }
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    unsigned char* base = nullptr;
+    venu_status ss = noalloc_scratch(&base);
+    if (ss != VENU_OK) return ss;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t* bu = reinterpret_cast<uint32_t*>(base + kOffBounds);
+    float* bounds = reinterpret_cast<float*>(base + kOffBounds + 24);
+    uint32_t* keys_alt = reinterpret_cast<uint32_t*>(base + kOffKeysAlt);
+    uint32_t* vals = reinterpret_cast<uint32_t*>(base + kOffVals);
+    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(base + kOffValsAlt);
+    uint32_t* hist = reinterpret_cast<uint32_t*>(base + kOffHist);
+    uint32_t* arrive = reinterpret_cast<uint32_t*>(base + kOffArrive);
+    int32_t* pint = reinterpret_cast<int32_t*>(base + kOffParentInt);
+    int32_t* pleaf = reinterpret_cast<int32_t*>(base + kOffParentLeaf);
+    float4* leafbox = reinterpret_cast<float4*>(base + kOffLeafBox);
+    const uint32_t nint = n > 1 ? n - 1 : 1;
+    const uint32_t ntiles = cdiv(n, kTileKeys);
+    // The scratch keeps the previous call's contents: reset what must start
+    // from a known value (min/max seeds of the bounds, arrival counters,
+    // parent links).
+    VENU_CUDA(cudaMemsetAsync(bu, 0xff, 3 * sizeof(uint32_t), st));
+    VENU_CUDA(cudaMemsetAsync(bu + 3, 0x00, 3 * sizeof(uint32_t), st));
+    VENU_CUDA(cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * nint, st));
+    VENU_CUDA(cudaMemsetAsync(pint, 0xff, sizeof(int32_t) * nint, st));
+    VENU_CUDA(cudaMemsetAsync(pleaf, 0xff, sizeof(int32_t) * n, st));
+    const uint32_t blocks = std::min(cdiv(n, 256), (uint32_t)(sm_count() * 8));
+    k_bounds<<<blocks, 256, 0, st>>>(spheres_dev, n, bu);
+    k_morton<<<blocks, 256, 0, st>>>(spheres_dev, n, bu, bounds, morton_out, vals);
+    uint32_t *kin = morton_out, *kout = keys_alt, *vin = vals, *vout = vals_alt;
+    const uint32_t sblocks = cdiv(ntiles, kWarpsPerBlock);
+    for (int shift = 0; shift < 32; shift += kRadixBits) {
+        k_hist<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, n, shift, ntiles, hist);
+        k_scan<<<1, 1024, 0, st>>>(hist, (uint32_t)(kBuckets * ntiles));
+        k_scatter<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, vin, n, shift, ntiles, hist, kout, vout);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    float4* nodes = reinterpret_cast<float4*>(nodes_out);
+    if (n > 1) {
+        k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(morton_out, (int)n, nodes, pint, pleaf);
+        k_refit<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, (int)n, nodes, pint, pleaf, leafbox, arrive);
+    }
+    k_gather<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, n, reinterpret_cast<float4*>(spheres_out),
+                                          reinterpret_cast<float4*>(materials_out), meta_out);
+    VENU_CUDA(cudaGetLastError());
+    return VENU_OK;
+}
