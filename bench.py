@@ -195,6 +195,7 @@ def main():
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--max-paths", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     world, rank, local, dist = dist_setup(args.gpus)
@@ -214,7 +215,17 @@ def main():
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
-    wf = venu.Wavefront(args.max_paths)
+    tuning, tune_log = None, []
+    max_paths = args.max_paths
+    if not args.no_autotune:
+        from venusaur_gb300 import tune
+
+        tuning, best_mp, tune_log = tune.autotune(
+            ds, cam, W, H, spp, depth, max_paths=(args.max_paths,) if args.max_paths else (4 << 20, 8 << 20, 16 << 20))
+        max_paths = best_mp
+    wf = venu.Wavefront(max_paths)
+    if tuning:
+        wf.set_tuning(**tuning)
     accum = venu.new_accum(W, H)
     img8 = torch.zeros((H * W, 4), dtype=torch.uint8, device="cuda")
 
@@ -266,12 +277,16 @@ def main():
     # deterministic replays of the same workload as the timed steps.
     last_sub = 1 + args.warmup + args.steps - 1
     acc2 = venu.new_accum(W, H)
-    wfp = venu.Wavefront(args.max_paths, profile=True)
+    wfp = venu.Wavefront(max_paths, profile=True)
+    if tuning:
+        wfp.set_tuning(**tuning)
     wfp.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
     torch.cuda.synchronize()
     st = wfp.stats()
     wfp.close()
-    wfc = venu.Wavefront(args.max_paths, count=True)
+    wfc = venu.Wavefront(max_paths, count=True)
+    if tuning:
+        wfc.set_tuning(**tuning)
     wfc.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
     torch.cuda.synchronize()
     sc = wfc.stats()
@@ -303,7 +318,9 @@ def main():
 
     host_sph = torch.from_numpy(spheres.view(np.uint8)).pin_memory()
     host_img = torch.empty((H * W, 4), dtype=torch.uint8).pin_memory()
-    wf_plain = venu.Wavefront(args.max_paths)
+    wf_plain = venu.Wavefront(max_paths)
+    if tuning:
+        wf_plain.set_tuning(**tuning)
     cam_np = np.ascontiguousarray(cam)
     h = C.c_void_p(stream.cuda_stream)
 
@@ -340,7 +357,9 @@ def main():
                    "spheres": int(len(spheres)), "method": "plain single-scene wavefront",
                    "l2": "working set (ray queues > 1.5 GB) larger than L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "segments_per_step": segs_step, "paths_per_step": st["paths"]},
+                   "segments_per_step": segs_step, "paths_per_step": st["paths"],
+                   "tuning": dict(wf.tuning(), max_paths=max_paths),
+                   "autotune_candidates": len(tune_log)},
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": e2e,

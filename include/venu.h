@@ -214,6 +214,20 @@ VENU_API venu_status venu_render(venu_renderer* r, const venu_scene* scene, cons
                         const venu_render_opts* opts, float* accum_dev, float* image_f_dev,
                         uint8_t* image8_dev, void* stream);
 VENU_API venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* out);
+
+/* Launch shapes and traversal variant of a renderer (chosen by the
+ * autotuner, venusaur_gb300/tune.py; results do not depend on them). */
+typedef struct venu_tuning {
+    uint32_t traverse_variant;       /* 0: each warp takes 32 rays and runs them to the end;
+                                        1: idle lanes take new rays (default) */
+    uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
+    uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
+    uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
+    uint32_t shade_block;            /* threads per shade block: 64..512, multiple of 32 */
+    uint32_t shade_blocks_per_sm;    /* 0 = as many as fit */
+} venu_tuning;
+VENU_API venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tuning* t);
+VENU_API venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tuning* t);
 VENU_API venu_status venu_renderer_destroy(venu_renderer* r);
 
 #ifdef __cplusplus

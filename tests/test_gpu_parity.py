@@ -224,3 +224,34 @@ def test_empty_and_tiny_scenes(venu, oracle, cuda):
         acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, 2, 0, 10)
         want = oracle.render(sp, cam, W, H, 2, subframe=0, max_depth=10, mode=pyoracle.MODE_GB300)
         assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
+
+
+@pytest.mark.parametrize("tuning", [
+    dict(traverse_variant=0, refill_min=32, traverse_block=64, shade_block=128),
+    dict(traverse_variant=1, refill_min=1, traverse_block=256, shade_block=64),
+    dict(traverse_variant=1, refill_min=16, traverse_block=128, shade_block=512, traverse_blocks_per_sm=2),
+])
+def test_render_tunings_bit_exact(venu, oracle, cuda, tuning):
+    """Launch shapes and traversal variants change speed, never bits."""
+    torch = cuda
+    sp = oracle.scene_rtiow(0)
+    W, H, spp, depth = 40, 24, 3, 12
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    ds = venu.DeviceScene(sp)
+    wf = venu.Wavefront(1500)
+    wf.set_tuning(**tuning)
+    assert {k: wf.tuning()[k] for k in tuning} == tuning
+    accum = venu.new_accum(W, H)
+    wf.render(ds, cam, W, H, spp, accum, subframe=2, max_depth=depth, reset=True)
+    torch.cuda.synchronize()
+    want = oracle.render(sp, cam, W, H, spp, subframe=2, max_depth=depth, mode=pyoracle.MODE_GB300)
+    assert np.array_equal(accum.cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
+    assert wf.stats()["segments"] == want["segments"]
+
+
+def test_tuning_rejects_bad_values(venu, cuda):
+    wf = venu.Wavefront(1000)
+    with pytest.raises(venu.VenuError):
+        wf.set_tuning(traverse_block=96)
+    with pytest.raises(venu.VenuError):
+        wf.set_tuning(refill_min=0)

@@ -58,6 +58,12 @@ class RenderStats(C.Structure):
                 ("traverse_launches", C.c_uint32), ("shade_launches", C.c_uint32)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("traverse_variant", C.c_uint32), ("refill_min", C.c_uint32), ("traverse_block", C.c_uint32),
+                ("traverse_blocks_per_sm", C.c_uint32), ("shade_block", C.c_uint32),
+                ("shade_blocks_per_sm", C.c_uint32)]
+
+
 _lib = None
 
 
@@ -91,10 +97,13 @@ def lib() -> C.CDLL:
     L.venu_render.argtypes = [vp, vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp]
     L.venu_renderer_stats.argtypes = [vp, C.POINTER(RenderStats)]
     L.venu_renderer_destroy.argtypes = [vp]
+    L.venu_renderer_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.venu_renderer_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     for name in ("venu_device_check", "venu_scene_generate_random", "venu_scene_create",
                  "venu_scene_create_device", "venu_scene_info_get", "venu_scene_export_bvh",
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
-                 "venu_renderer_stats", "venu_renderer_destroy"):
+                 "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
+                 "venu_renderer_get_tuning"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

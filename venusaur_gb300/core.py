@@ -13,7 +13,10 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import CAMERA_DTYPE, NODE_DTYPE, SPHERE_DTYPE, RenderOpts, RenderStats, SceneInfo, check, lib, ptr
+from ._lib import CAMERA_DTYPE, NODE_DTYPE, SPHERE_DTYPE, RenderOpts, RenderStats, SceneInfo, Tuning, check, lib, ptr
+
+TUNING_FIELDS = ("traverse_variant", "refill_min", "traverse_block", "traverse_blocks_per_sm", "shade_block",
+                 "shade_blocks_per_sm")
 
 
 def _torch():
@@ -303,6 +306,18 @@ class Wavefront:
         cam = np.ascontiguousarray(camera, CAMERA_DTYPE)
         check(lib().venu_render(self.handle, scene.handle, ptr(cam), C.byref(o), ptr(accum), ptr(image_f),
                                 ptr(image8), _stream_handle(stream)))
+
+    def set_tuning(self, **kw) -> None:
+        """Launch shapes / traversal variant (venu_tuning); unspecified fields keep their value."""
+        cur = self.tuning()
+        cur.update(kw)
+        t = Tuning(*(int(cur[f]) for f in TUNING_FIELDS))
+        check(lib().venu_renderer_set_tuning(self.handle, C.byref(t)))
+
+    def tuning(self) -> dict:
+        t = Tuning()
+        check(lib().venu_renderer_get_tuning(self.handle, C.byref(t)))
+        return {f: int(getattr(t, f)) for f in TUNING_FIELDS}
 
     def stats(self) -> dict:
         s = RenderStats()

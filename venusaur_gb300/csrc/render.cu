@@ -44,7 +44,7 @@ __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, u
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
+__global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                   uint32_t* __restrict__ work, int2* __restrict__ hits,
                                                   uint32_t* __restrict__ err,
                                                   unsigned long long* __restrict__ stats) {
@@ -85,7 +85,79 @@ __global__ void __launch_bounds__(128) k_traverse(SceneView S, Queue q, const ui
     }
 }
 
-__global__ void __launch_bounds__(256) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
+// Persistent lanes: a lane whose ray is finished takes a new one as soon as
+// at least `refill_min` lanes of its warp are idle (one atomic per refill),
+// so warps stay full while the queue lasts instead of waiting for their
+// slowest ray (dynamic fetch, Aila & Laine 2009).
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
+                                                      uint32_t* __restrict__ work, int2* __restrict__ hits,
+                                                      uint32_t* __restrict__ err,
+                                                      unsigned long long* __restrict__ stats, uint32_t refill_min) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.pair = reinterpret_cast<int2*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    const uint32_t n = *cnt;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt = (1u << lane) - 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    Tracer<COUNT> T;
+    int2 spill[kSpill];
+    float spill_tn[kSpill];
+    uint32_t ray = 0;
+    bool active = false, exhausted = false;
+    for (;;) {
+        const uint32_t idle = __ballot_sync(0xffffffffu, !active);
+        if (!exhausted && (idle == 0xffffffffu || (uint32_t)__popc(idle) >= refill_min)) {
+            const uint32_t k = (uint32_t)__popc(idle);
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(work, k);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + k >= n) exhausted = true;
+            if (!active) {
+                const uint32_t my = base + (uint32_t)__popc(idle & lt);
+                if (my < n) {
+                    ray = my;
+                    const float4 o4 = q.o[my], d4 = q.d[my];
+                    if (T.begin(S, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), 0.001f, 1e16f, K)) {
+                        active = true;
+                    } else {
+                        float t;
+                        const int32_t kk = T.result(t);
+                        hits[my] = make_int2(__float_as_int(t), kk);
+                    }
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active && !T.step(S, sm, threadIdx.x, blockDim.x, spill, spill_tn, overflow, K)) {
+            active = false;
+            float t;
+            const int32_t kk = T.result(t);
+            hits[ray] = make_int2(__float_as_int(t), kk);
+        }
+    }
+    if (overflow) atomicOr(err, 1u);
+    if (COUNT) {
+        unsigned long long a = K.nodes, b = K.spheres;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+        }
+        if (lane == 0) {
+            atomicAdd(stats + 1, a);
+            atomicAdd(stats + 2, b);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
                                                const uint32_t* __restrict__ cnt_in, Queue qout,
                                                uint32_t* __restrict__ cnt_out, float4* __restrict__ slots) {
     const uint32_t n = *cnt_in;
@@ -196,6 +268,7 @@ struct venu_renderer {
     uint32_t* work = nullptr;  // [65]
     uint32_t* err = nullptr;
     unsigned long long* stats = nullptr;  // segments, nodes, spheres
+    venu_tuning tune = {1u, 8u, 128u, 0u, 256u, 0u};
     int trav_blocks = 0, shade_blocks = 0;
     venu_render_stats last = {};
     // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
@@ -204,9 +277,37 @@ struct venu_renderer {
 };
 
 namespace {
-constexpr int kTravBlock = 128;
-constexpr int kShadeBlock = 256;
+constexpr int kTravBlock = 128;  // venu_trace
 constexpr uint32_t kMaxDepth = 64;
+
+template <typename K>
+cudaError_t occupancy_grid(K kernel, int block, size_t smem, uint32_t per_sm_cap, int& grid) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
+    if (e != cudaSuccess) return e;
+    per_sm = std::max(1, per_sm);
+    if (per_sm_cap) per_sm = std::min(per_sm, (int)per_sm_cap);
+    grid = per_sm * sm_count();
+    return cudaSuccess;
+}
+
+// Persistent grids: as many resident blocks as fit (or the tuned cap) on every SM.
+cudaError_t configure(venu_renderer* r) {
+    const venu_tuning& t = r->tune;
+    const size_t sm = traverse_smem((int)t.traverse_block);
+    cudaError_t e;
+    if (t.traverse_variant == 0) {
+        e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    } else {
+        e = occupancy_grid(k_traverse_dyn<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_traverse_dyn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    }
+    if (e == cudaSuccess) e = occupancy_grid(k_shade, (int)t.shade_block, 0, t.shade_blocks_per_sm, r->shade_blocks);
+    return e;
+}
 
 // Returns an event pair for the next profiled launch, growing the pool.
 cudaError_t next_events(venu_renderer* r, cudaEvent_t& a, cudaEvent_t& b) {
@@ -271,20 +372,7 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 4);
     if (e == cudaSuccess) e = cudaMemset(r->err, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(r->stats, 0, sizeof(unsigned long long) * 4);
-    if (e == cudaSuccess) {
-        const size_t sm = traverse_smem(kTravBlock);
-        e = cudaFuncSetAttribute(k_traverse<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        int per_sm = 0;
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_traverse<false>, kTravBlock, sm);
-        r->trav_blocks = std::max(1, per_sm) * sm_count();
-        int per_sm2 = 0;
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_shade, kShadeBlock, 0);
-        r->shade_blocks = std::max(1, per_sm2) * sm_count();
-    }
+    if (e == cudaSuccess) e = configure(r);
     if (e != cudaSuccess) {
         free_renderer(r);
         delete r;
@@ -292,6 +380,39 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
                                               : cuda_fail(e, "venu_renderer_create");
     }
     *out = r;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tuning* t) {
+    if (!r || !t) {
+        set_error("venu_renderer_set_tuning: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    const bool ok = t->traverse_variant <= 1u && t->refill_min >= 1u && t->refill_min <= 32u &&
+                    (t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) &&
+                    t->shade_block >= 64u && t->shade_block <= 512u && (t->shade_block % 32u) == 0u &&
+                    t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u;
+    if (!ok) {
+        set_error("venu_renderer_set_tuning: value out of range");
+        return VENU_ERR_INVALID;
+    }
+    const venu_tuning old = r->tune;
+    r->tune = *t;
+    cudaError_t e = configure(r);
+    if (e != cudaSuccess) {
+        r->tune = old;
+        configure(r);
+        return cuda_fail(e, "venu_renderer_set_tuning");
+    }
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tuning* t) {
+    if (!r || !t) {
+        set_error("venu_renderer_get_tuning: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    *t = r->tune;
     return VENU_OK;
 }
 
@@ -336,8 +457,9 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     const bool count = (r->flags & VENU_RENDERER_COUNT) != 0;
     const bool prof = (r->flags & VENU_RENDERER_PROFILE) != 0;
     r->ev_used = 0;
-    std::vector<uint8_t> kinds;  // 0 traverse, 1 shade, per event pair
-    const size_t tsm = traverse_smem(kTravBlock);
+    const venu_tuning& tu = r->tune;
+    const size_t tsm = traverse_smem((int)tu.traverse_block);
+    const int tb = (int)tu.traverse_block, sb = (int)tu.shade_block;
     float4* accum = reinterpret_cast<float4*>(accum_dev);
     uint32_t launches = 0, waves = 0;
     // wave shape: all pixels x k samples, or P pixels x 1 sample
@@ -366,18 +488,26 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                     VENU_CUDA(next_events(r, e2, e3));
                     VENU_CUDA(cudaEventRecord(e0, st));
                 }
-                if (count)
-                    k_traverse<true><<<r->trav_blocks, kTravBlock, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
-                                                                             r->err, r->stats);
-                else
-                    k_traverse<false><<<r->trav_blocks, kTravBlock, tsm, st>>>(S, qi, r->cnt + b, r->work + b,
-                                                                              r->hits, r->err, r->stats);
+                if (tu.traverse_variant == 0) {
+                    if (count)
+                        k_traverse<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
+                                                                         r->err, r->stats);
+                    else
+                        k_traverse<false><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
+                                                                          r->err, r->stats);
+                } else {
+                    if (count)
+                        k_traverse_dyn<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
+                                                                             r->err, r->stats, tu.refill_min);
+                    else
+                        k_traverse_dyn<false><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b,
+                                                                              r->hits, r->err, r->stats, tu.refill_min);
+                }
                 if (prof) {
                     VENU_CUDA(cudaEventRecord(e1, st));
                     VENU_CUDA(cudaEventRecord(e2, st));
                 }
-                k_shade<<<r->shade_blocks, kShadeBlock, 0, st>>>(S, qi, r->hits, r->cnt + b, qo, r->cnt + b + 1,
-                                                                 r->slots);
+                k_shade<<<r->shade_blocks, sb, 0, st>>>(S, qi, r->hits, r->cnt + b, qo, r->cnt + b + 1, r->slots);
                 if (prof) VENU_CUDA(cudaEventRecord(e3, st));
                 launches += 2;
             }
@@ -392,7 +522,6 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
         ++launches;
     }
     VENU_CUDA(cudaGetLastError());
-    (void)kinds;
     r->last = venu_render_stats{};
     r->last.paths = (uint64_t)npix * spp;
     r->last.waves = waves;

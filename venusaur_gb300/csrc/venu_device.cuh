@@ -300,133 +300,165 @@ struct TraceCounters {
     uint32_t nodes, spheres;
 };
 
+// Per-lane traversal state.  begin() prepares a ray and tests the root;
+// step() expands one child pair (or pops); both return whether more work
+// remains.  The same state machine serves the one-ray-per-thread kernels
+// (trace_closest) and the persistent kernels that refill idle lanes.
+template <bool COUNT>
+struct Tracer {
+    RayPre R;
+    float tmin, tmax, best_t;
+    int32_t best, pl, pr;
+    int sp;
+    uint32_t guard;
+
+    __device__ __forceinline__ void leaf(const SceneView& S, int32_t k, TraceCounters& K) {
+        float t;
+        if (COUNT) ++K.spheres;
+        float4 s4 = __ldg(S.sph + k);
+        if (sphere_test(R, s4, tmin, tmax, t) && (t < best_t || (t == best_t && k < best))) {
+            best_t = t;
+            best = k;
+        }
+    }
+
+    __device__ __forceinline__ bool begin(const SceneView& S, f3 o, f3 d, float tmin_, float tmax_,
+                                          TraceCounters& K) {
+        R = prep(o, d);
+        tmin = tmin_;
+        tmax = tmax_;
+        best_t = tmax_;
+        best = kNone;
+        sp = 0;
+        const uint32_t n = S.n;
+        if (n == 0) return false;
+        if (n == 1) {
+            leaf(S, 0, K);
+            return false;
+        }
+        float tn;
+        float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
+        if (COUNT) ++K.nodes;
+        if (!box_test(R, rlo, rhi, tmin, best_t, tn)) return false;
+        pl = __float_as_int(rlo.w);
+        pr = __float_as_int(rhi.w);
+        // A tree has n-1 internal nodes and each step expands the child pair
+        // of a different one; the guard and the index checks turn a corrupt
+        // tree into an error flag instead of a hang.
+        guard = 2u * n + 8u;
+        return true;
+    }
+
+    // spill / spill_tn: this thread's local-memory stack entries beyond the
+    // kShared in shared memory.
+    __device__ __forceinline__ bool step(const SceneView& S, StackSmem sm, uint32_t tid, uint32_t bdim,
+                                         int2* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
+        const uint32_t n = S.n;
+        if (--guard == 0u || (!(pl & kLeaf) && (uint32_t)pl >= n - 1u) || (!(pr & kLeaf) && (uint32_t)pr >= n - 1u) ||
+            (uint32_t)(pl & ~kLeaf) >= n || (uint32_t)(pr & ~kLeaf) >= n) {
+            overflow = true;
+            return false;
+        }
+        bool h0 = false, h1 = false;
+        float tn0 = 0.0f, tn1 = 0.0f;
+        int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
+        if (pl & kLeaf) {
+            leaf(S, pl & ~kLeaf, K);
+        } else {
+            float4 lo = __ldg(S.nodes + 2 * pl), hi = __ldg(S.nodes + 2 * pl + 1);
+            if (COUNT) ++K.nodes;
+            h0 = box_test(R, lo, hi, tmin, best_t, tn0);
+            c0l = __float_as_int(lo.w);
+            c0r = __float_as_int(hi.w);
+        }
+        if (pr & kLeaf) {
+            leaf(S, pr & ~kLeaf, K);
+        } else {
+            float4 lo = __ldg(S.nodes + 2 * pr), hi = __ldg(S.nodes + 2 * pr + 1);
+            if (COUNT) ++K.nodes;
+            h1 = box_test(R, lo, hi, tmin, best_t, tn1);
+            c1l = __float_as_int(lo.w);
+            c1r = __float_as_int(hi.w);
+        }
+        if (h0 && h1) {
+            int2 far;
+            float far_tn;
+            if (tn1 < tn0) {
+                far = make_int2(c0l, c0r);
+                far_tn = tn0;
+                pl = c1l;
+                pr = c1r;
+            } else {
+                far = make_int2(c1l, c1r);
+                far_tn = tn1;
+                pl = c0l;
+                pr = c0r;
+            }
+            const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
+            if (sp >= kShared) {
+                const int g = sp - kShared;
+                if (g >= kSpill) {
+                    overflow = true;
+                    return false;
+                }
+                spill[g] = sm.pair[j];
+                spill_tn[g] = sm.tn[j];
+            }
+            sm.pair[j] = far;
+            sm.tn[j] = far_tn;
+            ++sp;
+            return true;
+        }
+        if (h0) {
+            pl = c0l;
+            pr = c0r;
+            return true;
+        }
+        if (h1) {
+            pl = c1l;
+            pr = c1r;
+            return true;
+        }
+        while (sp > 0) {
+            --sp;
+            const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
+            int2 e = sm.pair[j];
+            float etn = sm.tn[j];
+            if (sp >= kShared) {
+                sm.pair[j] = spill[sp - kShared];
+                sm.tn[j] = spill_tn[sp - kShared];
+            }
+            if (etn <= best_t) {
+                pl = e.x;
+                pr = e.y;
+                return true;
+            }
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ int32_t result(float& t) const {
+        if (best == kNone) {
+            t = tmax;
+            return -1;
+        }
+        t = best_t;
+        return best;
+    }
+};
+
 template <bool COUNT>
 __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPre& R, float tmin,
                                                  float tmax, float& t_out, StackSmem sm,
                                                  uint32_t tid, uint32_t bdim, bool& overflow,
                                                  TraceCounters& K) {
-    float best_t = tmax;
-    int32_t best = kNone;
-    const uint32_t n = S.n;
-    if (n == 0) {
-        t_out = tmax;
-        return -1;
-    }
-    auto leaf = [&](int32_t k) {
-        float t;
-        if (COUNT) ++K.spheres;
-        float4 sp = __ldg(S.sph + k);
-        if (sphere_test(R, sp, tmin, tmax, t) && (t < best_t || (t == best_t && k < best))) {
-            best_t = t;
-            best = k;
+    Tracer<COUNT> T;
+    int2 spill[kSpill];
+    float spill_tn[kSpill];
+    if (T.begin(S, R.o, R.d, tmin, tmax, K))
+        while (T.step(S, sm, tid, bdim, spill, spill_tn, overflow, K)) {
         }
-    };
-    if (n == 1) {
-        leaf(0);
-    } else {
-        float tn;
-        float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
-        if (COUNT) ++K.nodes;
-        if (box_test(R, rlo, rhi, tmin, best_t, tn)) {
-            int2 spill[kSpill];
-            float spill_tn[kSpill];
-            int sp = 0;
-            int32_t pl = __float_as_int(rlo.w), pr = __float_as_int(rhi.w);
-            // A tree has n-1 internal nodes and each iteration expands the
-            // child pair of a different one; the guard and the index checks
-            // turn a corrupt tree into an error flag instead of a hang.
-            uint32_t guard = 2u * n + 8u;
-            for (;;) {
-                if (--guard == 0u || (!(pl & kLeaf) && (uint32_t)pl >= n - 1u) ||
-                    (!(pr & kLeaf) && (uint32_t)pr >= n - 1u) || (uint32_t)(pl & ~kLeaf) >= n ||
-                    (uint32_t)(pr & ~kLeaf) >= n) {
-                    overflow = true;
-                    break;
-                }
-                bool h0 = false, h1 = false;
-                float tn0 = 0.0f, tn1 = 0.0f;
-                int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
-                if (pl & kLeaf) {
-                    leaf(pl & ~kLeaf);
-                } else {
-                    float4 lo = __ldg(S.nodes + 2 * pl), hi = __ldg(S.nodes + 2 * pl + 1);
-                    if (COUNT) ++K.nodes;
-                    h0 = box_test(R, lo, hi, tmin, best_t, tn0);
-                    c0l = __float_as_int(lo.w);
-                    c0r = __float_as_int(hi.w);
-                }
-                if (pr & kLeaf) {
-                    leaf(pr & ~kLeaf);
-                } else {
-                    float4 lo = __ldg(S.nodes + 2 * pr), hi = __ldg(S.nodes + 2 * pr + 1);
-                    if (COUNT) ++K.nodes;
-                    h1 = box_test(R, lo, hi, tmin, best_t, tn1);
-                    c1l = __float_as_int(lo.w);
-                    c1r = __float_as_int(hi.w);
-                }
-                if (h0 && h1) {
-                    int2 far;
-                    float far_tn;
-                    if (tn1 < tn0) {
-                        far = make_int2(c0l, c0r);
-                        far_tn = tn0;
-                        pl = c1l;
-                        pr = c1r;
-                    } else {
-                        far = make_int2(c1l, c1r);
-                        far_tn = tn1;
-                        pl = c0l;
-                        pr = c0r;
-                    }
-                    // push
-                    const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
-                    if (sp >= kShared) {
-                        const int g = sp - kShared;
-                        if (g >= kSpill) {
-                            overflow = true;
-                            break;
-                        }
-                        spill[g] = sm.pair[j];
-                        spill_tn[g] = sm.tn[j];
-                    }
-                    sm.pair[j] = far;
-                    sm.tn[j] = far_tn;
-                    ++sp;
-                } else if (h0) {
-                    pl = c0l;
-                    pr = c0r;
-                } else if (h1) {
-                    pl = c1l;
-                    pr = c1r;
-                } else {
-                    bool found = false;
-                    while (sp > 0) {
-                        --sp;
-                        const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
-                        int2 e = sm.pair[j];
-                        float etn = sm.tn[j];
-                        if (sp >= kShared) {
-                            sm.pair[j] = spill[sp - kShared];
-                            sm.tn[j] = spill_tn[sp - kShared];
-                        }
-                        if (etn <= best_t) {
-                            pl = e.x;
-                            pr = e.y;
-                            found = true;
-                            break;
-                        }
-                    }
-                    if (!found) break;
-                }
-            }
-        }
-    }
-    if (best == kNone) {
-        t_out = tmax;
-        return -1;
-    }
-    t_out = best_t;
-    return best;
+    return T.result(t_out);
 }
 
 // ---------------------------------------------------------------------------

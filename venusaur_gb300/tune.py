@@ -1,0 +1,69 @@
+"""Autotuner for the wavefront renderer's launch shapes.
+
+Times candidate venu_tuning settings (traversal variant, refill threshold,
+block shapes, resident blocks per SM) and queue sizes (paths in flight) on a
+reduced copy of the caller's workload -- the same scene, camera, resolution
+and depth with fewer samples per pixel -- and returns the fastest.  Results
+never change the image (every setting is bit-identical); only speed differs.
+"""
+from __future__ import annotations
+
+import itertools
+
+from .core import DeviceScene, Wavefront, new_accum
+
+DEFAULT_SPACE = {
+    "traverse_variant": (0, 1),
+    "refill_min": (4, 8, 16),
+    "traverse_block": (64, 128, 256),
+    "shade_block": (128, 256),
+}
+
+
+def candidates(space=None):
+    space = dict(DEFAULT_SPACE, **(space or {}))
+    seen = set()
+    for v, r, tb, sb in itertools.product(space["traverse_variant"], space["refill_min"],
+                                          space["traverse_block"], space["shade_block"]):
+        key = (v, r if v == 1 else 32, tb, sb)
+        if key in seen:
+            continue
+        seen.add(key)
+        yield dict(traverse_variant=v, refill_min=key[1], traverse_block=tb, traverse_blocks_per_sm=0,
+                   shade_block=sb, shade_blocks_per_sm=0)
+
+
+def time_render(wf: Wavefront, scene: DeviceScene, cam, W, H, spp, depth, accum, reps=2):
+    import torch
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    wf.render(scene, cam, W, H, spp, accum, subframe=1, max_depth=depth, reset=True)  # warm
+    ev0.record()
+    for i in range(reps):
+        wf.render(scene, cam, W, H, spp, accum, subframe=2 + i, max_depth=depth, reset=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    segs = wf.stats()["segments"]
+    ms = ev0.elapsed_time(ev1) / reps
+    return segs / (ms / 1000.0), ms
+
+
+def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8 << 20,), tune_spp=None,
+             reps=2, log=None):
+    """Returns (best_tuning: dict, best_max_paths: int, results: list)."""
+    tune_spp = tune_spp or max(1, min(spp, 8))
+    accum = new_accum(W, H)
+    results = []
+    best = None
+    for mp in max_paths:
+        wf = Wavefront(mp)
+        for cand in candidates(space):
+            wf.set_tuning(**cand)
+            rate, ms = time_render(wf, scene, cam, W, H, tune_spp, depth, accum, reps)
+            results.append(dict(cand, max_paths=mp, segments_per_s=rate, ms=ms))
+            if log:
+                log(results[-1])
+            if best is None or rate > best[0]:
+                best = (rate, dict(cand), mp)
+        wf.close()
+    return best[1], best[2], results
