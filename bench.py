@@ -293,22 +293,37 @@ def main():
     wfc.close()
     del acc2
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
-    # algorithmic bytes of the traversal stage per render: 32 B per node
-    # record visited, 16 B per sphere tested, 32 B ray read + 8 B hit write
-    trav_bytes = nodes * 32 + sph * 16 + sc["segments"] * (32 + 8)
-    per_launch_bytes = trav_bytes / max(1, st["traverse_launches"])
+    segs_c, paths_c = sc["segments"], sc["paths"]
+    fused = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"]) == 2
+    # Algorithmic bytes of the dominant kernel per render.  Traversal: 32 B per
+    # node record tested, 16 B per sphere tested, 32 B ray read.  Separate
+    # traversal kernel: + 8 B hit write.  Fused traverse+shade kernel: + 16 B
+    # throughput/seed read, 36 B sphere+material+meta read, 48 B continuation
+    # write per continuing segment, 16 B radiance slot per finished path.
+    trav_bytes = nodes * 32 + sph * 16 + segs_c * 32
+    if fused:
+        kernel = "k_trace_shade"
+        kbytes = trav_bytes + segs_c * (16 + 36) + (segs_c - paths_c) * 48 + paths_c * 16
+    else:
+        kernel = "k_traverse"
+        kbytes = trav_bytes + segs_c * 8
+    per_launch_bytes = kbytes / max(1, st["traverse_launches"])
     avg_launch_ms = st["traverse_ms"] / max(1, st["traverse_launches"])
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
-    # FP32 issue view (per segment, SURVEY-style estimate): 20 flop/node, 25/sphere
-    trav_flops = nodes * 20 + sph * 25
+    # FP32 view (SURVEY-style per-segment estimate): 20 flop per box, 25 per
+    # sphere, 60 per shade; peak = 152 SMs x 128 lanes x 2 x max SM clock
+    kflops = nodes * 20 + sph * 25 + (segs_c * 60 if fused else 0)
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_kind": peak_kind, "traffic": None, "kernel": "k_traverse",
-        "bytes_per_segment": trav_bytes / max(1, sc["segments"]),
-        "nodes_per_segment": nodes / max(1, sc["segments"]), "spheres_per_segment": sph / max(1, sc["segments"]),
-        "traverse_share": st["traverse_ms"] / max(1e-9, ms / args.steps),
-        "fp32_tflops": trav_flops / (st["traverse_ms"] / 1000.0) / 1e12,
+        "peak_kind": peak_kind, "traffic": None, "kernel": kernel,
+        "bytes_per_segment": kbytes / max(1, segs_c),
+        "nodes_per_segment": nodes / max(1, segs_c), "spheres_per_segment": sph / max(1, segs_c),
+        "kernel_share": st["traverse_ms"] / max(1e-9, ms / args.steps),
+        "note": "algorithmic bytes; the node set of this scene is L1/L2-resident, so DRAM carries "
+                "only the ray queues and the kernel is issue-bound (see profiles/)",
+        "fp32_tflops": kflops / (st["traverse_ms"] / 1000.0) / 1e12, "fp32_peak_tflops": fp32_peak,
     }
 
     # --- end-to-end through the C ABI from host memory ----------------------

@@ -219,7 +219,9 @@ VENU_API venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* ou
  * autotuner, venusaur_gb300/tune.py; results do not depend on them). */
 typedef struct venu_tuning {
     uint32_t traverse_variant;       /* 0: each warp takes 32 rays and runs them to the end;
-                                        1: idle lanes take new rays (default) */
+                                        1: idle lanes take new rays (default);
+                                        2: as 0, then the warp shades its 32 hits in the same
+                                           kernel (no separate shade launch) */
     uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */

@@ -157,6 +157,72 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     }
 }
 
+// Traverse and shade in one pass: each warp takes 32 rays, traverses them,
+// then shades all 32 together once the warp has reconverged and appends the
+// continuing paths with one ballot and one atomic.  Saves the hit record
+// round trip, the second read of the rays and one launch per bounce.
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+                                                     uint32_t* __restrict__ work, Queue qout,
+                                                     uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
+                                                     uint32_t* __restrict__ err,
+                                                     unsigned long long* __restrict__ stats) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.pair = reinterpret_cast<int2*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    const uint32_t n = *cnt_in;
+    const uint32_t lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        const bool valid = i < n;
+        float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4;
+        int2 hit = make_int2(0, -1);
+        if (valid) {
+            o4 = qin.o[i];
+            d4 = qin.d[i];
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float t;
+            const int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            hit = make_int2(__float_as_int(t), k);
+        }
+        ShadeOut r;
+        r.cont = false;
+        uint32_t slot = 0;
+        if (valid) {
+            slot = (uint32_t)__float_as_int(o4.w);
+            r = shade_one(S, o4, d4, qin.t[i], hit);
+        }
+        const uint32_t pos = warp_append(r.cont, cnt_out);
+        if (r.cont) {
+            qout.o[pos] = r.o;
+            qout.d[pos] = r.d;
+            qout.t[pos] = r.t;
+        } else if (valid) {
+            slots[slot] = r.result;
+        }
+    }
+    if (overflow) atomicOr(err, 1u);
+    if (COUNT) {
+        unsigned long long a = K.nodes, b = K.spheres;
+        for (int off = 16; off > 0; off >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, off);
+            b += __shfl_xor_sync(0xffffffffu, b, off);
+        }
+        if (lane == 0) {
+            atomicAdd(stats + 1, a);
+            atomicAdd(stats + 2, b);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
                                                const uint32_t* __restrict__ cnt_in, Queue qout,
                                                uint32_t* __restrict__ cnt_out, float4* __restrict__ slots) {
@@ -300,6 +366,10 @@ cudaError_t configure(venu_renderer* r) {
     if (t.traverse_variant == 0) {
         e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    } else if (t.traverse_variant == 2) {
+        e = occupancy_grid(k_trace_shade<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     } else {
         e = occupancy_grid(k_traverse_dyn<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess)
@@ -388,7 +458,7 @@ extern "C" venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tun
         set_error("venu_renderer_set_tuning: NULL argument");
         return VENU_ERR_INVALID;
     }
-    const bool ok = t->traverse_variant <= 1u && t->refill_min >= 1u && t->refill_min <= 32u &&
+    const bool ok = t->traverse_variant <= 2u && t->refill_min >= 1u && t->refill_min <= 32u &&
                     (t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) &&
                     t->shade_block >= 64u && t->shade_block <= 512u && (t->shade_block % 32u) == 0u &&
                     t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u;
@@ -487,6 +557,21 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                     VENU_CUDA(next_events(r, e0, e1));
                     VENU_CUDA(next_events(r, e2, e3));
                     VENU_CUDA(cudaEventRecord(e0, st));
+                }
+                if (tu.traverse_variant == 2) {
+                    if (count)
+                        k_trace_shade<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
+                                                                            r->cnt + b + 1, r->slots, r->err, r->stats);
+                    else
+                        k_trace_shade<false><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
+                                                                             r->cnt + b + 1, r->slots, r->err, r->stats);
+                    if (prof) {
+                        VENU_CUDA(cudaEventRecord(e1, st));
+                        VENU_CUDA(cudaEventRecord(e2, st));
+                        VENU_CUDA(cudaEventRecord(e3, st));
+                    }
+                    launches += 1;
+                    continue;
                 }
                 if (tu.traverse_variant == 0) {
                     if (count)

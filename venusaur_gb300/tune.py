@@ -13,7 +13,7 @@ import itertools
 from .core import DeviceScene, Wavefront, new_accum
 
 DEFAULT_SPACE = {
-    "traverse_variant": (0, 1),
+    "traverse_variant": (0, 1, 2),
     "refill_min": (4, 8, 16),
     "traverse_block": (64, 128, 256),
     "shade_block": (128, 256),
