@@ -230,6 +230,57 @@ typedef struct venu_tuning {
 } venu_tuning;
 VENU_API venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tuning* t);
 VENU_API venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tuning* t);
+
+/* ---- batched / served rendering ----------------------------------------
+ * No single counterpart in the reference (it renders one scene per
+ * optixLaunch); each job is one Renderer::Draw of its own scene, camera and
+ * image.  All admitted jobs share one pool of paths in flight: every ray
+ * carries its job, finished paths are replaced by new camera rays of the
+ * jobs in submission order, and the whole path loop -- traverse+shade,
+ * regenerate, repeat -- is one CUDA graph launch driven by a device-side
+ * while condition.  Results are bit-identical to venu_render of each job
+ * alone (same seeds, same per-pixel sample order). */
+typedef struct venu_batch venu_batch;
+
+typedef struct venu_job_desc {
+    const venu_scene* scene;
+    venu_camera camera;
+    venu_render_opts opts;  /* width, height, spp, subframe_index, max_depth, flags */
+    float* accum;           /* device, VENU_ACCUM_FLOATS_PER_PIXEL per pixel, caller-owned */
+    float* image_f;         /* optional RGBA32F mean */
+    uint8_t* image8;        /* optional sRGB RGBA8 */
+} venu_job_desc;
+
+typedef struct venu_batch_stats {
+    uint64_t segments;        /* ray casts since creation */
+    uint64_t paths_done;      /* finished paths since creation */
+    uint64_t iterations;      /* path-loop iterations since creation */
+    uint64_t graph_launches;  /* venu_batch_run calls that launched the graph */
+    uint64_t resident_bytes;  /* device bytes held for admitted jobs (seed tables, sample slots) */
+    uint32_t active_jobs;
+    uint32_t reserved;
+} venu_batch_stats;
+
+#define VENU_BATCH_NO_GRAPH 1u /* run the path loop from the host (one launch per stage) */
+
+/* pool_paths: paths in flight (0 = 16 Mi); max_jobs: concurrently admitted jobs (<= 4096). */
+VENU_API venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs, uint32_t flags, venu_batch** out);
+VENU_API venu_status venu_batch_set_tuning(venu_batch* b, const venu_tuning* t);
+/* Bytes venu_batch_submit allocates for a job of this size (seed table + slots). */
+VENU_API uint64_t venu_batch_job_bytes(uint32_t width, uint32_t height, uint32_t spp);
+/* Admits a job: allocates its seed table and per-sample slots and computes the
+ * seeds on `stream`.  The scene and output buffers must stay valid until the
+ * job is collected.  VENU_ERR_TOO_LARGE when max_jobs are admitted. */
+VENU_API venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id);
+/* Runs the shared path loop for at most max_iterations iterations (0 = until
+ * every admitted job has finished) as one graph launch on `stream`. */
+VENU_API venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, void* stream);
+/* Waits for `stream`, then accumulates, resolves and releases every finished
+ * job; writes their ids (up to cap) and the count. */
+VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* finished_ids, uint32_t cap,
+                                        uint32_t* count);
+VENU_API venu_status venu_batch_stats_get(venu_batch* b, venu_batch_stats* out);
+VENU_API venu_status venu_batch_destroy(venu_batch* b);
 VENU_API venu_status venu_renderer_destroy(venu_renderer* r);
 
 #ifdef __cplusplus

@@ -1,0 +1,118 @@
+"""GPU tests of the batched/served engine (venu_batch_*): jobs of different
+scenes, sizes, sample counts and depths share one path pool; each job's
+accumulator must equal the oracle's (and venu_render's) bit for bit, whether
+it ran alone or in the mix, in one graph launch or in chunks."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _jobs(oracle):
+    return [
+        dict(scene=oracle.scene_rtiow(0), eye=(13, 2, 3), W=40, H=24, spp=3, depth=8, sub=1),
+        dict(scene=oracle.scene_random(3000, 5), eye=(60, 15, 60), W=33, H=17, spp=5, depth=50, sub=2),
+        dict(scene=oracle.scene_rtiow(3), eye=(13, 2, 3), W=16, H=9, spp=1, depth=4, sub=7),
+        dict(scene=oracle.scene_rtiow(0)[:2], eye=(13, 2, 3), W=8, H=6, spp=4, depth=3, sub=1),
+    ]
+
+
+def _want(oracle, j):
+    cam = oracle.camera(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
+    r = oracle.render(j["scene"], cam, j["W"], j["H"], j["spp"], subframe=j["sub"], max_depth=j["depth"],
+                      mode=pyoracle.MODE_GB300)
+    return cam, r
+
+
+def _submit_all(venu, torch, batch, oracle, jobs):
+    out = []
+    for j in jobs:
+        cam, want = _want(oracle, j)
+        ds = venu.DeviceScene(j["scene"])
+        acc = venu.new_accum(j["W"], j["H"])
+        img = torch.zeros((j["W"] * j["H"], 4), dtype=torch.float32, device="cuda")
+        jid = batch.submit(ds, cam, j["W"], j["H"], j["spp"], acc, subframe=j["sub"], max_depth=j["depth"],
+                           image_f=img)
+        out.append(dict(id=jid, ds=ds, acc=acc, img=img, want=want))
+    return out
+
+
+@pytest.mark.parametrize("pool,graph", [(0, True), (700, True), (700, False)])
+def test_batch_matches_oracle(venu, oracle, cuda, pool, graph):
+    torch = cuda
+    b = venu.Batch(pool_paths=pool, max_jobs=8, graph=graph)
+    sub = _submit_all(venu, torch, b, oracle, _jobs(oracle))
+    b.run()
+    done = b.collect()
+    torch.cuda.synchronize()
+    assert sorted(done) == sorted(s["id"] for s in sub)
+    total_segments = 0
+    for s in sub:
+        assert np.array_equal(s["acc"].cpu().numpy().view(np.uint32), s["want"]["accum"].view(np.uint32))
+        assert np.array_equal(s["img"].cpu().numpy().view(np.uint32), s["want"]["image_f"].view(np.uint32))
+        total_segments += s["want"]["segments"]
+    st = b.stats()
+    assert st["segments"] == total_segments
+    assert st["active_jobs"] == 0 and st["resident_bytes"] == 0
+    if graph:
+        assert st["graph_launches"] == 1
+
+
+def test_batch_chunked_runs_and_late_admission(venu, oracle, cuda):
+    """Continuous batching: jobs arrive while others are in flight; runs of a
+    few iterations interleave with admission and collection."""
+    torch = cuda
+    b = venu.Batch(pool_paths=500, max_jobs=8)
+    jobs = _jobs(oracle)
+    first = _submit_all(venu, torch, b, oracle, jobs[:2])
+    b.run(max_iterations=2)
+    finished = b.collect()
+    late = _submit_all(venu, torch, b, oracle, jobs[2:])
+    allsub = first + late
+    for _ in range(500):
+        b.run(max_iterations=4)
+        finished += b.collect()
+        if len(finished) == len(allsub):
+            break
+    torch.cuda.synchronize()
+    assert sorted(finished) == sorted(s["id"] for s in allsub)
+    for s in allsub:
+        assert np.array_equal(s["acc"].cpu().numpy().view(np.uint32), s["want"]["accum"].view(np.uint32))
+
+
+def test_batch_equals_plain_render(venu, oracle, cuda):
+    """The same job alone through venu_render and in a batch mix."""
+    torch = cuda
+    sp = oracle.scene_random(20000, 9)
+    W, H, spp = 48, 32, 4
+    cam = oracle.camera((60, 15, 60), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    ds = venu.DeviceScene(sp)
+    a1 = venu.new_accum(W, H)
+    wf = venu.Wavefront(3000)
+    wf.render(ds, cam, W, H, spp, a1, subframe=4, max_depth=50, reset=True)
+    b = venu.Batch(pool_paths=4000, max_jobs=4)
+    a2 = venu.new_accum(W, H)
+    other = _submit_all(venu, torch, b, oracle, _jobs(oracle)[:1])
+    b.submit(ds, cam, W, H, spp, a2, subframe=4, max_depth=50)
+    b.run()
+    b.collect()
+    torch.cuda.synchronize()
+    assert np.array_equal(a1.cpu().numpy().view(np.uint32), a2.cpu().numpy().view(np.uint32))
+    assert np.array_equal(other[0]["acc"].cpu().numpy().view(np.uint32), other[0]["want"]["accum"].view(np.uint32))
+
+
+def test_batch_limits(venu, oracle, cuda):
+    b = venu.Batch(pool_paths=1000, max_jobs=1)
+    sp = oracle.scene_rtiow(0)
+    ds = venu.DeviceScene(sp)
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, 1.0, 0.1, 10.0)
+    acc = venu.new_accum(8, 8)
+    b.submit(ds, cam, 8, 8, 1, acc)
+    with pytest.raises(venu.VenuError):
+        b.submit(ds, cam, 8, 8, 1, acc)  # max_jobs reached
+    with pytest.raises(venu.VenuError):
+        venu.Batch(pool_paths=1000, max_jobs=0)
+    b.run()
+    assert len(b.collect()) == 1

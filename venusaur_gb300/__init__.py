@@ -4,6 +4,7 @@ Material / Sphere interface.  All compute runs in libvenusaur_gb300.so
 (include/venu.h); this package is the host-side mirror of the interface."""
 from ._lib import CAMERA_DTYPE, NODE_DTYPE, SPHERE_DTYPE, VenuError, lib  # noqa: F401
 from .core import (  # noqa: F401
+    Batch,
     Camera,
     CUDAOutputBuffer,
     DeviceScene,
@@ -18,7 +19,7 @@ from .core import (  # noqa: F401
 )
 
 __all__ = [
-    "Camera", "CUDAOutputBuffer", "DeviceScene", "Material", "Renderer", "Scene", "Sphere",
+    "Batch", "Camera", "CUDAOutputBuffer", "DeviceScene", "Material", "Renderer", "Scene", "Sphere",
     "Wavefront", "VenuError", "generate_random", "generate_rtiow", "new_accum", "lib",
     "SPHERE_DTYPE", "CAMERA_DTYPE", "NODE_DTYPE",
 ]

@@ -64,6 +64,24 @@ class Tuning(C.Structure):
                 ("shade_blocks_per_sm", C.c_uint32)]
 
 
+class CameraC(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("u", C.c_float * 3), ("v", C.c_float * 3), ("w", C.c_float * 3),
+                ("lens_radius", C.c_float)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", CameraC), ("opts", RenderOpts), ("accum", C.c_void_p),
+                ("image_f", C.c_void_p), ("image8", C.c_void_p)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("segments", C.c_uint64), ("paths_done", C.c_uint64), ("iterations", C.c_uint64),
+                ("graph_launches", C.c_uint64), ("resident_bytes", C.c_uint64), ("active_jobs", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+BATCH_NO_GRAPH = 1
+
 _lib = None
 
 
@@ -97,13 +115,23 @@ def lib() -> C.CDLL:
     L.venu_render.argtypes = [vp, vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp]
     L.venu_renderer_stats.argtypes = [vp, C.POINTER(RenderStats)]
     L.venu_renderer_destroy.argtypes = [vp]
+    L.venu_batch_create.argtypes = [u32, u32, u32, C.POINTER(vp)]
+    L.venu_batch_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+    L.venu_batch_job_bytes.restype = C.c_uint64
+    L.venu_batch_job_bytes.argtypes = [u32, u32, u32]
+    L.venu_batch_submit.argtypes = [vp, C.POINTER(JobDesc), vp, C.POINTER(u32)]
+    L.venu_batch_run.argtypes = [vp, u32, vp]
+    L.venu_batch_collect.argtypes = [vp, vp, vp, u32, C.POINTER(u32)]
+    L.venu_batch_stats_get.argtypes = [vp, C.POINTER(BatchStats)]
+    L.venu_batch_destroy.argtypes = [vp]
     L.venu_renderer_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.venu_renderer_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     for name in ("venu_device_check", "venu_scene_generate_random", "venu_scene_create",
                  "venu_scene_create_device", "venu_scene_info_get", "venu_scene_export_bvh",
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
                  "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
-                 "venu_renderer_get_tuning"):
+                 "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit",
+                 "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -423,3 +423,76 @@ class Renderer:
         if self.scene is not None:
             self.scene.close()
         self.wave = self.scene = self.accum = None
+
+
+# ---------------------------------------------------------------------------
+# Batched / served rendering: many jobs in one shared path pool
+# ---------------------------------------------------------------------------
+def _camera_c(camera: np.ndarray) -> "_lib.CameraC":
+    c = np.ascontiguousarray(camera, CAMERA_DTYPE)[0]
+    cc = _lib.CameraC()
+    for f in ("origin", "u", "v", "w"):
+        getattr(cc, f)[:] = [float(x) for x in c[f]]
+    cc.lens_radius = float(c["lens_radius"])
+    return cc
+
+
+class Batch:
+    """A venu_batch: jobs admitted with submit(), advanced together by run(),
+    finished ones accumulated and released by collect()."""
+
+    def __init__(self, pool_paths: int = 0, max_jobs: int = 256, graph: bool = True):
+        h = C.c_void_p()
+        check(lib().venu_batch_create(pool_paths, max_jobs, 0 if graph else _lib.BATCH_NO_GRAPH, C.byref(h)))
+        self.handle = h
+        self.max_jobs = max_jobs
+
+    def set_tuning(self, **kw) -> None:
+        base = dict(traverse_variant=2, refill_min=8, traverse_block=256, traverse_blocks_per_sm=0,
+                    shade_block=256, shade_blocks_per_sm=0)
+        base.update(kw)
+        t = Tuning(*(int(base[f]) for f in TUNING_FIELDS))
+        check(lib().venu_batch_set_tuning(self.handle, C.byref(t)))
+
+    @staticmethod
+    def job_bytes(width: int, height: int, spp: int) -> int:
+        return int(lib().venu_batch_job_bytes(width, height, spp))
+
+    def submit(self, scene: DeviceScene, camera: np.ndarray, width: int, height: int, spp: int, accum,
+               subframe: int = 1, max_depth: int = 50, reset: bool = True, image_f=None, image8=None,
+               stream=None) -> int:
+        d = _lib.JobDesc()
+        d.scene = scene.handle.value
+        d.camera = _camera_c(camera)
+        d.opts = RenderOpts(width, height, spp, subframe, max_depth, _lib.FLAG_RESET_ACCUM if reset else 0)
+        d.accum = ptr(accum).value
+        d.image_f = ptr(image_f).value if image_f is not None else None
+        d.image8 = ptr(image8).value if image8 is not None else None
+        jid = C.c_uint32()
+        check(lib().venu_batch_submit(self.handle, C.byref(d), _stream_handle(stream), C.byref(jid)))
+        return int(jid.value)
+
+    def run(self, max_iterations: int = 0, stream=None) -> None:
+        check(lib().venu_batch_run(self.handle, max_iterations, _stream_handle(stream)))
+
+    def collect(self, stream=None) -> list:
+        ids = (C.c_uint32 * self.max_jobs)()
+        n = C.c_uint32()
+        check(lib().venu_batch_collect(self.handle, _stream_handle(stream), ids, self.max_jobs, C.byref(n)))
+        return [int(ids[i]) for i in range(n.value)]
+
+    def stats(self) -> dict:
+        s = _lib.BatchStats()
+        check(lib().venu_batch_stats_get(self.handle, C.byref(s)))
+        return {f: int(getattr(s, f)) for f, _ in _lib.BatchStats._fields_ if f != "reserved"}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().venu_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,613 @@
+// batch.cu -- many render jobs in one shared path pool (batched and served
+// rendering).
+//
+// Every admitted job is a Renderer::Draw (Core/Renderer.h:35-78) of its own
+// scene.  Instead of one wavefront per job, all jobs feed one pool of paths
+// in flight:
+//
+//   trace+shade  every queued ray against its own job's LBVH, shaded, the
+//                survivors compacted into the other queue (the job index
+//                rides in the upper bits of the depth word);
+//   plan         one thread hands the free queue slots to the admitted jobs
+//                in submission order (oldest first);
+//   regen        new camera rays for the planned (job, sample, pixel)
+//                triples, from each job's precomputed raygen seed table;
+//
+// repeated under a device-side while condition, so the whole loop is one
+// CUDA graph launch.  Paths finish into per-job sample slots; a job whose
+// paths are all done is accumulated (Kahan, sample order) and resolved by
+// venu_batch_collect.  The seed table holds, for every (sample, pixel), the
+// raygen RNG state at the start of that sample (Core/RayTracer.cu:169-177),
+// which makes every path independent of generation order: results are
+// bit-identical to venu_render of each job alone.
+#include "render_kernels.cuh"
+#include "venu_internal.h"
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+namespace venu {
+
+struct DevJob {
+    SceneView scene;
+    venu_camera cam;
+    uint32_t W, H, npix, spp, max_depth, subframe;
+    const uint32_t* seeds;  // [spp * npix], sample-major
+    float4* slots;          // [spp * npix], sample-major
+    unsigned long long total;
+};
+
+struct LoopCtl {  // device-owned loop state
+    uint32_t cnt[2], work[2];
+    uint32_t iter, running, more_gen, take_total, out_base, plan_n, err, pad;
+    unsigned long long segments, paths_done, iterations;
+};
+
+struct RunCtl {  // host-written before each run
+    uint32_t max_iter, nactive;
+};
+
+struct CollectEntry {
+    float4* accum;
+    float4* image_f;
+    uchar4* image8;
+    const float4* slots;
+    uint32_t npix, spp, reset, pix_off;
+};
+
+// Raygen RNG state at the start of every sample of every pixel.
+__global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t spp, uint32_t subframe,
+                             uint32_t* __restrict__ seeds) {
+    const uint32_t npix = W * H;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= npix) return;
+    const DevCamera C = load_camera(cam);
+    const uint32_t x = pix % W, y = pix / W;
+    uint32_t seed = tea4(pix, subframe);
+    for (uint32_t s = 0; s < spp; ++s) {
+        seeds[(size_t)s * npix + pix] = seed;
+        f3 o, d;
+        camera_ray(C, x, y, W, H, seed, o, d);  // advances the seed past the sample's draws
+    }
+}
+
+__global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
+                       const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
+                       uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
+                       uint32_t* __restrict__ plan_off, uint32_t Q, int out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int in = 1 - out;
+    const uint32_t survivors = ctl->cnt[out];
+    const uint32_t free = survivors < Q ? Q - survivors : 0u;
+    const uint32_t na = run->nactive;
+    uint32_t off = 0, more = 0;
+    for (uint32_t i = 0; i < na; ++i) {
+        const uint32_t j = order[i];
+        const unsigned long long total = jobs[j].total, nx = job_next[j];
+        const unsigned long long rem = total - nx;
+        const uint32_t take = (uint32_t)min(rem, (unsigned long long)(free - off));
+        plan_job[i] = j;
+        plan_start[i] = nx;
+        plan_off[i] = off;
+        off += take;
+        job_next[j] = nx + take;
+        if (nx + take < total) more = 1;
+    }
+    plan_off[na] = off;
+    ctl->plan_n = na;
+    ctl->take_total = off;
+    ctl->out_base = survivors;
+    ctl->cnt[out] = survivors + off;
+    ctl->more_gen = more;
+    ctl->cnt[in] = 0;   // the next trace writes into the other queue
+    ctl->work[out] = 0; // and fetches from this one
+}
+
+__global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restrict__ ctl,
+                        const uint32_t* __restrict__ plan_job, const unsigned long long* __restrict__ plan_start,
+                        const uint32_t* __restrict__ plan_off, Queue q) {
+    const uint32_t total = ctl->take_total, base = ctl->out_base, np = ctl->plan_n;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        // last plan entry i with plan_off[i] <= t (entries may be empty)
+        uint32_t lo = 0, hi = np;  // invariant: plan_off[lo] <= t < plan_off[hi]
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (plan_off[mid] <= t) lo = mid; else hi = mid;
+        }
+        const uint32_t j = plan_job[lo];
+        const DevJob& J = jobs[j];
+        const unsigned long long l = plan_start[lo] + (t - plan_off[lo]);
+        const uint32_t s = (uint32_t)(l / J.npix);
+        const uint32_t pix = (uint32_t)(l - (unsigned long long)s * J.npix);
+        uint32_t seed = J.seeds[l];
+        const DevCamera C = load_camera(J.cam);
+        f3 o, d;
+        camera_ray(C, pix % J.W, pix / J.W, J.W, J.H, seed, o, d);
+        write_primary(q, base + t, o, d, (uint32_t)l, (int)J.max_depth - 1, seed, j);
+    }
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_trace_shade_multi(const DevJob* __restrict__ jobs,
+                                                           unsigned long long* __restrict__ job_done, LoopCtl* ctl,
+                                                           Queue qin, Queue qout, int in) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.pair = reinterpret_cast<int2*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    const int out = 1 - in;
+    const uint32_t n = ctl->cnt[in];
+    const uint32_t lane = threadIdx.x & 31;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctl->segments, (unsigned long long)n);
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    uint32_t finished = 0;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&ctl->work[in], 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        const bool valid = i < n;
+        uint32_t job = 0xFFFFFFFFu;
+        ShadeOut r;
+        r.cont = false;
+        if (valid) {
+            const float4 o4 = qin.o[i], d4 = qin.d[i];
+            job = __float_as_uint(d4.w) >> 8;
+            const SceneView S = jobs[job].scene;
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float t;
+            const int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            r = shade_one(S, o4, d4, qin.t[i], make_int2(__float_as_int(t), k));
+            if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(o4.w)] = r.result;
+        }
+        const uint32_t pos = warp_append(r.cont, &ctl->cnt[out]);
+        if (r.cont) {
+            qout.o[pos] = r.o;
+            qout.d[pos] = r.d;
+            qout.t[pos] = r.t;
+        }
+        // finished paths per job: one atomic per distinct job in the warp
+        const bool fin = valid && !r.cont;
+        const uint32_t key = fin ? job : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xffffffffu, key);
+        if (fin && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&job_done[job], (unsigned long long)__popc(peers));
+        finished += __popc(__ballot_sync(0xffffffffu, fin));
+    }
+    if (lane == 0 && finished) atomicAdd(&ctl->paths_done, (unsigned long long)finished);
+    if (overflow) atomicOr(&ctl->err, 1u);
+}
+
+__global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, cudaGraphConditionalHandle handle,
+                            int use_handle) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t it = ctl->iter + 2u;
+    ctl->iter = it;
+    ctl->iterations += 2u;
+    uint32_t more = (ctl->cnt[0] > 0u || ctl->more_gen) ? 1u : 0u;
+    if (run->max_iter && it >= run->max_iter) more = 0u;
+    ctl->running = more;
+    if (use_handle) cudaGraphSetConditional(handle, more);
+}
+
+// Accumulate (Kahan, sample order) and resolve finished jobs: one thread per
+// pixel of the listed jobs.
+__global__ void k_collect(const CollectEntry* __restrict__ ent, uint32_t nent, uint32_t total_pix) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total_pix) return;
+    uint32_t lo = 0, hi = nent;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (ent[mid].pix_off <= t) lo = mid; else hi = mid;
+    }
+    const CollectEntry& E = ent[lo];
+    const uint32_t pix = t - E.pix_off;
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    if (!E.reset) {
+        a0 = E.accum[2 * (size_t)pix];
+        a1 = E.accum[2 * (size_t)pix + 1];
+    }
+    for (uint32_t s = 0; s < E.spp; ++s) kahan_add(a0, a1, E.slots[(size_t)s * E.npix + pix]);
+    E.accum[2 * (size_t)pix] = a0;
+    E.accum[2 * (size_t)pix + 1] = a1;
+    const f3 mean = mk(a0.x / a0.w, a0.y / a0.w, a0.z / a0.w);
+    if (E.image_f) E.image_f[pix] = make_float4(mean.x, mean.y, mean.z, 1.0f);
+    if (E.image8) E.image8[pix] = make_color(mean);
+}
+
+SceneView view_of(const venu_scene* s);
+size_t traverse_smem(int block);
+
+}  // namespace venu
+
+using namespace venu;
+
+namespace {
+
+struct JobHost {
+    bool active = false;
+    venu_job_desc desc{};
+    uint64_t total = 0, bytes = 0;
+    uint32_t* seeds = nullptr;
+    float4* slots = nullptr;
+};
+
+constexpr uint32_t kMaxJobs = 4096;
+
+}  // namespace
+
+struct venu_batch {
+    uint32_t Q = 0, max_jobs = 0, flags = 0;
+    Queue q[2] = {};
+    DevJob* d_jobs = nullptr;
+    unsigned long long *d_next = nullptr, *d_done = nullptr, *d_plan_start = nullptr;
+    uint32_t *d_order = nullptr, *d_plan_job = nullptr, *d_plan_off = nullptr;
+    LoopCtl* d_ctl = nullptr;
+    RunCtl* d_run = nullptr;
+    CollectEntry* d_collect = nullptr;
+    std::vector<JobHost> jobs;
+    std::vector<uint32_t> order;  // active job slots, submission order
+    venu_tuning tune = {2u, 8u, 256u, 0u, 256u, 0u};
+    int trav_blocks = 0, regen_blocks = 0;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle handle = 0;
+    uint64_t graph_launches = 0, resident = 0;
+};
+
+namespace {
+
+cudaError_t batch_configure(venu_batch* b) {
+    const size_t sm = traverse_smem((int)b->tune.traverse_block);
+    cudaError_t e = cudaFuncSetAttribute(k_trace_shade_multi<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int per_sm = 0;
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_shade_multi<false>,
+                                                          (int)b->tune.traverse_block, sm);
+    if (e != cudaSuccess) return e;
+    per_sm = std::max(1, per_sm);
+    if (b->tune.traverse_blocks_per_sm) per_sm = std::min(per_sm, (int)b->tune.traverse_blocks_per_sm);
+    b->trav_blocks = per_sm * sm_count();
+    b->regen_blocks = 4 * sm_count();
+    return cudaSuccess;
+}
+
+// One iteration pair of the path loop (queue 0 -> 1 -> 0) + the condition.
+cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
+    const size_t sm = traverse_smem((int)b->tune.traverse_block);
+    for (int in = 0; in < 2; ++in) {
+        const int out = 1 - in;
+        k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
+                                                                                      b->q[in], b->q[out], in);
+        k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
+                                 b->d_plan_start, b->d_plan_off, b->Q, out);
+        k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
+                                                 b->q[out]);
+    }
+    k_loop_cond<<<1, 32, 0, st>>>(b->d_ctl, b->d_run, b->handle, use_handle ? 1 : 0);
+    return cudaGetLastError();
+}
+
+void destroy_graph(venu_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->handle = 0;
+}
+
+// while (condition) { body } as one executable graph.
+venu_status build_graph(venu_batch* b) {
+    destroy_graph(b);
+    VENU_CUDA(cudaGraphCreate(&b->graph, 0));
+    VENU_CUDA(cudaGraphConditionalHandleCreate(&b->handle, b->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = b->handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    VENU_CUDA(cudaGraphAddNode(&node, b->graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    VENU_CUDA(cudaStreamBeginCaptureToGraph(b->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    cudaError_t le = launch_body(b, b->cap, true);
+    cudaGraph_t captured = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(b->cap, &captured);
+    if (le != cudaSuccess) return cuda_fail(le, "venu_batch: capture of the path loop");
+    if (ee != cudaSuccess) return cuda_fail(ee, "venu_batch: cudaStreamEndCapture");
+    VENU_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    return VENU_OK;
+}
+
+void free_batch(venu_batch* b) {
+    destroy_graph(b);
+    for (auto& j : b->jobs) {
+        cudaFree(j.seeds);
+        cudaFree(j.slots);
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(b->q[i].o);
+        cudaFree(b->q[i].d);
+        cudaFree(b->q[i].t);
+    }
+    cudaFree(b->d_jobs);
+    cudaFree(b->d_next);
+    cudaFree(b->d_done);
+    cudaFree(b->d_plan_start);
+    cudaFree(b->d_order);
+    cudaFree(b->d_plan_job);
+    cudaFree(b->d_plan_off);
+    cudaFree(b->d_ctl);
+    cudaFree(b->d_run);
+    cudaFree(b->d_collect);
+    if (b->cap) cudaStreamDestroy(b->cap);
+}
+
+venu_status upload_order(venu_batch* b, cudaStream_t st) {
+    if (!b->order.empty())
+        VENU_CUDA(cudaMemcpyAsync(b->d_order, b->order.data(), sizeof(uint32_t) * b->order.size(),
+                                  cudaMemcpyHostToDevice, st));
+    return VENU_OK;
+}
+
+}  // namespace
+
+extern "C" uint64_t venu_batch_job_bytes(uint32_t width, uint32_t height, uint32_t spp) {
+    const uint64_t paths = (uint64_t)width * height * spp;
+    return paths * (sizeof(uint32_t) + sizeof(float4));
+}
+
+extern "C" venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs, uint32_t flags, venu_batch** out) {
+    if (!out) {
+        set_error("venu_batch_create: out is NULL");
+        return VENU_ERR_INVALID;
+    }
+    *out = nullptr;
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    if (pool_paths == 0) pool_paths = 16u << 20;
+    if (max_jobs == 0 || max_jobs > kMaxJobs || pool_paths > (1u << 28)) {
+        set_error("venu_batch_create: need 1 <= max_jobs <= 4096 and pool_paths <= 2^28");
+        return VENU_ERR_INVALID;
+    }
+    venu_batch* b = new venu_batch();
+    b->Q = pool_paths;
+    b->max_jobs = max_jobs;
+    b->flags = flags;
+    b->jobs.resize(max_jobs);
+    cudaError_t e = cudaSuccess;
+    const size_t Q = pool_paths;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        if (e == cudaSuccess) e = cudaMalloc(&b->q[i].o, sizeof(float4) * Q);
+        if (e == cudaSuccess) e = cudaMalloc(&b->q[i].d, sizeof(float4) * Q);
+        if (e == cudaSuccess) e = cudaMalloc(&b->q[i].t, sizeof(float4) * Q);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_jobs, sizeof(DevJob) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned long long) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_done, sizeof(unsigned long long) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_plan_start, sizeof(unsigned long long) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_order, sizeof(uint32_t) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_plan_job, sizeof(uint32_t) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_plan_off, sizeof(uint32_t) * (max_jobs + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_ctl, sizeof(LoopCtl));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_run, sizeof(RunCtl));
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_collect, sizeof(CollectEntry) * max_jobs);
+    if (e == cudaSuccess) e = cudaMemset(b->d_ctl, 0, sizeof(LoopCtl));
+    if (e == cudaSuccess) e = cudaMemset(b->d_run, 0, sizeof(RunCtl));
+    if (e == cudaSuccess) e = cudaMemset(b->d_jobs, 0, sizeof(DevJob) * max_jobs);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = batch_configure(b);
+    if (e != cudaSuccess) {
+        venu_status s = cuda_fail(e, "venu_batch_create");
+        free_batch(b);
+        delete b;
+        return s;
+    }
+    *out = b;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_set_tuning(venu_batch* b, const venu_tuning* t) {
+    if (!b || !t) {
+        set_error("venu_batch_set_tuning: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    if (!(t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) ||
+        t->traverse_blocks_per_sm > 32u) {
+        set_error("venu_batch_set_tuning: traverse_block must be 64, 128 or 256");
+        return VENU_ERR_INVALID;
+    }
+    b->tune = *t;
+    b->tune.traverse_variant = 2u;  // the batch loop always traces and shades in one kernel
+    cudaError_t e = batch_configure(b);
+    if (e != cudaSuccess) return cuda_fail(e, "venu_batch_set_tuning");
+    destroy_graph(b);  // rebuilt with the new launch shapes on the next run
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id) {
+    if (!b || !job || !job->scene || !job->accum) {
+        set_error("venu_batch_submit: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    const venu_render_opts& o = job->opts;
+    if (o.width < 2 || o.height < 2 || o.samples_per_pixel == 0 || o.max_depth == 0 || o.max_depth > 64) {
+        set_error("venu_batch_submit: need width,height >= 2, spp >= 1, 1 <= max_depth <= 64");
+        return VENU_ERR_INVALID;
+    }
+    const uint64_t npix = (uint64_t)o.width * o.height, total = npix * o.samples_per_pixel;
+    if (npix > (1u << 30) || total > 0x7fffffffull) {
+        set_error("venu_batch_submit: a job may have at most 2^31 - 1 paths");
+        return VENU_ERR_TOO_LARGE;
+    }
+    uint32_t slot = b->max_jobs;
+    for (uint32_t i = 0; i < b->max_jobs; ++i)
+        if (!b->jobs[i].active) {
+            slot = i;
+            break;
+        }
+    if (slot == b->max_jobs) {
+        set_error("venu_batch_submit: max_jobs jobs are already admitted");
+        return VENU_ERR_TOO_LARGE;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    JobHost& J = b->jobs[slot];
+    J = JobHost{};
+    cudaError_t e = cudaMallocAsync(&J.seeds, sizeof(uint32_t) * total, st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&J.slots, sizeof(float4) * total, st);
+    if (e != cudaSuccess) {
+        if (J.seeds) cudaFreeAsync(J.seeds, st);
+        J = JobHost{};
+        return cuda_fail(e, "venu_batch_submit: job buffers");
+    }
+    J.active = true;
+    J.desc = *job;
+    J.total = total;
+    J.bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel);
+    DevJob dj;
+    std::memset(&dj, 0, sizeof(dj));
+    dj.scene = view_of(job->scene);
+    dj.cam = job->camera;
+    dj.W = o.width;
+    dj.H = o.height;
+    dj.npix = (uint32_t)npix;
+    dj.spp = o.samples_per_pixel;
+    dj.max_depth = o.max_depth;
+    dj.subframe = o.subframe_index;
+    dj.seeds = J.seeds;
+    dj.slots = J.slots;
+    dj.total = total;
+    VENU_CUDA(cudaMemcpyAsync(b->d_jobs + slot, &dj, sizeof(dj), cudaMemcpyHostToDevice, st));
+    VENU_CUDA(cudaMemsetAsync(b->d_next + slot, 0, sizeof(unsigned long long), st));
+    VENU_CUDA(cudaMemsetAsync(b->d_done + slot, 0, sizeof(unsigned long long), st));
+    k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(job->camera, o.width, o.height, o.samples_per_pixel,
+                                                                 o.subframe_index, J.seeds);
+    VENU_CUDA(cudaGetLastError());
+    b->order.push_back(slot);
+    b->resident += J.bytes;
+    venu_status us = upload_order(b, st);
+    if (us != VENU_OK) return us;
+    if (job_id) *job_id = slot;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, void* stream) {
+    if (!b) {
+        set_error("venu_batch_run: NULL batch");
+        return VENU_ERR_INVALID;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    RunCtl rc;
+    rc.max_iter = max_iterations;
+    rc.nactive = (uint32_t)b->order.size();
+    VENU_CUDA(cudaMemcpyAsync(b->d_run, &rc, sizeof(rc), cudaMemcpyHostToDevice, st));
+    VENU_CUDA(cudaMemsetAsync(&b->d_ctl->iter, 0, sizeof(uint32_t), st));
+    if (b->flags & VENU_BATCH_NO_GRAPH) {
+        // host-driven loop: one body, then read the device's running flag
+        for (;;) {
+            cudaError_t e = launch_body(b, st, false);
+            if (e != cudaSuccess) return cuda_fail(e, "venu_batch_run");
+            uint32_t running = 0;
+            VENU_CUDA(cudaMemcpyAsync(&running, &b->d_ctl->running, sizeof(running), cudaMemcpyDeviceToHost, st));
+            VENU_CUDA(cudaStreamSynchronize(st));
+            if (!running) break;
+        }
+        return VENU_OK;
+    }
+    if (!b->exec) {
+        venu_status gs = build_graph(b);
+        if (gs != VENU_OK) return gs;
+    }
+    VENU_CUDA(cudaGraphLaunch(b->exec, st));
+    ++b->graph_launches;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* finished_ids, uint32_t cap,
+                                          uint32_t* count) {
+    if (!b) {
+        set_error("venu_batch_collect: NULL batch");
+        return VENU_ERR_INVALID;
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    VENU_CUDA(cudaStreamSynchronize(st));
+    uint32_t err = 0;
+    VENU_CUDA(cudaMemcpy(&err, &b->d_ctl->err, sizeof(err), cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> done(b->max_jobs);
+    VENU_CUDA(cudaMemcpy(done.data(), b->d_done, sizeof(unsigned long long) * b->max_jobs, cudaMemcpyDeviceToHost));
+    std::vector<CollectEntry> ent;
+    std::vector<uint32_t> fin;
+    uint32_t pix_off = 0;
+    for (uint32_t slot : b->order) {
+        JobHost& J = b->jobs[slot];
+        if (done[slot] < J.total) continue;
+        const venu_render_opts& o = J.desc.opts;
+        CollectEntry c;
+        c.accum = reinterpret_cast<float4*>(J.desc.accum);
+        c.image_f = reinterpret_cast<float4*>(J.desc.image_f);
+        c.image8 = reinterpret_cast<uchar4*>(J.desc.image8);
+        c.slots = J.slots;
+        c.npix = o.width * o.height;
+        c.spp = o.samples_per_pixel;
+        c.reset = (o.flags & VENU_FLAG_RESET_ACCUM) ? 1u : 0u;
+        c.pix_off = pix_off;
+        pix_off += c.npix;
+        ent.push_back(c);
+        fin.push_back(slot);
+    }
+    if (!ent.empty()) {
+        VENU_CUDA(cudaMemcpyAsync(b->d_collect, ent.data(), sizeof(CollectEntry) * ent.size(), cudaMemcpyHostToDevice, st));
+        k_collect<<<(pix_off + 255) / 256, 256, 0, st>>>(b->d_collect, (uint32_t)ent.size(), pix_off);
+        VENU_CUDA(cudaGetLastError());
+        for (uint32_t slot : fin) {
+            JobHost& J = b->jobs[slot];
+            VENU_CUDA(cudaFreeAsync(J.seeds, st));
+            VENU_CUDA(cudaFreeAsync(J.slots, st));
+            b->resident -= J.bytes;
+            J = JobHost{};
+        }
+        std::vector<uint32_t> keep;
+        for (uint32_t slot : b->order)
+            if (b->jobs[slot].active) keep.push_back(slot);
+        b->order.swap(keep);
+        venu_status us = upload_order(b, st);
+        if (us != VENU_OK) return us;
+    }
+    const uint32_t n = (uint32_t)fin.size();
+    if (finished_ids)
+        for (uint32_t i = 0; i < n && i < cap; ++i) finished_ids[i] = fin[i];
+    if (count) *count = n;
+    if (err) {
+        set_error("venu_batch: traversal stack overflow");
+        return VENU_ERR_STACK;
+    }
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_stats_get(venu_batch* b, venu_batch_stats* out) {
+    if (!b || !out) {
+        set_error("venu_batch_stats_get: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    LoopCtl c;
+    VENU_CUDA(cudaMemcpy(&c, b->d_ctl, sizeof(c), cudaMemcpyDeviceToHost));
+    out->segments = c.segments;
+    out->paths_done = c.paths_done;
+    out->iterations = c.iterations;
+    out->graph_launches = b->graph_launches;
+    out->resident_bytes = b->resident;
+    out->active_jobs = (uint32_t)b->order.size();
+    out->reserved = 0;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_destroy(venu_batch* b) {
+    if (!b) return VENU_OK;
+    cudaDeviceSynchronize();
+    free_batch(b);
+    delete b;
+    return VENU_OK;
+}

@@ -10,10 +10,13 @@ namespace venu {
 // optixTrace).  The bounce seed is the raygen seed after the sample's jitter
 // and lens draws; the raygen seed continues from that same state to the next
 // sample (the reference copies it into the PRD and never copies it back).
+// d4.w packs the remaining depth (low 8 bits) and the job index (upper 24
+// bits, 0 for the single-scene renderer).
+constexpr uint32_t kDepthMask = 0xFFu;
 __device__ __forceinline__ void write_primary(const Queue& q, uint32_t pos, f3 o, f3 d, uint32_t slot,
-                                              int depth, uint32_t seed) {
+                                              int depth, uint32_t seed, uint32_t job = 0) {
     q.o[pos] = make_float4(o.x, o.y, o.z, __int_as_float((int)slot));
-    q.d[pos] = make_float4(d.x, d.y, d.z, __int_as_float(depth));
+    q.d[pos] = make_float4(d.x, d.y, d.z, __uint_as_float((job << 8) | ((uint32_t)depth & kDepthMask)));
     q.t[pos] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
 }
 
@@ -41,7 +44,8 @@ __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, flo
     ShadeOut out;
     out.cont = false;
     f3 o = mk(o4.x, o4.y, o4.z), d = mk(d4.x, d4.y, d4.z);
-    int depth = __float_as_int(d4.w);
+    const uint32_t dbits = __float_as_uint(d4.w);
+    int depth = (int)(dbits & kDepthMask);
     f3 T = mk(t4.x, t4.y, t4.z);
     uint32_t seed = __float_as_uint(t4.w);
     if (h.y < 0) {
@@ -89,7 +93,7 @@ __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, flo
     }
     out.cont = true;
     out.o = make_float4(p.x, p.y, p.z, o4.w);
-    out.d = make_float4(dir.x, dir.y, dir.z, __int_as_float(depth - 1));
+    out.d = make_float4(dir.x, dir.y, dir.z, __uint_as_float((dbits & ~kDepthMask) | (uint32_t)(depth - 1)));
     out.t = make_float4(T.x, T.y, T.z, __uint_as_float(seed));
     return out;
 }
