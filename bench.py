@@ -156,6 +156,75 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     return rate, dt, sample, res["segments"]
 
 
+def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
+    """Mixed-scene workload: the plain method (one venu_render per job, in
+    sequence) against the batched engine (all jobs in one shared pool, one
+    graph launch).  BVHs are built before timing (resident scenes)."""
+    from venusaur_gb300 import workloads
+
+    jobs = workloads.mixed_jobs(n_jobs)
+    scenes = {}
+    for j in jobs:
+        key = (j["n"], j["scene_seed"])
+        if key not in scenes:
+            scenes[key] = venu.DeviceScene(venu.generate_random(j["n"], j["scene_seed"]))
+    cams = [venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0) for j in jobs]
+    acc_plain = [venu.new_accum(j["W"], j["H"]) for j in jobs]
+    acc_batch = [venu.new_accum(j["W"], j["H"]) for j in jobs]
+    img_plain = [torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda") for j in jobs]
+    img_batch = [torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda") for j in jobs]
+    wf = venu.Wavefront(max_paths)
+    if tuning:
+        wf.set_tuning(**tuning)
+    b = venu.Batch(pool_paths=max_paths, max_jobs=n_jobs)
+    if tuning:
+        b.set_tuning(**tuning)
+
+    def plain(rep):
+        segs = 0
+        for j, cam, acc, img in zip(jobs, cams, acc_plain, img_plain):
+            wf.render(scenes[(j["n"], j["scene_seed"])], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
+                      max_depth=j["depth"], reset=True, image8=img)
+        return segs
+
+    def batched(rep):
+        for j, cam, acc, img in zip(jobs, cams, acc_batch, img_batch):
+            b.submit(scenes[(j["n"], j["scene_seed"])], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
+                     max_depth=j["depth"], reset=True, image8=img)
+        b.run()
+        done = b.collect()
+        assert len(done) == len(jobs)
+
+    def timed(fn):
+        fn(-1)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record()
+        fn(0)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), 1000 * (time.perf_counter() - t0)
+
+    seg0 = b.stats()["segments"]
+    b_ms, b_wall = timed(batched)
+    segs = (b.stats()["segments"] - seg0) // 2
+    p_ms, p_wall = timed(plain)
+    same = all(torch.equal(acc_plain[i], acc_batch[i]) for i in range(min(check_jobs, len(jobs))))
+    same_all = all(torch.equal(acc_plain[i], acc_batch[i]) for i in range(len(jobs)))
+    return {
+        "workload": f"{n_jobs} scenes, spheres log-uniform 100..200000, resolutions {{256x256, 512x512, "
+                    f"640x360, 1024x1024}}, spp {{4, 16, 64}}, depth 50 (seeded)",
+        "paths": workloads.paths(jobs), "segments": int(segs),
+        "plain": {"value": segs / (p_ms / 1000), "ms": p_ms, "wall_ms": p_wall,
+                  "method": "venu_render per job, in sequence"},
+        "batched": {"value": segs / (b_ms / 1000), "ms": b_ms, "wall_ms": b_wall,
+                    "method": "one shared path pool, one graph launch", "pool_paths": max_paths},
+        "speedup": p_ms / b_ms,
+        "identical_accumulators": bool(same_all),
+    }
+
+
 def run_reference(args, cfg, world, rank):
     if rank != 0:
         return
@@ -196,6 +265,7 @@ def main():
     ap.add_argument("--max-paths", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
     world, rank, local, dist = dist_setup(args.gpus)
@@ -380,6 +450,8 @@ def main():
         "e2e": e2e,
         "roofline": roofline,
     }
+    if not args.no_batched:
+        line["batched"] = run_batched(venu, torch, tuning, max_paths)
     if not args.no_cpu:
         from oracle import pyoracle
 

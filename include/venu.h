@@ -154,7 +154,10 @@ VENU_API venu_status venu_scene_create_device(const venu_sphere* spheres_dev, ui
 VENU_API venu_status venu_scene_info_get(const venu_scene* scene, venu_scene_info* out);
 /* Copies the built LBVH to host buffers (any may be NULL): sorted Morton
  * codes [n], sorted original ids [n], internal nodes [(n-1) x 32 bytes:
- * lo[3], left, hi[3], right; child >= 0 internal, child|0x80000000 leaf slot]. */
+ * lo[3], left, hi[3], right; child >= 0 internal, 0x80000000 | slot leaf,
+ * and 0x40000000 also set on the leaf of a hoisted sphere -- one of at most
+ * four huge spheres (radius above a quarter of the largest centroid extent)
+ * that every ray tests before the traversal]. */
 VENU_API venu_status venu_scene_export_bvh(const venu_scene* scene, uint32_t* morton, uint32_t* ids,
                                   void* nodes);
 VENU_API venu_status venu_scene_destroy(venu_scene* scene);

@@ -180,6 +180,10 @@ vo_sphere draw_material(SceneRng& R, float choose, f3 center, float radius) {
 // LBVH (Karras 2012) host build.
 // ---------------------------------------------------------------------------
 const int32_t kLeaf = (int32_t)0x80000000u;
+const int32_t kHoisted = 0x40000000;  // leaf tested before traversal
+const int32_t kSlotMask = 0x3fffffff;
+const int kMaxHoisted = 4;
+const uint32_t kHoistCandidates = 64;
 
 uint32_t spread10(uint32_t v) {  // bit i of v -> bit 3i
     uint32_t r = 0;
@@ -220,6 +224,7 @@ struct Bvh {
     std::vector<float> radius;
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     uint32_t depth = 0;
+    std::vector<int32_t> hoist;  // slots of huge spheres tested first
 };
 
 int delta(const std::vector<uint32_t>& k, int n, int i, int j) {
@@ -237,23 +242,27 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
     B.radius.assign(n, 0);
     B.nodes.assign(n > 1 ? n - 1 : 0, vo_node{});
     if (n == 0) return;
+    // Centroid bounds; Morton codes use one quantisation scale for all axes
+    // (the largest extent: cubic cells).  A sphere is huge -- hoisted, below --
+    // when its radius exceeds a quarter of that extent.
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t i = 0; i < n; ++i)
         for (int a = 0; a < 3; ++a) {
             lo[a] = std::fmin(lo[a], s[i].center[a]);
             hi[a] = std::fmax(hi[a], s[i].center[a]);
         }
-    float ext[3];
+    float ext = 0.0f;
     for (int a = 0; a < 3; ++a) {
-        ext[a] = hi[a] - lo[a];
+        ext = std::fmax(ext, hi[a] - lo[a]);
         B.bounds[a] = lo[a];
         B.bounds[3 + a] = hi[a];
     }
+    const float thr = 0.25f * ext;
     std::vector<uint32_t> key(n), idx(n);
     for (uint32_t i = 0; i < n; ++i) {
-        uint32_t qx = quant10(s[i].center[0], lo[0], ext[0]);
-        uint32_t qy = quant10(s[i].center[1], lo[1], ext[1]);
-        uint32_t qz = quant10(s[i].center[2], lo[2], ext[2]);
+        uint32_t qx = quant10(s[i].center[0], lo[0], ext);
+        uint32_t qy = quant10(s[i].center[1], lo[1], ext);
+        uint32_t qz = quant10(s[i].center[2], lo[2], ext);
         key[i] = (spread10(qx) << 2) | (spread10(qy) << 1) | spread10(qz);
         idx[i] = i;
     }
@@ -305,7 +314,7 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
     dep[0] = 1;
     auto child_box = [&](int c, float* blo, float* bhi) {
         if (c & kLeaf) {
-            int k = c & ~kLeaf;
+            int k = c & kSlotMask;
             float r = std::fabs(B.radius[k]);
             blo[0] = sub_rd(B.center[k].x, r);
             blo[1] = sub_rd(B.center[k].y, r);
@@ -345,6 +354,22 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
         }
     }
     B.depth = maxdepth;
+    // Hoisted spheres: the (at most 4) lowest huge slots, if there are at
+    // most 64 huge spheres; their leaf words are flagged.
+    std::vector<int32_t> cand;
+    for (uint32_t k = 0; k < n; ++k)
+        if (std::fabs(B.radius[k]) > thr) cand.push_back((int32_t)k);
+    if (!cand.empty() && cand.size() <= kHoistCandidates) {
+        const size_t nh = std::min(cand.size(), (size_t)kMaxHoisted);
+        for (size_t i = 0; i < nh; ++i) {
+            const int32_t k = cand[i];
+            B.hoist.push_back(k);
+            const int32_t p = parent_leaf[k];
+            if (p < 0) continue;
+            if (B.nodes[p].left == (k | kLeaf)) B.nodes[p].left |= kHoisted;
+            else if (B.nodes[p].right == (k | kLeaf)) B.nodes[p].right |= kHoisted;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -396,6 +421,8 @@ inline bool sphere_gb300(const RayPre& R, f3 C, float r, float tmin, float tmax,
     float hh = std::fma(hx, hx, std::fma(hy, hy, hz * hz));
     float r2 = r * r;
     float c = hh - r2;
+    // origin clearly outside and moving away from the centre: no hit
+    if (hb > 0.0f && c > (hh + r2) * 9.5367431640625e-07f) return false;  // 2^-20
     float discp;
     if (std::fabs(c) < (hh + r2) * 0.0625f) {
         // exact residuals of h = o - C (TwoDiff)
@@ -488,6 +515,7 @@ Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, 
             best = k;
         }
     };
+    for (int32_t k : B.hoist) leaf(k);  // huge spheres first (the ground)
     if (B.n == 1) {
         leaf(0);
     } else {
@@ -503,7 +531,7 @@ Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, 
                 float tn0 = 0, tn1 = 0;
                 int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
                 if (pl & kLeaf) {
-                    leaf(pl & ~kLeaf);
+                    if (!(pl & kHoisted)) leaf(pl & kSlotMask);
                 } else {
                     const vo_node& nd = B.nodes[pl];
                     if (nv) ++*nv;
@@ -512,7 +540,7 @@ Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, 
                     c0r = nd.right;
                 }
                 if (pr & kLeaf) {
-                    leaf(pr & ~kLeaf);
+                    if (!(pr & kHoisted)) leaf(pr & kSlotMask);
                 } else {
                     const vo_node& nd = B.nodes[pr];
                     if (nv) ++*nv;

@@ -92,8 +92,8 @@ def test_lbvh_structure(oracle):
             i = stack.pop()
             for c in (int(nodes[i]["left"]), int(nodes[i]["right"])):
                 if c < 0:
-                    seen_leaf.add(c & 0x7FFFFFFF)
-                    k = c & 0x7FFFFFFF
+                    seen_leaf.add(c & 0x3FFFFFFF)  # bit 30 marks a hoisted leaf
+                    k = c & 0x3FFFFFFF
                     s = sp[b["ids"][k]]
                     assert np.all(nodes[i]["lo"] <= s["center"] - abs(s["radius"]))
                     assert np.all(nodes[i]["hi"] >= s["center"] + abs(s["radius"]))

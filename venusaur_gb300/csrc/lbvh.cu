@@ -16,6 +16,7 @@
 #include "venu_internal.h"
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -36,6 +37,39 @@ __device__ __forceinline__ float u2f(uint32_t u) {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
 }
 
+// Build-time control block: centroid bounds (order-preserving encoded),
+// the bounds used for quantisation, and the hoisted-sphere list.
+struct LbvhCtl {
+    uint32_t b0[6];       // all centroids: lo.xyz, hi.xyz
+    float bounds[6];      // the same bounds as floats
+    uint32_t hoist_cnt;   // huge spheres found
+    uint32_t nhoist;      // hoisted (<= kMaxHoisted), 0 if more than kHoistCandidates
+    int32_t hoist[kMaxHoisted];
+    uint32_t hoist_buf[64];
+};
+constexpr uint32_t kHoistCandidates = 64;
+
+// A sphere is huge when its radius exceeds a quarter of the largest extent of
+// all centroids (the r = 1000 ground sphere of the RTIOW scene).
+__device__ __forceinline__ float huge_threshold(const uint32_t* b0) {
+    float m = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) m = fmaxf(m, u2f(b0[3 + a]) - u2f(b0[a]));
+    return 0.25f * m;
+}
+
+__global__ void k_lbvh_init(LbvhCtl* c) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        for (int a = 0; a < 3; ++a) {
+            c->b0[a] = 0xffffffffu;
+            c->b0[3 + a] = 0u;
+        }
+        c->hoist_cnt = 0;
+        c->nhoist = 0;
+    }
+}
+
+// Centroid bounds (exact min/max through order-preserving integer atomics).
 __global__ void k_bounds(const venu_sphere* __restrict__ s, uint32_t n, uint32_t* __restrict__ bu) {
     uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0, 0, 0};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -80,27 +114,77 @@ __device__ __forceinline__ uint32_t quant10(float c, float lo, float ext) {
     return (uint32_t)f;
 }
 
-__global__ void k_morton(const venu_sphere* __restrict__ s, uint32_t n, const uint32_t* __restrict__ bu,
-                         float* __restrict__ bounds_out, uint32_t* __restrict__ keys,
+// Morton codes quantised to the centroid bounds with one scale for all three
+// axes (the largest extent), so cells stay cubic: a flat scene is split flat
+// instead of its thin axis being stretched over 1024 levels.  (Measured on
+// the oracle: 27 % fewer box tests per segment on a 200 000-sphere scene and
+// 18 % on 1 M spheres than per-axis scaling, equal on the RTIOW scene.)
+__global__ void k_morton(const venu_sphere* __restrict__ s, uint32_t n, LbvhCtl* c, uint32_t* __restrict__ keys,
                          uint32_t* __restrict__ vals) {
-    float lo[3], ext[3];
+    const uint32_t* bu = c->b0;
+    float lo[3], ext = 0.0f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         lo[a] = u2f(bu[a]);
         float hi = u2f(bu[3 + a]);
-        ext[a] = hi - lo[a];
+        ext = fmaxf(ext, hi - lo[a]);
         if (blockIdx.x == 0 && threadIdx.x == 0) {
-            bounds_out[a] = lo[a];
-            bounds_out[3 + a] = hi;
+            c->bounds[a] = lo[a];
+            c->bounds[3 + a] = hi;
         }
     }
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t qx = quant10(s[i].center[0], lo[0], ext[0]);
-        uint32_t qy = quant10(s[i].center[1], lo[1], ext[1]);
-        uint32_t qz = quant10(s[i].center[2], lo[2], ext[2]);
+        uint32_t qx = quant10(s[i].center[0], lo[0], ext);
+        uint32_t qy = quant10(s[i].center[1], lo[1], ext);
+        uint32_t qz = quant10(s[i].center[2], lo[2], ext);
         keys[i] = (spread10(qx) << 2) | (spread10(qy) << 1) | spread10(qz);
         vals[i] = i;
     }
+}
+
+// Huge spheres in slot order -> candidates (unordered, at most 64).
+__global__ void k_hoist_collect(const float4* __restrict__ sph, uint32_t n, LbvhCtl* c) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float thr = huge_threshold(c->b0);
+    if (fabsf(sph[k].w) > thr) {
+        const uint32_t i = atomicAdd(&c->hoist_cnt, 1u);
+        if (i < kHoistCandidates) c->hoist_buf[i] = k;
+    }
+}
+
+// The (at most 4) lowest huge slots are hoisted and their leaf words flagged;
+// with more than 64 huge spheres nothing is hoisted (deterministically).
+__global__ void k_hoist_finalize(LbvhCtl* c, const int32_t* __restrict__ pleaf, float4* nodes, uint32_t n) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const uint32_t cnt = c->hoist_cnt;
+    if (cnt == 0 || cnt > kHoistCandidates) {
+        c->nhoist = 0;
+        return;
+    }
+    uint32_t buf[kHoistCandidates];
+    for (uint32_t i = 0; i < cnt; ++i) buf[i] = c->hoist_buf[i];
+    for (uint32_t i = 1; i < cnt; ++i) {  // insertion sort
+        uint32_t v = buf[i], j = i;
+        while (j > 0 && buf[j - 1] > v) {
+            buf[j] = buf[j - 1];
+            --j;
+        }
+        buf[j] = v;
+    }
+    const uint32_t nh = cnt < (uint32_t)kMaxHoisted ? cnt : (uint32_t)kMaxHoisted;
+    for (uint32_t i = 0; i < nh; ++i) {
+        const uint32_t k = buf[i];
+        const int32_t p = pleaf[k];
+        c->hoist[i] = (int32_t)k;
+        if (p < 0 || (uint32_t)p >= n - 1) continue;
+        const int32_t want = (int32_t)k | kLeaf;
+        if (__float_as_int(nodes[2 * p].w) == want)
+            nodes[2 * p].w = __int_as_float(want | kHoisted);
+        else if (__float_as_int(nodes[2 * p + 1].w) == want)
+            nodes[2 * p + 1].w = __int_as_float(want | kHoisted);
+    }
+    c->nhoist = nh;
 }
 
 // Per-tile digit histogram, digit-major: hist[d * ntiles + tile].
@@ -266,6 +350,51 @@ __global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* __re
 
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
+// Device buffers of one LBVH build: outputs and scratch.
+struct LbvhBuffers {
+    float4 *nodes, *sph, *mat;
+    uint32_t *meta, *keys;
+    LbvhCtl* ctl;
+    uint32_t *keys_alt, *vals, *vals_alt, *hist, *arrive;
+    int32_t *pint, *pleaf;
+    float4* leafbox;
+};
+
+// The whole build, asynchronously on `st`; both venu_scene_create and
+// venu_lbvh_build_noalloc run exactly this sequence.
+cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const LbvhBuffers& B) {
+    const uint32_t nint = n > 1 ? n - 1 : 1;
+    const uint32_t ntiles = cdiv(n, kTileKeys);
+    k_lbvh_init<<<1, 32, 0, st>>>(B.ctl);
+    cudaError_t e = cudaMemsetAsync(B.arrive, 0, sizeof(uint32_t) * nint, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.pint, 0xff, sizeof(int32_t) * nint, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B.pleaf, 0xff, sizeof(int32_t) * n, st);
+    if (e != cudaSuccess) return e;
+    const uint32_t blocks = std::min(cdiv(n, 256), (uint32_t)(sm_count() * 8));
+    k_bounds<<<blocks, 256, 0, st>>>(s, n, B.ctl->b0);
+    k_morton<<<blocks, 256, 0, st>>>(s, n, B.ctl, B.keys, B.vals);
+    uint32_t *kin = B.keys, *kout = B.keys_alt, *vin = B.vals, *vout = B.vals_alt;
+    const uint32_t sblocks = cdiv(ntiles, kWarpsPerBlock);
+    for (int shift = 0; shift < 32; shift += kRadixBits) {
+        k_hist<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, n, shift, ntiles, B.hist);
+        k_scan<<<1, 1024, 0, st>>>(B.hist, kBuckets * ntiles);
+        k_scatter<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, vin, n, shift, ntiles, B.hist, kout, vout);
+        std::swap(kin, kout);
+        std::swap(vin, vout);
+    }
+    // four passes: the sorted codes / ids are back in B.keys / B.vals
+    if (n > 1) {
+        k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(B.keys, (int)n, B.nodes, B.pint, B.pleaf);
+        k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, (int)n, B.nodes, B.pint, B.pleaf, B.leafbox, B.arrive);
+    }
+    k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, n, B.sph, B.mat, B.meta);
+    if (n > 1) {
+        k_hoist_collect<<<cdiv(n, 256), 256, 0, st>>>(B.sph, n, B.ctl);
+        k_hoist_finalize<<<1, 32, 0, st>>>(B.ctl, B.pleaf, B.nodes, n);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 void free_scene(venu_scene* s) {
@@ -289,94 +418,70 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     }
     const uint32_t ntiles = cdiv(n, kTileKeys);
     const size_t hist_n = (size_t)kBuckets * ntiles;
-    // persistent buffers
     size_t bytes = 0;
     auto alloc = [&](void** p, size_t b) -> cudaError_t {
         bytes += b;
         return cudaMalloc(p, b ? b : 16);
     };
-    uint32_t nint = n > 1 ? n - 1 : 1;
+    const uint32_t nint = n > 1 ? n - 1 : 1;
     VENU_CUDA(alloc((void**)&S->nodes, sizeof(float4) * 2 * nint));
     VENU_CUDA(alloc((void**)&S->sph, sizeof(float4) * n));
     VENU_CUDA(alloc((void**)&S->mat, sizeof(float4) * n));
     VENU_CUDA(alloc((void**)&S->meta, sizeof(uint32_t) * n));
     VENU_CUDA(alloc((void**)&S->keys, sizeof(uint32_t) * n));
     S->bytes = bytes;
-    // scratch
-    uint32_t *bu = nullptr, *keys_alt = nullptr, *vals = nullptr, *vals_alt = nullptr, *hist = nullptr,
-             *arrive = nullptr;
-    int32_t *pint = nullptr, *pleaf = nullptr;
-    float4* leafbox = nullptr;
-    float* bounds_dev = nullptr;
+    LbvhBuffers B{};
+    B.nodes = S->nodes;
+    B.sph = S->sph;
+    B.mat = S->mat;
+    B.meta = S->meta;
+    B.keys = S->keys;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     venu_status rc = VENU_OK;
-    auto fail = [&](cudaError_t e, const char* what) {
-        rc = cuda_fail(e, what);
-    };
-#define STEP(call)                              \
-    do {                                        \
-        cudaError_t _e = (call);                \
-        if (_e != cudaSuccess) {                \
-            fail(_e, #call);                    \
-            goto done;                          \
-        }                                       \
+    LbvhCtl hc;
+#define STEP(call)                               \
+    do {                                         \
+        cudaError_t _e = (call);                 \
+        if (_e != cudaSuccess) {                 \
+            rc = cuda_fail(_e, #call);           \
+            goto done;                           \
+        }                                        \
     } while (0)
-    STEP(cudaMalloc(&bu, 6 * sizeof(uint32_t) + 6 * sizeof(float)));
-    bounds_dev = reinterpret_cast<float*>(bu + 6);
-    STEP(cudaMalloc(&keys_alt, sizeof(uint32_t) * n));
-    STEP(cudaMalloc(&vals, sizeof(uint32_t) * n));
-    STEP(cudaMalloc(&vals_alt, sizeof(uint32_t) * n));
-    STEP(cudaMalloc(&hist, sizeof(uint32_t) * hist_n));
-    STEP(cudaMalloc(&arrive, sizeof(uint32_t) * nint));
-    STEP(cudaMalloc(&pint, sizeof(int32_t) * nint));
-    STEP(cudaMalloc(&pleaf, sizeof(int32_t) * n));
-    STEP(cudaMalloc(&leafbox, sizeof(float4) * 2 * n));
+    STEP(cudaMalloc(&B.ctl, sizeof(LbvhCtl)));
+    STEP(cudaMalloc(&B.keys_alt, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&B.vals, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&B.vals_alt, sizeof(uint32_t) * n));
+    STEP(cudaMalloc(&B.hist, sizeof(uint32_t) * hist_n));
+    STEP(cudaMalloc(&B.arrive, sizeof(uint32_t) * nint));
+    STEP(cudaMalloc(&B.pint, sizeof(int32_t) * nint));
+    STEP(cudaMalloc(&B.pleaf, sizeof(int32_t) * n));
+    STEP(cudaMalloc(&B.leafbox, sizeof(float4) * 2 * n));
     STEP(cudaEventCreate(&e0));
     STEP(cudaEventCreate(&e1));
     STEP(cudaEventRecord(e0, st));
+    STEP(launch_lbvh(spheres_dev, n, st, B));
+    STEP(cudaEventRecord(e1, st));
+    STEP(cudaMemcpyAsync(&hc, B.ctl, sizeof(LbvhCtl), cudaMemcpyDeviceToHost, st));
+    STEP(cudaStreamSynchronize(st));
     {
-        const uint32_t init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
-        STEP(cudaMemcpyAsync(bu, init, sizeof(init), cudaMemcpyHostToDevice, st));
-        STEP(cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * nint, st));
-        STEP(cudaMemsetAsync(pleaf, 0xff, sizeof(int32_t) * n, st));
-        STEP(cudaMemsetAsync(pint, 0xff, sizeof(int32_t) * nint, st));
-        const uint32_t blocks = std::min(cdiv(n, 256), (uint32_t)(sm_count() * 8));
-        k_bounds<<<blocks, 256, 0, st>>>(spheres_dev, n, bu);
-        k_morton<<<blocks, 256, 0, st>>>(spheres_dev, n, bu, bounds_dev, S->keys, vals);
-        uint32_t *kin = S->keys, *kout = keys_alt, *vin = vals, *vout = vals_alt;
-        const uint32_t sblocks = cdiv(ntiles, kWarpsPerBlock);
-        for (int shift = 0; shift < 32; shift += kRadixBits) {
-            k_hist<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, n, shift, ntiles, hist);
-            k_scan<<<1, 1024, 0, st>>>(hist, (uint32_t)hist_n);
-            k_scatter<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, vin, n, shift, ntiles, hist, kout, vout);
-            std::swap(kin, kout);
-            std::swap(vin, vout);
-        }
-        // 4 passes: sorted data is back in S->keys / vals.
-        if (n > 1) {
-            k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(S->keys, (int)n, S->nodes, pint, pleaf);
-            k_refit<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, (int)n, S->nodes, pint, pleaf, leafbox, arrive);
-        }
-        k_gather<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, n, S->sph, S->mat, S->meta);
-        STEP(cudaGetLastError());
-        STEP(cudaEventRecord(e1, st));
-        STEP(cudaMemcpyAsync(S->bounds, bounds_dev, 6 * sizeof(float), cudaMemcpyDeviceToHost, st));
-        STEP(cudaStreamSynchronize(st));
         float ms = 0.0f;
         STEP(cudaEventElapsedTime(&ms, e0, e1));
         S->build_ms = ms;
+        std::memcpy(S->bounds, hc.bounds, sizeof(S->bounds));
+        S->nhoist = n > 1 ? hc.nhoist : 0u;
+        for (int i = 0; i < kMaxHoisted; ++i) S->hoist[i] = hc.hoist[i];
     }
 #undef STEP
 done:
-    cudaFree(bu);
-    cudaFree(keys_alt);
-    cudaFree(vals);
-    cudaFree(vals_alt);
-    cudaFree(hist);
-    cudaFree(arrive);
-    cudaFree(pint);
-    cudaFree(pleaf);
-    cudaFree(leafbox);
+    cudaFree(B.ctl);
+    cudaFree(B.keys_alt);
+    cudaFree(B.vals);
+    cudaFree(B.vals_alt);
+    cudaFree(B.hist);
+    cudaFree(B.arrive);
+    cudaFree(B.pint);
+    cudaFree(B.pleaf);
+    cudaFree(B.leafbox);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return rc;
@@ -395,8 +500,8 @@ constexpr uint32_t kNoAllocMaxSpheres = VENU_NOALLOC_MAX_SPHERES;
 constexpr uint32_t kNoAllocMaxTiles = (kNoAllocMaxSpheres + kTileKeys - 1) / kTileKeys;
 constexpr size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 constexpr size_t kNA = kNoAllocMaxSpheres;
-constexpr size_t kOffBounds = 0;                                      // 6 uint32 + 6 float
-constexpr size_t kOffKeysAlt = al256(kOffBounds + 48);
+constexpr size_t kOffCtl = 0;                                         // LbvhCtl
+constexpr size_t kOffKeysAlt = al256(kOffCtl + sizeof(LbvhCtl));
 constexpr size_t kOffVals = al256(kOffKeysAlt + 4 * kNA);
 constexpr size_t kOffValsAlt = al256(kOffVals + 4 * kNA);
 constexpr size_t kOffHist = al256(kOffValsAlt + 4 * kNA);
@@ -470,45 +575,25 @@ extern "C" venu_status venu_lbvh_build_noalloc(const venu_sphere* spheres_dev, u
     venu_status ss = noalloc_scratch(&base);
     if (ss != VENU_OK) return ss;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    uint32_t* bu = reinterpret_cast<uint32_t*>(base + kOffBounds);
-    float* bounds = reinterpret_cast<float*>(base + kOffBounds + 24);
-    uint32_t* keys_alt = reinterpret_cast<uint32_t*>(base + kOffKeysAlt);
-    uint32_t* vals = reinterpret_cast<uint32_t*>(base + kOffVals);
-    uint32_t* vals_alt = reinterpret_cast<uint32_t*>(base + kOffValsAlt);
-    uint32_t* hist = reinterpret_cast<uint32_t*>(base + kOffHist);
-    uint32_t* arrive = reinterpret_cast<uint32_t*>(base + kOffArrive);
-    int32_t* pint = reinterpret_cast<int32_t*>(base + kOffParentInt);
-    int32_t* pleaf = reinterpret_cast<int32_t*>(base + kOffParentLeaf);
-    float4* leafbox = reinterpret_cast<float4*>(base + kOffLeafBox);
-    const uint32_t nint = n > 1 ? n - 1 : 1;
-    const uint32_t ntiles = cdiv(n, kTileKeys);
-    // The scratch keeps the previous call's contents: reset what must start
-    // from a known value (min/max seeds of the bounds, arrival counters,
-    // parent links).
-    VENU_CUDA(cudaMemsetAsync(bu, 0xff, 3 * sizeof(uint32_t), st));
-    VENU_CUDA(cudaMemsetAsync(bu + 3, 0x00, 3 * sizeof(uint32_t), st));
-    VENU_CUDA(cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * nint, st));
-    VENU_CUDA(cudaMemsetAsync(pint, 0xff, sizeof(int32_t) * nint, st));
-    VENU_CUDA(cudaMemsetAsync(pleaf, 0xff, sizeof(int32_t) * n, st));
-    const uint32_t blocks = std::min(cdiv(n, 256), (uint32_t)(sm_count() * 8));
-    k_bounds<<<blocks, 256, 0, st>>>(spheres_dev, n, bu);
-    k_morton<<<blocks, 256, 0, st>>>(spheres_dev, n, bu, bounds, morton_out, vals);
-    uint32_t *kin = morton_out, *kout = keys_alt, *vin = vals, *vout = vals_alt;
-    const uint32_t sblocks = cdiv(ntiles, kWarpsPerBlock);
-    for (int shift = 0; shift < 32; shift += kRadixBits) {
-        k_hist<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, n, shift, ntiles, hist);
-        k_scan<<<1, 1024, 0, st>>>(hist, (uint32_t)(kBuckets * ntiles));
-        k_scatter<<<sblocks, 32 * kWarpsPerBlock, 0, st>>>(kin, vin, n, shift, ntiles, hist, kout, vout);
-        std::swap(kin, kout);
-        std::swap(vin, vout);
-    }
-    float4* nodes = reinterpret_cast<float4*>(nodes_out);
-    if (n > 1) {
-        k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(morton_out, (int)n, nodes, pint, pleaf);
-        k_refit<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, (int)n, nodes, pint, pleaf, leafbox, arrive);
-    }
-    k_gather<<<cdiv(n, 256), 256, 0, st>>>(spheres_dev, vals, n, reinterpret_cast<float4*>(spheres_out),
-                                          reinterpret_cast<float4*>(materials_out), meta_out);
+    LbvhBuffers B{};
+    B.nodes = reinterpret_cast<float4*>(nodes_out);
+    B.sph = reinterpret_cast<float4*>(spheres_out);
+    B.mat = reinterpret_cast<float4*>(materials_out);
+    B.meta = meta_out;
+    B.keys = morton_out;
+    B.ctl = reinterpret_cast<LbvhCtl*>(base + kOffCtl);
+    B.keys_alt = reinterpret_cast<uint32_t*>(base + kOffKeysAlt);
+    B.vals = reinterpret_cast<uint32_t*>(base + kOffVals);
+    B.vals_alt = reinterpret_cast<uint32_t*>(base + kOffValsAlt);
+    B.hist = reinterpret_cast<uint32_t*>(base + kOffHist);
+    B.arrive = reinterpret_cast<uint32_t*>(base + kOffArrive);
+    B.pint = reinterpret_cast<int32_t*>(base + kOffParentInt);
+    B.pleaf = reinterpret_cast<int32_t*>(base + kOffParentLeaf);
+    B.leafbox = reinterpret_cast<float4*>(base + kOffLeafBox);
+    // The scratch keeps the previous call's contents; launch_lbvh resets what
+    // must start from a known value (bounds seeds, hoist counters, arrival
+    // counters, parent links) before using it.
+    VENU_CUDA(launch_lbvh(spheres_dev, n, st, B));
     VENU_CUDA(cudaGetLastError());
     return VENU_OK;
 }

@@ -313,6 +313,8 @@ SceneView view_of(const venu_scene* s) {
     v.mat = s->mat;
     v.meta = s->meta;
     v.n = s->n;
+    v.nhoist = s->nhoist;
+    for (int i = 0; i < kMaxHoisted; ++i) v.hoist[i] = s->hoist[i];
     return v;
 }
 

@@ -138,8 +138,13 @@ __device__ __forceinline__ float reflectance(float cosine, float ref_idx) {
 // ---------------------------------------------------------------------------
 // Scene view: LBVH nodes + spheres/materials in Morton (slot) order.
 // ---------------------------------------------------------------------------
+// Child words: bit 31 = leaf, bit 30 = leaf already tested before the
+// traversal (a hoisted huge sphere), bits 0-29 = slot or internal index.
 constexpr int32_t kLeaf = (int32_t)0x80000000u;
+constexpr int32_t kHoisted = 0x40000000;
+constexpr int32_t kSlotMask = 0x3fffffff;
 constexpr int32_t kNone = 0x7fffffff;
+constexpr int kMaxHoisted = 4;
 
 struct SceneView {
     const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
@@ -147,6 +152,8 @@ struct SceneView {
     const float4* __restrict__ mat;    // {albedo, fuzz or ir} per slot
     const uint32_t* __restrict__ meta; // original id | material << 30
     uint32_t n;
+    uint32_t nhoist;                   // huge spheres tested first by every ray
+    int32_t hoist[kMaxHoisted];        // their slots (ascending)
 };
 
 struct RayPre {
@@ -210,6 +217,9 @@ __device__ __forceinline__ bool sphere_test(const RayPre& R, float4 S, float tmi
     float hh = fmaf(hx, hx, fmaf(hy, hy, hz * hz));
     float r2 = r * r;
     float c = hh - r2;
+    // Origin clearly outside (c above its rounding bound) and moving away from
+    // the centre (h.d > 0): both roots are negative, no hit.
+    if (hb > 0.0f && c > (hh + r2) * 9.5367431640625e-07f) return false;  // 2^-20
     float discp;
     if (fabsf(c) < (hh + r2) * 0.0625f) {
         // exact residuals of h = o - C (TwoDiff)
@@ -332,6 +342,10 @@ struct Tracer {
         sp = 0;
         const uint32_t n = S.n;
         if (n == 0) return false;
+        // Huge spheres (the ground) are tested by every ray up front, with the
+        // whole warp converged; their leaves are skipped during traversal and
+        // their hit distance already culls boxes behind them.
+        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S, S.hoist[h], K);
         if (n == 1) {
             leaf(S, 0, K);
             return false;
@@ -355,7 +369,7 @@ struct Tracer {
                                          int2* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
         const uint32_t n = S.n;
         if (--guard == 0u || (!(pl & kLeaf) && (uint32_t)pl >= n - 1u) || (!(pr & kLeaf) && (uint32_t)pr >= n - 1u) ||
-            (uint32_t)(pl & ~kLeaf) >= n || (uint32_t)(pr & ~kLeaf) >= n) {
+            (uint32_t)(pl & kSlotMask) >= n || (uint32_t)(pr & kSlotMask) >= n) {
             overflow = true;
             return false;
         }
@@ -363,7 +377,7 @@ struct Tracer {
         float tn0 = 0.0f, tn1 = 0.0f;
         int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
         if (pl & kLeaf) {
-            leaf(S, pl & ~kLeaf, K);
+            if (!(pl & kHoisted)) leaf(S, pl & kSlotMask, K);
         } else {
             float4 lo = __ldg(S.nodes + 2 * pl), hi = __ldg(S.nodes + 2 * pl + 1);
             if (COUNT) ++K.nodes;
@@ -372,7 +386,7 @@ struct Tracer {
             c0r = __float_as_int(hi.w);
         }
         if (pr & kLeaf) {
-            leaf(S, pr & ~kLeaf, K);
+            if (!(pr & kHoisted)) leaf(S, pr & kSlotMask, K);
         } else {
             float4 lo = __ldg(S.nodes + 2 * pr), hi = __ldg(S.nodes + 2 * pr + 1);
             if (COUNT) ++K.nodes;

@@ -32,6 +32,8 @@ struct venu_scene {
     uint32_t* meta = nullptr;  // original id | material << 30
     uint32_t* keys = nullptr;  // sorted Morton codes
     float bounds[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t nhoist = 0;          // huge spheres tested before traversal
+    int32_t hoist[4] = {0, 0, 0, 0};
     float build_ms = 0.0f;
     uint64_t bytes = 0;
 };
