@@ -284,6 +284,66 @@ VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* f
                                         uint32_t* count);
 VENU_API venu_status venu_batch_stats_get(venu_batch* b, venu_batch_stats* out);
 VENU_API venu_status venu_batch_destroy(venu_batch* b);
+
+/* ---- render server (continuous batching) ------------------------------
+ * No counterpart in the reference (it serves one interactive window).  A
+ * server owns one host thread and one venu_batch.  Requests arrive at any
+ * time from any thread; the server admits them first-come first-served
+ * while the device memory they need fits the HBM budget, keeps scene BVHs
+ * resident across requests that share a scene_key (evicting unused ones,
+ * least recently used first, when the budget needs room), advances every
+ * admitted job together in the shared path pool a few iterations at a time,
+ * and retires finished jobs: image copied to host memory, buffers freed,
+ * latency recorded.  A request that can never fit the budget fails with
+ * VENU_ERR_OOM; a cancelled pending request completes with
+ * VENU_ERR_CANCELLED; a failure of one request never stops the others. */
+typedef struct venu_server venu_server;
+
+typedef struct venu_request {
+    const venu_sphere* spheres; /* host; copied by venu_server_submit (may be NULL if cached) */
+    uint32_t num_spheres;
+    uint32_t reserved;
+    uint64_t scene_key;         /* != 0: requests with the same key share one resident BVH */
+    venu_camera camera;
+    venu_render_opts opts;      /* accumulation is reset per request */
+    uint64_t tag;               /* returned with the result */
+} venu_request;
+
+typedef struct venu_result {
+    uint64_t request_id;
+    uint64_t tag;
+    int32_t status;             /* venu_status of the request */
+    uint32_t width, height;
+    uint32_t reserved;
+    const uint8_t* image8;      /* host sRGB RGBA8, valid until venu_server_release */
+    double t_submit, t_admit, t_done; /* seconds, steady clock of the server */
+} venu_result;
+
+typedef struct venu_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t resident_bytes;    /* scenes + admitted jobs */
+    uint64_t budget_bytes;
+    uint64_t segments;          /* ray casts traced by the server */
+    uint32_t active, pending;
+    double p50_ms, p99_ms;      /* request latency (submit -> image on host), completed requests */
+    double busy_seconds;        /* wall time with at least one admitted job */
+} venu_server_stats;
+
+/* Test hooks: make the next admission fail as if its allocation failed
+ * (VENU_INJECT_ALLOC) or its BVH build failed (VENU_INJECT_SCENE). */
+#define VENU_INJECT_ALLOC 1u
+#define VENU_INJECT_SCENE 2u
+
+VENU_API venu_status venu_server_create(uint64_t hbm_budget_bytes, uint32_t pool_paths, uint32_t max_jobs,
+                                        uint32_t iterations_per_step, venu_server** out);
+VENU_API venu_status venu_server_submit(venu_server* s, const venu_request* req, uint64_t* request_id);
+/* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY). */
+VENU_API venu_status venu_server_wait(venu_server* s, uint64_t request_id, double timeout_s, venu_result* out);
+VENU_API venu_status venu_server_cancel(venu_server* s, uint64_t request_id);
+VENU_API venu_status venu_server_release(venu_server* s, uint64_t request_id);
+VENU_API venu_status venu_server_inject(venu_server* s, uint32_t what);
+VENU_API venu_status venu_server_stats_get(venu_server* s, venu_server_stats* out);
+VENU_API venu_status venu_server_destroy(venu_server* s);
 VENU_API venu_status venu_renderer_destroy(venu_renderer* r);
 
 #ifdef __cplusplus

@@ -1,0 +1,86 @@
+"""GPU tests of the render server (continuous batching under an HBM budget).
+Failures are made on the host (injected allocation / build failures, a
+cancelled request, a request larger than the budget); the GPU never faults."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(oracle, seed, W, H, spp, depth=6):
+    sp = oracle.scene_rtiow(seed)
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    want = oracle.render(sp, cam, W, H, spp, subframe=1, max_depth=depth, mode=pyoracle.MODE_GB300)
+    return sp, cam, want
+
+
+def test_server_results_match_oracle(venu, oracle, cuda):
+    srv = venu.Server(hbm_budget_bytes=1 << 30, pool_paths=2000, max_jobs=8, iterations_per_step=4)
+    cases = [_case(oracle, s, W, H, spp) for s, W, H, spp in ((0, 32, 18, 2), (1, 20, 20, 3), (2, 16, 9, 1))]
+    ids = []
+    for i, (sp, cam, _) in enumerate(cases):
+        ids.append(srv.submit(cam, *((32, 18, 2), (20, 20, 3), (16, 9, 1))[i], spheres=sp, max_depth=6, tag=i))
+    # same scene key twice: the second request reuses the resident BVH
+    sp0, cam0, want0 = cases[0]
+    k1 = srv.submit(cam0, 32, 18, 2, spheres=sp0, scene_key=77, max_depth=6)
+    k2 = srv.submit(cam0, 32, 18, 2, spheres=None, scene_key=77, max_depth=6)
+    for i, rid in enumerate(ids):
+        r = srv.wait(rid)
+        assert r["status"] == 0 and r["tag"] == i
+        want = cases[i][2]["image8"].reshape(r["image"].shape)
+        assert np.abs(r["image"].astype(int) - want.astype(int)).max() <= 1
+    for rid in (k1, k2):
+        r = srv.wait(rid)
+        assert r["status"] == 0
+        assert np.abs(r["image"].astype(int) - want0["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    st = srv.stats()
+    assert st["completed"] == 5 and st["failed"] == 0 and st["p99_ms"] >= st["p50_ms"] > 0
+    srv.close()
+
+
+def test_server_budget_fifo_and_faults(venu, oracle, cuda):
+    sp, cam, want = _case(oracle, 0, 24, 16, 2)
+    job = venu.Batch.job_bytes(24, 16, 2) + 24 * 16 * 36 + 485 * 72 + 256
+    # room for about one job at a time: requests queue and run in order
+    srv = venu.Server(hbm_budget_bytes=job + 40000, pool_paths=1000, max_jobs=4, iterations_per_step=2)
+    too_big = srv.submit(cam, 2000, 2000, 64, spheres=sp)
+    assert srv.wait(too_big)["status"] == 3  # VENU_ERR_OOM: can never fit the budget
+    ra = srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6))
+    assert ra["status"] == 0
+    assert np.abs(ra["image"].astype(int) - want["image8"].reshape(ra["image"].shape).astype(int)).max() <= 1
+    # injected allocation failure: that request fails, the next one runs
+    srv.inject(venu._lib.INJECT_ALLOC)
+    assert srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6))["status"] == 3
+    # FIFO under the budget: c is admitted before d; d can be cancelled while it waits
+    c = srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6)
+    d = srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6)
+    try:
+        srv.cancel(d)
+        cancelled = True
+    except venu.VenuError:
+        cancelled = False  # already admitted
+    rc, rd = srv.wait(c), srv.wait(d)
+    assert rc["status"] == 0
+    if cancelled:
+        assert rd["status"] == 7  # VENU_ERR_CANCELLED
+    else:
+        assert rd["status"] == 0 and rd["t_admit"] >= rc["t_admit"]
+    # injected BVH build failure
+    srv.inject(venu._lib.INJECT_SCENE)
+    assert srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6))["status"] == 2
+    assert srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp, max_depth=6))["status"] == 0
+    st = srv.stats()
+    assert st["failed"] == 3 + (1 if cancelled else 0)
+    srv.close()
+
+
+def test_server_rejects_malformed(venu, oracle, cuda):
+    srv = venu.Server(hbm_budget_bytes=1 << 28, max_jobs=2)
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, 1.0, 0.1, 10.0)
+    with pytest.raises(venu.VenuError):
+        srv.submit(cam, 1, 1, 1, spheres=oracle.scene_rtiow(0))
+    with pytest.raises(venu.VenuError):
+        srv.submit(cam, 8, 8, 1, spheres=oracle.scene_rtiow(0), max_depth=0)
+    srv.close()

@@ -11,6 +11,7 @@ from .core import (  # noqa: F401
     Material,
     Renderer,
     Scene,
+    Server,
     Sphere,
     Wavefront,
     generate_random,
@@ -19,7 +20,7 @@ from .core import (  # noqa: F401
 )
 
 __all__ = [
-    "Batch", "Camera", "CUDAOutputBuffer", "DeviceScene", "Material", "Renderer", "Scene", "Sphere",
+    "Batch", "Camera", "CUDAOutputBuffer", "DeviceScene", "Material", "Renderer", "Scene", "Server", "Sphere",
     "Wavefront", "VenuError", "generate_random", "generate_rtiow", "new_accum", "lib",
     "SPHERE_DTYPE", "CAMERA_DTYPE", "NODE_DTYPE",
 ]

@@ -80,7 +80,27 @@ class BatchStats(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class Request(C.Structure):
+    _fields_ = [("spheres", C.c_void_p), ("num_spheres", C.c_uint32), ("reserved", C.c_uint32),
+                ("scene_key", C.c_uint64), ("camera", CameraC), ("opts", RenderOpts), ("tag", C.c_uint64)]
+
+
+class Result(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("reserved", C.c_uint32), ("image8", C.c_void_p), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("resident_bytes", C.c_uint64), ("budget_bytes", C.c_uint64), ("segments", C.c_uint64),
+                ("active", C.c_uint32), ("pending", C.c_uint32), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("busy_seconds", C.c_double)]
+
+
 BATCH_NO_GRAPH = 1
+INJECT_ALLOC = 1
+INJECT_SCENE = 2
 
 _lib = None
 
@@ -115,6 +135,14 @@ def lib() -> C.CDLL:
     L.venu_render.argtypes = [vp, vp, vp, C.POINTER(RenderOpts), vp, vp, vp, vp]
     L.venu_renderer_stats.argtypes = [vp, C.POINTER(RenderStats)]
     L.venu_renderer_destroy.argtypes = [vp]
+    L.venu_server_create.argtypes = [C.c_uint64, u32, u32, u32, C.POINTER(vp)]
+    L.venu_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
+    L.venu_server_wait.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(Result)]
+    L.venu_server_cancel.argtypes = [vp, C.c_uint64]
+    L.venu_server_release.argtypes = [vp, C.c_uint64]
+    L.venu_server_inject.argtypes = [vp, u32]
+    L.venu_server_stats_get.argtypes = [vp, C.POINTER(ServerStats)]
+    L.venu_server_destroy.argtypes = [vp]
     L.venu_batch_create.argtypes = [u32, u32, u32, C.POINTER(vp)]
     L.venu_batch_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.venu_batch_job_bytes.restype = C.c_uint64
@@ -131,7 +159,9 @@ def lib() -> C.CDLL:
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
                  "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
                  "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit",
-                 "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy"):
+                 "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy",
+                 "venu_server_create", "venu_server_submit", "venu_server_wait", "venu_server_cancel",
+                 "venu_server_release", "venu_server_inject", "venu_server_stats_get", "venu_server_destroy"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -496,3 +496,67 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """A venu_server: requests are admitted FIFO under an HBM budget and
+    rendered together in one shared path pool by the server's own thread."""
+
+    def __init__(self, hbm_budget_bytes: int, pool_paths: int = 0, max_jobs: int = 64,
+                 iterations_per_step: int = 8):
+        h = C.c_void_p()
+        check(lib().venu_server_create(int(hbm_budget_bytes), pool_paths, max_jobs, iterations_per_step,
+                                       C.byref(h)))
+        self.handle = h
+
+    def submit(self, camera: np.ndarray, width: int, height: int, spp: int, spheres=None, scene_key: int = 0,
+               subframe: int = 1, max_depth: int = 50, tag: int = 0) -> int:
+        r = _lib.Request()
+        arr = None
+        if spheres is not None:
+            arr = np.ascontiguousarray(spheres, SPHERE_DTYPE)
+            r.spheres = arr.ctypes.data
+            r.num_spheres = len(arr)
+        r.scene_key = scene_key
+        r.camera = _camera_c(camera)
+        r.opts = RenderOpts(width, height, spp, subframe, max_depth, 0)
+        r.tag = tag
+        rid = C.c_uint64()
+        check(lib().venu_server_submit(self.handle, C.byref(r), C.byref(rid)))
+        return int(rid.value)
+
+    def wait(self, request_id: int, timeout_s: float = 600.0, release: bool = True) -> dict:
+        res = _lib.Result()
+        check(lib().venu_server_wait(self.handle, request_id, timeout_s, C.byref(res)))
+        image = None
+        if res.image8:
+            n = res.width * res.height * 4
+            image = np.ctypeslib.as_array((C.c_uint8 * n).from_address(res.image8)).copy().reshape(
+                res.height, res.width, 4)
+        out = dict(request_id=res.request_id, tag=res.tag, status=res.status, image=image, t_submit=res.t_submit,
+                   t_admit=res.t_admit, t_done=res.t_done, latency_ms=1000.0 * (res.t_done - res.t_submit))
+        if release:
+            lib().venu_server_release(self.handle, request_id)
+        return out
+
+    def cancel(self, request_id: int) -> None:
+        check(lib().venu_server_cancel(self.handle, request_id))
+
+    def inject(self, what: int) -> None:
+        check(lib().venu_server_inject(self.handle, what))
+
+    def stats(self) -> dict:
+        s = _lib.ServerStats()
+        check(lib().venu_server_stats_get(self.handle, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in _lib.ServerStats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().venu_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
