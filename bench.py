@@ -116,19 +116,6 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_setup(n_gpus):
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    pg = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl" if n_gpus > 0 else "gloo")
-        pg = dist
-    return world, rank, local, pg
-
-
 def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     """Times the CPU port on a bounded row sample sized to ~target_s seconds."""
     from oracle import pyoracle
@@ -136,17 +123,18 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     mode = pyoracle.MODE_GB300 if mode is None else mode
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     r0 = H // 2
-    rows, spp_s = 2, min(spp, 4)
+    # probe: rate and segments per path, then size rows (and samples) to the target
+    rows, spp_s = 4, min(spp, 2)
     t0 = time.perf_counter()
     res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
                    rows=(r0, r0 + rows))
-    dt = time.perf_counter() - t0
-    # scale rows (up to the lower half of the image), then samples, to the target time
-    grow = target_s / max(dt, 1e-3)
-    new_rows = int(max(2, min(H - r0, rows * grow)))
-    grow /= new_rows / rows
-    rows = new_rows
-    spp_s = int(max(spp_s, min(spp, spp_s * grow)))
+    dt = max(time.perf_counter() - t0, 1e-3)
+    seg_per_path = res["segments"] / (rows * W * spp_s)
+    want_paths = (res["segments"] / dt) * target_s / max(seg_per_path, 1e-9)
+    spp_s = min(spp, 4)
+    rows = int(max(2, min(H - r0, want_paths / (W * spp_s))))
+    if rows == H - r0:
+        spp_s = int(max(spp_s, min(spp, want_paths / (W * rows))))
     t0 = time.perf_counter()
     res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
                    rows=(r0, r0 + rows))
@@ -225,6 +213,102 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
     }
 
 
+def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30):
+    """Serving: a Poisson request stream at ~80 % of the server's capacity;
+    the render server (continuous batching, resident BVHs, 150 GB HBM budget)
+    against the plain method serving the same stream one job at a time."""
+    import threading
+
+    from venusaur_gb300 import workloads
+
+    srv = venu.Server(budget, pool_paths=16 << 20, max_jobs=256, iterations_per_step=8)
+    scenes = {}
+
+    def spheres_of(j):
+        if j["scene_seed"] not in scenes:
+            scenes[j["scene_seed"]] = venu.generate_random(j["n"], j["scene_seed"])
+        return scenes[j["scene_seed"]]
+
+    def cam_of(j):
+        return venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
+
+    sent = set()
+
+    def submit(j):
+        key = 1 + j["scene_seed"]
+        sp = None if key in sent else spheres_of(j)
+        sent.add(key)
+        return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=sp, scene_key=key, max_depth=j["depth"])
+
+    # capacity: a burst of requests all at once
+    calib = workloads.serving_jobs(24, rate_per_s=1.0, seed=2)
+    t0 = time.perf_counter()
+    ids = [submit(j) for j in calib]
+    for i in ids:
+        assert srv.wait(i)["status"] == 0
+    cap_jobs_per_s = len(calib) / (time.perf_counter() - t0)
+    lam = util * cap_jobs_per_s
+    jobs = workloads.serving_jobs(n_requests, rate_per_s=lam, seed=3)
+    for j in jobs:
+        spheres_of(j)
+    seg0 = srv.stats()["segments"]
+    ids = [None] * len(jobs)
+    start = time.perf_counter()
+
+    def client():
+        for k, j in enumerate(jobs):
+            dt = start + j["arrival"] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids[k] = submit(j)
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    res = [srv.wait(i) for i in ids]
+    makespan = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+    lat = np.array([r["latency_ms"] for r in res])
+    st = srv.stats()
+    segs = st["segments"] - seg0
+    srv.close()
+    served = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+              "value": segs / makespan, "unit": UNIT, "makespan_s": makespan, "failed": int(st["failed"])}
+
+    # the plain method: one job at a time, same arrivals, resident BVHs
+    wf = venu.Wavefront(16 << 20)
+    if tuning:
+        wf.set_tuning(**tuning)
+    dscenes = {}
+    plain_lat = []
+    start = time.perf_counter()
+    tfree = 0.0
+    for j in jobs:
+        now = time.perf_counter() - start
+        if now < j["arrival"]:
+            time.sleep(j["arrival"] - now)
+        if j["scene_seed"] not in dscenes:
+            dscenes[j["scene_seed"]] = venu.DeviceScene(spheres_of(j))
+        acc = venu.new_accum(j["W"], j["H"])
+        img = torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda")
+        wf.render(dscenes[j["scene_seed"]], cam_of(j), j["W"], j["H"], j["spp"], acc, subframe=1,
+                  max_depth=j["depth"], reset=True, image8=img)
+        img.cpu()
+        tfree = time.perf_counter() - start
+        plain_lat.append(1000.0 * (tfree - j["arrival"]))
+    plat = np.array(plain_lat)
+    plain_makespan = tfree - jobs[0]["arrival"]
+    return {
+        "workload": f"{n_requests} requests, Poisson arrivals at {lam:.2f}/s (~{int(100 * util)} % of the "
+                    f"server's measured capacity {cap_jobs_per_s:.2f} jobs/s), scenes from 16 resident scenes with "
+                    "100..200000 spheres, resolutions {256x256, 512x512, 640x360, 1024x1024}, spp "
+                    "{8, 16, 32, 64, 128}, depth 50, HBM budget 150 GB",
+        "served": served,
+        "plain": {"p50_ms": float(np.percentile(plat, 50)), "p99_ms": float(np.percentile(plat, 99)),
+                  "value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
+                  "method": "venu_render one job at a time (FIFO), same arrivals"},
+    }
+
+
 def run_reference(args, cfg, world, rank):
     if rank != 0:
         return
@@ -268,7 +352,10 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
     args = ap.parse_args()
     cfg = CONFIGS[args.config]
-    world, rank, local, dist = dist_setup(args.gpus)
+    from venusaur_gb300.replicas import Replicas
+
+    rep = Replicas()
+    world, rank, local = rep.world, rep.rank, rep.local
     if args.impl == "reference":
         run_reference(args, cfg, world, rank)
         return
@@ -306,9 +393,7 @@ def main():
         step(i)
     torch.cuda.synchronize()
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
+    barrier = rep.barrier
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -316,10 +401,6 @@ def main():
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    segs = 0
-    trav_ms = 0.0
-    trav_n = 0
-    launches = 0
     e0.record(stream)
     for i in range(args.steps):
         step(args.warmup + i)
@@ -331,13 +412,9 @@ def main():
     # same workload (only the seed differs), so counts are per step
     st = wf.stats()
     segs_step = st["segments"]
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    total_segs = segs_step * args.steps * world
-    value = total_segs / (ms / 1000.0)
+    # replicas: segments of every rank over the slowest rank's time
+    total_segs, secs, value = rep.throughput(segs_step * args.steps, e0.elapsed_time(e1) / 1000.0)
+    ms = 1000.0 * secs
     launches = st["kernel_launches"] * args.steps
 
     # --- roofline of the traversal kernel -----------------------------------
@@ -424,11 +501,7 @@ def main():
     for i in range(args.steps):
         e2e_step(i + 1)
     t1 = time.perf_counter()
-    e2e_s = t1 - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = rep.max(t1 - t0)
     e2e = {"value": total_segs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(spheres.nbytes),
            "d2h_bytes_per_step": int(H * W * 4), "ms_per_step": 1000 * e2e_s / args.steps}
 
@@ -450,8 +523,9 @@ def main():
         "e2e": e2e,
         "roofline": roofline,
     }
-    if not args.no_batched:
+    if not args.no_batched and world == 1:
         line["batched"] = run_batched(venu, torch, tuning, max_paths)
+        line["served"] = run_served(venu, torch, tuning)
     if not args.no_cpu:
         from oracle import pyoracle
 

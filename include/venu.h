@@ -300,7 +300,9 @@ VENU_API venu_status venu_batch_destroy(venu_batch* b);
 typedef struct venu_server venu_server;
 
 typedef struct venu_request {
-    const venu_sphere* spheres; /* host; copied by venu_server_submit (may be NULL if cached) */
+    const venu_sphere* spheres; /* host; copied by venu_server_submit.  NULL with a
+                                   scene_key: use the resident scene of that key
+                                   (VENU_ERR_INVALID if it is not resident) */
     uint32_t num_spheres;
     uint32_t reserved;
     uint64_t scene_key;         /* != 0: requests with the same key share one resident BVH */

@@ -34,6 +34,7 @@ struct Request {
     uint64_t id = 0;
     venu_request req{};
     std::vector<venu_sphere> spheres;
+    bool no_spheres = false;  // keyed request relying on a resident scene
     int32_t status = VENU_ERR_NOT_READY;
     bool done = false, cancelled = false;
     double t_submit = 0, t_admit = 0, t_done = 0;
@@ -151,6 +152,10 @@ void admit(venu_server* s, Request& R) {
     const uint64_t key = R.req.scene_key ? R.req.scene_key : (kPrivateKey | R.id);
     auto it = s->scenes.find(key);
     if (it == s->scenes.end()) {
+        if (R.no_spheres) {  // its scene was never sent or has been evicted
+            complete(s, R, VENU_ERR_INVALID);
+            return;
+        }
         if (inj & VENU_INJECT_SCENE) {
             complete(s, R, VENU_ERR_CUDA);
             return;
@@ -388,6 +393,7 @@ extern "C" venu_status venu_server_submit(venu_server* s, const venu_request* re
     auto R = std::make_unique<Request>();
     R->req = *req;
     if (req->num_spheres) R->spheres.assign(req->spheres, req->spheres + req->num_spheres);
+    R->no_spheres = (req->scene_key != 0 && req->spheres == nullptr);
     R->req.spheres = nullptr;
     std::lock_guard<std::mutex> lock(s->mu);
     if (s->stop) {
