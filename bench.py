@@ -144,18 +144,21 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     return rate, dt, sample, res["segments"]
 
 
-def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
-    """Mixed-scene workload: the plain method (one venu_render per job, in
-    sequence) against the batched engine (all jobs in one shared pool, one
-    graph launch).  BVHs are built before timing (resident scenes)."""
+def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
+    """The plain method (one venu_render per job, in sequence) against the
+    batched engine (all jobs in one shared pool, one graph launch) on the
+    mixed-scene workload (or, small=True, on many small RTIOW renders).
+    BVHs are built before timing (resident scenes)."""
     from venusaur_gb300 import workloads
 
-    jobs = workloads.mixed_jobs(n_jobs)
+    jobs = workloads.small_jobs() if small else workloads.mixed_jobs(n_jobs)
     scenes = {}
     for j in jobs:
-        key = (j["n"], j["scene_seed"])
+        key = ("rtiow", j["rtiow_seed"]) if small else (j["n"], j["scene_seed"])
+        j["key"] = key
         if key not in scenes:
-            scenes[key] = venu.DeviceScene(venu.generate_random(j["n"], j["scene_seed"]))
+            sp = venu.generate_rtiow(j["rtiow_seed"]) if small else venu.generate_random(j["n"], j["scene_seed"])
+            scenes[key] = venu.DeviceScene(sp)
     cams = [venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0) for j in jobs]
     acc_plain = [venu.new_accum(j["W"], j["H"]) for j in jobs]
     acc_batch = [venu.new_accum(j["W"], j["H"]) for j in jobs]
@@ -164,20 +167,20 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
     wf = venu.Wavefront(max_paths)
     if tuning:
         wf.set_tuning(**tuning)
-    b = venu.Batch(pool_paths=max_paths, max_jobs=n_jobs)
+    b = venu.Batch(pool_paths=max_paths, max_jobs=len(jobs))
     if tuning:
         b.set_tuning(**tuning)
 
     def plain(rep):
         segs = 0
         for j, cam, acc, img in zip(jobs, cams, acc_plain, img_plain):
-            wf.render(scenes[(j["n"], j["scene_seed"])], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
+            wf.render(scenes[j["key"]], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
                       max_depth=j["depth"], reset=True, image8=img)
         return segs
 
     def batched(rep):
         for j, cam, acc, img in zip(jobs, cams, acc_batch, img_batch):
-            b.submit(scenes[(j["n"], j["scene_seed"])], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
+            b.submit(scenes[j["key"]], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
                      max_depth=j["depth"], reset=True, image8=img)
         b.run()
         done = b.collect()
@@ -198,11 +201,12 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
     b_ms, b_wall = timed(batched)
     segs = (b.stats()["segments"] - seg0) // 2
     p_ms, p_wall = timed(plain)
-    same = all(torch.equal(acc_plain[i], acc_batch[i]) for i in range(min(check_jobs, len(jobs))))
     same_all = all(torch.equal(acc_plain[i], acc_batch[i]) for i in range(len(jobs)))
+    desc = (f"{len(jobs)} RTIOW scenes (seeds 0..{len(jobs) - 1}), 256x144, 4 spp, depth 50" if small else
+            f"{n_jobs} scenes, spheres log-uniform 100..200000, resolutions {{256x256, 512x512, 640x360, "
+            f"1024x1024}}, spp {{4, 16, 64}}, depth 50 (seeded)")
     return {
-        "workload": f"{n_jobs} scenes, spheres log-uniform 100..200000, resolutions {{256x256, 512x512, "
-                    f"640x360, 1024x1024}}, spp {{4, 16, 64}}, depth 50 (seeded)",
+        "workload": desc,
         "paths": workloads.paths(jobs), "segments": int(segs),
         "plain": {"value": segs / (p_ms / 1000), "ms": p_ms, "wall_ms": p_wall,
                   "method": "venu_render per job, in sequence"},
@@ -213,7 +217,7 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, check_jobs=4):
     }
 
 
-def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30):
+def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=4 << 20, iters=64):
     """Serving: a Poisson request stream at ~80 % of the server's capacity;
     the render server (continuous batching, resident BVHs, 150 GB HBM budget)
     against the plain method serving the same stream one job at a time."""
@@ -221,7 +225,7 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30):
 
     from venusaur_gb300 import workloads
 
-    srv = venu.Server(budget, pool_paths=16 << 20, max_jobs=256, iterations_per_step=8)
+    srv = venu.Server(budget, pool_paths=pool_paths, max_jobs=256, iterations_per_step=iters)
     scenes = {}
 
     def spheres_of(j):
@@ -525,6 +529,7 @@ def main():
     }
     if not args.no_batched and world == 1:
         line["batched"] = run_batched(venu, torch, tuning, max_paths)
+        line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True)
         line["served"] = run_served(venu, torch, tuning)
     if not args.no_cpu:
         from oracle import pyoracle

@@ -276,8 +276,11 @@ VENU_API uint64_t venu_batch_job_bytes(uint32_t width, uint32_t height, uint32_t
  * job is collected.  VENU_ERR_TOO_LARGE when max_jobs are admitted. */
 VENU_API venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id);
 /* Runs the shared path loop for at most max_iterations iterations (0 = until
- * every admitted job has finished) as one graph launch on `stream`. */
-VENU_API venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, void* stream);
+ * every admitted job has finished) as one graph launch on `stream`; with
+ * VENU_RUN_STOP_ON_FINISH the loop also ends after the iteration in which a
+ * job's last path finished, so a server can hand results out at once. */
+#define VENU_RUN_STOP_ON_FINISH 1u
+VENU_API venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, uint32_t flags, void* stream);
 /* Waits for `stream`, then accumulates, resolves and releases every finished
  * job; writes their ids (up to cap) and the count. */
 VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* finished_ids, uint32_t cap,

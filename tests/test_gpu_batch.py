@@ -116,3 +116,23 @@ def test_batch_limits(venu, oracle, cuda):
         venu.Batch(pool_paths=1000, max_jobs=0)
     b.run()
     assert len(b.collect()) == 1
+
+
+def test_batch_stop_on_finish(venu, oracle, cuda):
+    """Each run with stop_on_finish ends right after some job completes; the
+    jobs are handed out one run at a time and stay exact."""
+    torch = cuda
+    b = venu.Batch(pool_paths=600, max_jobs=8)
+    sub = _submit_all(venu, torch, b, oracle, _jobs(oracle))
+    got = []
+    for _ in range(64):
+        b.run(max_iterations=0, stop_on_finish=True)
+        fin = b.collect()
+        assert fin, "a run with stop_on_finish returned without finishing a job"
+        got += fin
+        if len(got) == len(sub):
+            break
+    assert sorted(got) == sorted(s["id"] for s in sub)
+    torch.cuda.synchronize()
+    for s in sub:
+        assert np.array_equal(s["acc"].cpu().numpy().view(np.uint32), s["want"]["accum"].view(np.uint32))

@@ -99,6 +99,7 @@ class ServerStats(C.Structure):
 
 
 BATCH_NO_GRAPH = 1
+RUN_STOP_ON_FINISH = 1
 INJECT_ALLOC = 1
 INJECT_SCENE = 2
 
@@ -148,7 +149,7 @@ def lib() -> C.CDLL:
     L.venu_batch_job_bytes.restype = C.c_uint64
     L.venu_batch_job_bytes.argtypes = [u32, u32, u32]
     L.venu_batch_submit.argtypes = [vp, C.POINTER(JobDesc), vp, C.POINTER(u32)]
-    L.venu_batch_run.argtypes = [vp, u32, vp]
+    L.venu_batch_run.argtypes = [vp, u32, u32, vp]
     L.venu_batch_collect.argtypes = [vp, vp, vp, u32, C.POINTER(u32)]
     L.venu_batch_stats_get.argtypes = [vp, C.POINTER(BatchStats)]
     L.venu_batch_destroy.argtypes = [vp]

@@ -472,8 +472,9 @@ class Batch:
         check(lib().venu_batch_submit(self.handle, C.byref(d), _stream_handle(stream), C.byref(jid)))
         return int(jid.value)
 
-    def run(self, max_iterations: int = 0, stream=None) -> None:
-        check(lib().venu_batch_run(self.handle, max_iterations, _stream_handle(stream)))
+    def run(self, max_iterations: int = 0, stop_on_finish: bool = False, stream=None) -> None:
+        flags = _lib.RUN_STOP_ON_FINISH if stop_on_finish else 0
+        check(lib().venu_batch_run(self.handle, max_iterations, flags, _stream_handle(stream)))
 
     def collect(self, stream=None) -> list:
         ids = (C.c_uint32 * self.max_jobs)()

@@ -40,12 +40,13 @@ struct DevJob {
 
 struct LoopCtl {  // device-owned loop state
     uint32_t cnt[2], work[2];
-    uint32_t iter, running, more_gen, take_total, out_base, plan_n, err, pad;
+    uint32_t iter, running, more_gen, take_total, out_base, plan_n, err;
+    uint32_t job_finished;  // set when a job's last path finishes (reset per run)
     unsigned long long segments, paths_done, iterations;
 };
 
 struct RunCtl {  // host-written before each run
-    uint32_t max_iter, nactive;
+    uint32_t max_iter, nactive, stop_on_finish, pad;
 };
 
 struct CollectEntry {
@@ -173,7 +174,10 @@ __global__ void __launch_bounds__(256) k_trace_shade_multi(const DevJob* __restr
         const bool fin = valid && !r.cont;
         const uint32_t key = fin ? job : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
-        if (fin && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&job_done[job], (unsigned long long)__popc(peers));
+        if (fin && lane == (uint32_t)(__ffs(peers) - 1)) {
+            const unsigned long long add = (unsigned long long)__popc(peers);
+            if (atomicAdd(&job_done[job], add) + add == jobs[job].total) atomicExch(&ctl->job_finished, 1u);
+        }
         finished += __popc(__ballot_sync(0xffffffffu, fin));
     }
     if (lane == 0 && finished) atomicAdd(&ctl->paths_done, (unsigned long long)finished);
@@ -188,6 +192,7 @@ __global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, cudaGr
     ctl->iterations += 2u;
     uint32_t more = (ctl->cnt[0] > 0u || ctl->more_gen) ? 1u : 0u;
     if (run->max_iter && it >= run->max_iter) more = 0u;
+    if (run->stop_on_finish && ctl->job_finished) more = 0u;  // hand finished jobs to the host now
     ctl->running = more;
     if (use_handle) cudaGraphSetConditional(handle, more);
 }
@@ -494,7 +499,7 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     return VENU_OK;
 }
 
-extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, void* stream) {
+extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, uint32_t flags, void* stream) {
     if (!b) {
         set_error("venu_batch_run: NULL batch");
         return VENU_ERR_INVALID;
@@ -503,8 +508,11 @@ extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, vo
     RunCtl rc;
     rc.max_iter = max_iterations;
     rc.nactive = (uint32_t)b->order.size();
+    rc.stop_on_finish = (flags & VENU_RUN_STOP_ON_FINISH) ? 1u : 0u;
+    rc.pad = 0;
     VENU_CUDA(cudaMemcpyAsync(b->d_run, &rc, sizeof(rc), cudaMemcpyHostToDevice, st));
     VENU_CUDA(cudaMemsetAsync(&b->d_ctl->iter, 0, sizeof(uint32_t), st));
+    VENU_CUDA(cudaMemsetAsync(&b->d_ctl->job_finished, 0, sizeof(uint32_t), st));
     if (b->flags & VENU_BATCH_NO_GRAPH) {
         // host-driven loop: one body, then read the device's running flag
         for (;;) {

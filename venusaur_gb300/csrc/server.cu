@@ -280,7 +280,7 @@ void server_loop(venu_server* s) {
             continue;
         }
         const Clock::time_point tb = Clock::now();
-        venu_status rs = venu_batch_run(s->batch, s->iters, s->st);
+        venu_status rs = venu_batch_run(s->batch, s->iters, VENU_RUN_STOP_ON_FINISH, s->st);
         uint32_t nfin = 0;
         if (rs == VENU_OK) rs = venu_batch_collect(s->batch, s->st, fin.data(), (uint32_t)fin.size(), &nfin);
         if (rs != VENU_OK) {

@@ -57,5 +57,12 @@ def serving_jobs(n_jobs: int, rate_per_s: float, seed: int = 1, nmin: int = 100,
     return jobs
 
 
+def small_jobs(n_jobs: int = 128, W: int = 256, H: int = 144, spp: int = 4, depth: int = 50):
+    """Many small renders of RTIOW scenes (seeds 0..n_jobs-1): the regime where
+    one render per launch sequence leaves the GPU mostly idle."""
+    return [dict(rtiow_seed=i, W=W, H=H, spp=spp, depth=depth, eye=(13.0, 2.0, 3.0), subframe=1)
+            for i in range(n_jobs)]
+
+
 def paths(jobs) -> int:
     return sum(j["W"] * j["H"] * j["spp"] for j in jobs)
