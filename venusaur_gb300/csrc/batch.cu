@@ -135,8 +135,8 @@ __global__ void __launch_bounds__(256) k_trace_shade_multi(const DevJob* __restr
                                                            Queue qin, Queue qout, int in) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
-    sm.pair = reinterpret_cast<int2*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const int out = 1 - in;
     const uint32_t n = ctl->cnt[in];
     const uint32_t lane = threadIdx.x & 31;

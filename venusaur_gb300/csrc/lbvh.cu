@@ -348,11 +348,42 @@ __global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* __re
     meta[k] = id | (type << 30);
 }
 
+// Traversal layout: internal node p becomes one 64-byte record holding both
+// children, child c in float4s 4p+2c and 4p+2c+1:
+//   internal child q: {lo.xyz, q}, {hi.xyz, 0}   (q's box from nodes)
+//   leaf child:       {center, word}, {radius, 0, 0, 0}   (word keeps the
+//                     leaf and hoisted flags; the sphere is inlined)
+// A step of the traversal then reads one record instead of two boxes or
+// spheres at two addresses.  Runs after k_hoist_finalize, so the flags are
+// final; the canonical nodes array stays the exported form.
+__global__ void k_trav_layout(const float4* __restrict__ nodes, const float4* __restrict__ sph, uint32_t n,
+                              float4* __restrict__ trav) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2u * (n - 1u)) return;
+    const uint32_t p = i >> 1, c = i & 1u;
+    const int32_t w = __float_as_int(nodes[2 * p + c].w);
+    float4 a, b;
+    if (w & kLeaf) {
+        const uint32_t k = (uint32_t)(w & kSlotMask);
+        const float4 s4 = k < n ? sph[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a = make_float4(s4.x, s4.y, s4.z, __int_as_float(w));
+        b = make_float4(s4.w, 0.0f, 0.0f, 0.0f);
+    } else {
+        const uint32_t q = (uint32_t)w < n - 1u ? (uint32_t)w : 0u;
+        const float4 lo = nodes[2 * q], hi = nodes[2 * q + 1];
+        a = make_float4(lo.x, lo.y, lo.z, __int_as_float(w));
+        b = make_float4(hi.x, hi.y, hi.z, 0.0f);
+    }
+    trav[4 * (size_t)p + 2 * c] = a;
+    trav[4 * (size_t)p + 2 * c + 1] = b;
+}
+
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
-// Device buffers of one LBVH build: outputs and scratch.
+// Device buffers of one LBVH build: outputs and scratch.  trav may be null
+// (the build then stops at the canonical layout).
 struct LbvhBuffers {
-    float4 *nodes, *sph, *mat;
+    float4 *nodes, *trav, *sph, *mat;
     uint32_t *meta, *keys;
     LbvhCtl* ctl;
     uint32_t *keys_alt, *vals, *vals_alt, *hist, *arrive;
@@ -391,6 +422,7 @@ cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const
     if (n > 1) {
         k_hoist_collect<<<cdiv(n, 256), 256, 0, st>>>(B.sph, n, B.ctl);
         k_hoist_finalize<<<1, 32, 0, st>>>(B.ctl, B.pleaf, B.nodes, n);
+        if (B.trav) k_trav_layout<<<cdiv(2 * (n - 1), 256), 256, 0, st>>>(B.nodes, B.sph, n, B.trav);
     }
     return cudaGetLastError();
 }
@@ -400,11 +432,12 @@ cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const
 void free_scene(venu_scene* s) {
     if (!s) return;
     cudaFree(s->nodes);
+    cudaFree(s->trav);
     cudaFree(s->sph);
     cudaFree(s->mat);
     cudaFree(s->meta);
     cudaFree(s->keys);
-    s->nodes = nullptr;
+    s->nodes = s->trav = nullptr;
     s->sph = s->mat = nullptr;
     s->meta = s->keys = nullptr;
 }
@@ -425,6 +458,7 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     };
     const uint32_t nint = n > 1 ? n - 1 : 1;
     VENU_CUDA(alloc((void**)&S->nodes, sizeof(float4) * 2 * nint));
+    VENU_CUDA(alloc((void**)&S->trav, sizeof(float4) * 4 * nint));
     VENU_CUDA(alloc((void**)&S->sph, sizeof(float4) * n));
     VENU_CUDA(alloc((void**)&S->mat, sizeof(float4) * n));
     VENU_CUDA(alloc((void**)&S->meta, sizeof(uint32_t) * n));
@@ -432,6 +466,7 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     S->bytes = bytes;
     LbvhBuffers B{};
     B.nodes = S->nodes;
+    B.trav = S->trav;
     B.sph = S->sph;
     B.mat = S->mat;
     B.meta = S->meta;

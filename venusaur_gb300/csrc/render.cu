@@ -50,8 +50,8 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
                                                   unsigned long long* __restrict__ stats) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
-    sm.pair = reinterpret_cast<int2*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const uint32_t n = *cnt;
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
@@ -96,8 +96,8 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                                                       unsigned long long* __restrict__ stats, uint32_t refill_min) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
-    sm.pair = reinterpret_cast<int2*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const uint32_t n = *cnt;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = (1u << lane) - 1u;
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     TraceCounters K{0, 0};
     bool overflow = false;
     Tracer<COUNT> T;
-    int2 spill[kSpill];
+    int spill[kSpill];
     float spill_tn[kSpill];
     uint32_t ray = 0;
     bool active = false, exhausted = false;
@@ -169,8 +169,8 @@ __global__ void __launch_bounds__(256) k_trace_shade(SceneView S, Queue qin, con
                                                      unsigned long long* __restrict__ stats) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
-    sm.pair = reinterpret_cast<int2*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const uint32_t n = *cnt_in;
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
@@ -280,8 +280,8 @@ __global__ void __launch_bounds__(128) k_trace_rays(SceneView S, const float* __
                                                     uint32_t* __restrict__ err) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
-    sm.pair = reinterpret_cast<int2*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int2) * kShared * blockDim.x);
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     f3 o = mk(rays[6 * (size_t)i], rays[6 * (size_t)i + 1], rays[6 * (size_t)i + 2]);
@@ -312,13 +312,14 @@ SceneView view_of(const venu_scene* s) {
     v.sph = s->sph;
     v.mat = s->mat;
     v.meta = s->meta;
+    v.trav = s->trav;
     v.n = s->n;
     v.nhoist = s->nhoist;
     for (int i = 0; i < kMaxHoisted; ++i) v.hoist[i] = s->hoist[i];
     return v;
 }
 
-size_t traverse_smem(int block) { return (size_t)block * kShared * (sizeof(int2) + sizeof(float)); }
+size_t traverse_smem(int block) { return (size_t)block * kShared * (sizeof(int) + sizeof(float)); }
 
 }  // namespace venu
 

@@ -148,6 +148,7 @@ constexpr int kMaxHoisted = 4;
 
 struct SceneView {
     const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
+    const float4* __restrict__ trav;   // 4 float4 per internal node: both children, see lbvh.cu
     const float4* __restrict__ sph;    // {center, radius} per slot
     const float4* __restrict__ mat;    // {albedo, fuzz or ir} per slot
     const uint32_t* __restrict__ meta; // original id | material << 30
@@ -290,10 +291,11 @@ __device__ __forceinline__ bool sphere_test(const RayPre& R, float4 S, float tmi
 // ---------------------------------------------------------------------------
 // Closest-hit traversal of the binary LBVH.
 //
-// Children are tested at their parent: internal children by their box (two
-// float4 loads each), leaf children directly by the sphere (one float4).
-// The nearer hit child is descended; the farther one's child pair and entry
-// distance go on a per-thread stack whose top kShared entries live in shared
+// Children are tested at their parent, from the parent's 64-byte record in
+// the traversal layout (one contiguous 4 x float4 load): internal children by
+// their box, leaf children directly by their sphere, stored inline.  The
+// nearer hit child is descended; the farther one's index and entry distance
+// go on a per-thread stack whose top kShared entries live in shared
 // memory (ring buffer, layout [entry][thread] so a warp touches 32 distinct
 // banks) and whose older entries spill to local memory.  Ties on t go to the
 // smaller slot, so the result does not depend on traversal order.
@@ -302,7 +304,7 @@ constexpr int kShared = 16;  // shared-memory entries per thread (power of two)
 constexpr int kSpill = 64;   // local-memory entries beyond those
 
 struct StackSmem {
-    int2* pair;  // [kShared][block]
+    int* node;   // [kShared][block]
     float* tn;   // [kShared][block]
 };
 
@@ -311,21 +313,22 @@ struct TraceCounters {
 };
 
 // Per-lane traversal state.  begin() prepares a ray and tests the root;
-// step() expands one child pair (or pops); both return whether more work
-// remains.  The same state machine serves the one-ray-per-thread kernels
-// (trace_closest) and the persistent kernels that refill idle lanes.
+// step() tests both children of the current node (from its 64-byte record in
+// the traversal layout: boxes of internal children, spheres of leaf children
+// inline) and descends or pops; both return whether more work remains.  The
+// same state machine serves the one-ray-per-thread kernels (trace_closest)
+// and the persistent kernels that refill idle lanes.
 template <bool COUNT>
 struct Tracer {
     RayPre R;
     float tmin, tmax, best_t;
-    int32_t best, pl, pr;
+    int32_t best, cur;
     int sp;
     uint32_t guard;
 
-    __device__ __forceinline__ void leaf(const SceneView& S, int32_t k, TraceCounters& K) {
+    __device__ __forceinline__ void leaf(int32_t k, float4 s4, TraceCounters& K) {
         float t;
         if (COUNT) ++K.spheres;
-        float4 s4 = __ldg(S.sph + k);
         if (sphere_test(R, s4, tmin, tmax, t) && (t < best_t || (t == best_t && k < best))) {
             best_t = t;
             best = k;
@@ -345,20 +348,19 @@ struct Tracer {
         // Huge spheres (the ground) are tested by every ray up front, with the
         // whole warp converged; their leaves are skipped during traversal and
         // their hit distance already culls boxes behind them.
-        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S, S.hoist[h], K);
+        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
         if (n == 1) {
-            leaf(S, 0, K);
+            leaf(0, __ldg(S.sph), K);
             return false;
         }
         float tn;
         float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
         if (COUNT) ++K.nodes;
         if (!box_test(R, rlo, rhi, tmin, best_t, tn)) return false;
-        pl = __float_as_int(rlo.w);
-        pr = __float_as_int(rhi.w);
-        // A tree has n-1 internal nodes and each step expands the child pair
-        // of a different one; the guard and the index checks turn a corrupt
-        // tree into an error flag instead of a hang.
+        cur = 0;
+        // A tree has n-1 internal nodes and each step expands a different one;
+        // the guard and the index checks turn a corrupt tree into an error
+        // flag instead of a hang.
         guard = 2u * n + 8u;
         return true;
     }
@@ -366,47 +368,44 @@ struct Tracer {
     // spill / spill_tn: this thread's local-memory stack entries beyond the
     // kShared in shared memory.
     __device__ __forceinline__ bool step(const SceneView& S, StackSmem sm, uint32_t tid, uint32_t bdim,
-                                         int2* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
+                                         int* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
         const uint32_t n = S.n;
-        if (--guard == 0u || (!(pl & kLeaf) && (uint32_t)pl >= n - 1u) || (!(pr & kLeaf) && (uint32_t)pr >= n - 1u) ||
-            (uint32_t)(pl & kSlotMask) >= n || (uint32_t)(pr & kSlotMask) >= n) {
+        if (--guard == 0u || (uint32_t)cur >= n - 1u) {
+            overflow = true;
+            return false;
+        }
+        const float4* T = S.trav + 4 * (size_t)cur;
+        const float4 a0 = __ldg(T), b0 = __ldg(T + 1), a1 = __ldg(T + 2), b1 = __ldg(T + 3);
+        const int32_t w0 = __float_as_int(a0.w), w1 = __float_as_int(a1.w);
+        if (((w0 & kLeaf) && (uint32_t)(w0 & kSlotMask) >= n) || ((w1 & kLeaf) && (uint32_t)(w1 & kSlotMask) >= n)) {
             overflow = true;
             return false;
         }
         bool h0 = false, h1 = false;
         float tn0 = 0.0f, tn1 = 0.0f;
-        int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
-        if (pl & kLeaf) {
-            if (!(pl & kHoisted)) leaf(S, pl & kSlotMask, K);
+        if (w0 & kLeaf) {
+            if (!(w0 & kHoisted)) leaf(w0 & kSlotMask, make_float4(a0.x, a0.y, a0.z, b0.x), K);
         } else {
-            float4 lo = __ldg(S.nodes + 2 * pl), hi = __ldg(S.nodes + 2 * pl + 1);
             if (COUNT) ++K.nodes;
-            h0 = box_test(R, lo, hi, tmin, best_t, tn0);
-            c0l = __float_as_int(lo.w);
-            c0r = __float_as_int(hi.w);
+            h0 = box_test(R, a0, b0, tmin, best_t, tn0);
         }
-        if (pr & kLeaf) {
-            if (!(pr & kHoisted)) leaf(S, pr & kSlotMask, K);
+        if (w1 & kLeaf) {
+            if (!(w1 & kHoisted)) leaf(w1 & kSlotMask, make_float4(a1.x, a1.y, a1.z, b1.x), K);
         } else {
-            float4 lo = __ldg(S.nodes + 2 * pr), hi = __ldg(S.nodes + 2 * pr + 1);
             if (COUNT) ++K.nodes;
-            h1 = box_test(R, lo, hi, tmin, best_t, tn1);
-            c1l = __float_as_int(lo.w);
-            c1r = __float_as_int(hi.w);
+            h1 = box_test(R, a1, b1, tmin, best_t, tn1);
         }
         if (h0 && h1) {
-            int2 far;
+            int32_t far;
             float far_tn;
             if (tn1 < tn0) {
-                far = make_int2(c0l, c0r);
+                far = w0;
                 far_tn = tn0;
-                pl = c1l;
-                pr = c1r;
+                cur = w1;
             } else {
-                far = make_int2(c1l, c1r);
+                far = w1;
                 far_tn = tn1;
-                pl = c0l;
-                pr = c0r;
+                cur = w0;
             }
             const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
             if (sp >= kShared) {
@@ -415,36 +414,33 @@ struct Tracer {
                     overflow = true;
                     return false;
                 }
-                spill[g] = sm.pair[j];
+                spill[g] = sm.node[j];
                 spill_tn[g] = sm.tn[j];
             }
-            sm.pair[j] = far;
+            sm.node[j] = far;
             sm.tn[j] = far_tn;
             ++sp;
             return true;
         }
         if (h0) {
-            pl = c0l;
-            pr = c0r;
+            cur = w0;
             return true;
         }
         if (h1) {
-            pl = c1l;
-            pr = c1r;
+            cur = w1;
             return true;
         }
         while (sp > 0) {
             --sp;
             const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
-            int2 e = sm.pair[j];
-            float etn = sm.tn[j];
+            const int32_t e = sm.node[j];
+            const float etn = sm.tn[j];
             if (sp >= kShared) {
-                sm.pair[j] = spill[sp - kShared];
+                sm.node[j] = spill[sp - kShared];
                 sm.tn[j] = spill_tn[sp - kShared];
             }
             if (etn <= best_t) {
-                pl = e.x;
-                pr = e.y;
+                cur = e;
                 return true;
             }
         }
@@ -467,7 +463,7 @@ __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPr
                                                  uint32_t tid, uint32_t bdim, bool& overflow,
                                                  TraceCounters& K) {
     Tracer<COUNT> T;
-    int2 spill[kSpill];
+    int spill[kSpill];
     float spill_tn[kSpill];
     if (T.begin(S, R.o, R.d, tmin, tmax, K))
         while (T.step(S, sm, tid, bdim, spill, spill_tn, overflow, K)) {

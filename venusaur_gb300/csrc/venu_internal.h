@@ -27,6 +27,7 @@ int sm_count();
 struct venu_scene {
     uint32_t n = 0;
     float4* nodes = nullptr;   // 2 per internal node
+    float4* trav = nullptr;    // 4 per internal node: both children (traversal layout)
     float4* sph = nullptr;     // slot order
     float4* mat = nullptr;
     uint32_t* meta = nullptr;  // original id | material << 30
