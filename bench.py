@@ -217,10 +217,12 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
     }
 
 
-def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=4 << 20, iters=64):
+def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=16 << 20, iters=64):
     """Serving: a Poisson request stream at ~80 % of the server's capacity;
-    the render server (continuous batching, resident BVHs, 150 GB HBM budget)
-    against the plain method serving the same stream one job at a time."""
+    the render server (continuous batching, resident BVHs, 150 GB HBM budget;
+    FIFO and shortest-first plan order) against the plain method serving the
+    same stream one job at a time.  All scenes are resident before the
+    streams start, for every method."""
     import threading
 
     from venusaur_gb300 import workloads
@@ -228,24 +230,31 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     srv = venu.Server(budget, pool_paths=pool_paths, max_jobs=256, iterations_per_step=iters)
     scenes = {}
 
+    def skey(j):
+        return (j["scene_seed"], j["n"])
+
     def spheres_of(j):
-        if j["scene_seed"] not in scenes:
-            scenes[j["scene_seed"]] = venu.generate_random(j["n"], j["scene_seed"])
-        return scenes[j["scene_seed"]]
+        if skey(j) not in scenes:
+            scenes[skey(j)] = venu.generate_random(j["n"], j["scene_seed"])
+        return scenes[skey(j)]
 
     def cam_of(j):
         return venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
 
-    sent = set()
+    keys = {}
 
     def submit(j):
-        key = 1 + j["scene_seed"]
-        sp = None if key in sent else spheres_of(j)
-        sent.add(key)
-        return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=sp, scene_key=key, max_depth=j["depth"])
+        k = keys.get(skey(j))
+        if k is None:
+            k = keys[skey(j)] = 1 + len(keys)
+            return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=spheres_of(j), scene_key=k,
+                              max_depth=j["depth"])
+        return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], scene_key=k, max_depth=j["depth"])
 
-    # capacity: a burst of requests all at once
+    # capacity: a burst of requests all at once (FIFO)
     calib = workloads.serving_jobs(24, rate_per_s=1.0, seed=2)
+    for j in calib:  # scenes resident first
+        srv.wait(submit(dict(j, W=16, H=16, spp=1)))
     t0 = time.perf_counter()
     ids = [submit(j) for j in calib]
     for i in ids:
@@ -254,35 +263,42 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     lam = util * cap_jobs_per_s
     jobs = workloads.serving_jobs(n_requests, rate_per_s=lam, seed=3)
     for j in jobs:
-        spheres_of(j)
-    seg0 = srv.stats()["segments"]
-    ids = [None] * len(jobs)
-    start = time.perf_counter()
+        srv.wait(submit(dict(j, W=16, H=16, spp=1)))
 
-    def client():
-        for k, j in enumerate(jobs):
-            dt = start + j["arrival"] - time.perf_counter()
-            if dt > 0:
-                time.sleep(dt)
-            ids[k] = submit(j)
+    def stream():
+        seg0 = srv.stats()["segments"]
+        ids = [None] * len(jobs)
+        start = time.perf_counter()
 
-    th = threading.Thread(target=client)
-    th.start()
-    th.join()
-    res = [srv.wait(i) for i in ids]
-    makespan = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
-    lat = np.array([r["latency_ms"] for r in res])
-    st = srv.stats()
-    segs = st["segments"] - seg0
+        def client():
+            for k, j in enumerate(jobs):
+                dt = start + j["arrival"] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ids[k] = submit(j)
+
+        th = threading.Thread(target=client)
+        th.start()
+        th.join()
+        res = [srv.wait(i) for i in ids]
+        makespan = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+        lat = np.array([r["latency_ms"] for r in res])
+        segs = srv.stats()["segments"] - seg0
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "value": segs / makespan, "unit": UNIT, "makespan_s": makespan,
+                "failed": int(sum(r["status"] != 0 for r in res))}, segs
+
+    out = {}
+    for name, sf in (("server_fifo", False), ("server_shortest_first", True)):
+        srv.set_policy(sf)
+        out[name], segs = stream()
     srv.close()
-    served = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-              "value": segs / makespan, "unit": UNIT, "makespan_s": makespan, "failed": int(st["failed"])}
 
     # the plain method: one job at a time, same arrivals, resident BVHs
     wf = venu.Wavefront(16 << 20)
     if tuning:
         wf.set_tuning(**tuning)
-    dscenes = {}
+    dscenes = {k: venu.DeviceScene(v) for k, v in scenes.items()}
     plain_lat = []
     start = time.perf_counter()
     tfree = 0.0
@@ -290,27 +306,23 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
         now = time.perf_counter() - start
         if now < j["arrival"]:
             time.sleep(j["arrival"] - now)
-        if j["scene_seed"] not in dscenes:
-            dscenes[j["scene_seed"]] = venu.DeviceScene(spheres_of(j))
         acc = venu.new_accum(j["W"], j["H"])
         img = torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda")
-        wf.render(dscenes[j["scene_seed"]], cam_of(j), j["W"], j["H"], j["spp"], acc, subframe=1,
+        wf.render(dscenes[skey(j)], cam_of(j), j["W"], j["H"], j["spp"], acc, subframe=1,
                   max_depth=j["depth"], reset=True, image8=img)
         img.cpu()
         tfree = time.perf_counter() - start
         plain_lat.append(1000.0 * (tfree - j["arrival"]))
     plat = np.array(plain_lat)
     plain_makespan = tfree - jobs[0]["arrival"]
-    return {
-        "workload": f"{n_requests} requests, Poisson arrivals at {lam:.2f}/s (~{int(100 * util)} % of the "
-                    f"server's measured capacity {cap_jobs_per_s:.2f} jobs/s), scenes from 16 resident scenes with "
-                    "100..200000 spheres, resolutions {256x256, 512x512, 640x360, 1024x1024}, spp "
-                    "{8, 16, 32, 64, 128}, depth 50, HBM budget 150 GB",
-        "served": served,
-        "plain": {"p50_ms": float(np.percentile(plat, 50)), "p99_ms": float(np.percentile(plat, 99)),
-                  "value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
-                  "method": "venu_render one job at a time (FIFO), same arrivals"},
-    }
+    out["plain"] = {"p50_ms": float(np.percentile(plat, 50)), "p99_ms": float(np.percentile(plat, 99)),
+                    "value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
+                    "method": "venu_render one job at a time (FIFO), same arrivals"}
+    out["workload"] = (f"{n_requests} requests, Poisson arrivals at {lam:.2f}/s (~{int(100 * util)} % of the "
+                       f"server's measured capacity {cap_jobs_per_s:.2f} jobs/s), scenes from 16 resident scenes "
+                       "with 100..200000 spheres, resolutions {256x256, 512x512, 640x360, 1024x1024}, spp "
+                       f"{{8, 16, 32, 64, 128}}, depth 50, HBM budget 150 GB, pool {pool_paths >> 20} Mi paths")
+    return out
 
 
 def run_reference(args, cfg, world, rank):
@@ -351,11 +363,15 @@ def main():
     ap.add_argument("--impl", default="venu", choices=["venu", "reference"])
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
     ap.add_argument("--max-paths", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0, help="override the config's samples per pixel (small profiling cases)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
     args = ap.parse_args()
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.spp:
+        cfg["spp"] = args.spp
+        cfg["workload"] = cfg["workload"].replace(f"{CONFIGS[args.config]['spp']} spp", f"{args.spp} spp")
     from venusaur_gb300.replicas import Replicas
 
     rep = Replicas()
@@ -446,12 +462,14 @@ def main():
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
     segs_c, paths_c = sc["segments"], sc["paths"]
     fused = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"]) == 2
-    # Algorithmic bytes of the dominant kernel per render.  Traversal: 32 B per
-    # node record tested, 16 B per sphere tested, 32 B ray read.  Separate
-    # traversal kernel: + 8 B hit write.  Fused traverse+shade kernel: + 16 B
-    # throughput/seed read, 36 B sphere+material+meta read, 48 B continuation
-    # write per continuing segment, 16 B radiance slot per finished path.
-    trav_bytes = nodes * 32 + sph * 16 + segs_c * 32
+    # Algorithmic bytes of the dominant kernel per render.  Traversal: each
+    # step reads one 64-byte record holding both children of a node (box or
+    # inline sphere each), i.e. 32 B per child tested, box or sphere; 32 B ray
+    # read.  Separate traversal kernel: + 8 B hit write.  Fused
+    # traverse+shade kernel: + 16 B throughput/seed read, 36 B
+    # sphere+material+meta read, 48 B continuation write per continuing
+    # segment, 16 B radiance slot per finished path.
+    trav_bytes = (nodes + sph) * 32 + segs_c * 32
     if fused:
         kernel = "k_trace_shade"
         kbytes = trav_bytes + segs_c * (16 + 36) + (segs_c - paths_c) * 48 + paths_c * 16
@@ -462,18 +480,29 @@ def main():
     avg_launch_ms = st["traverse_ms"] / max(1, st["traverse_launches"])
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
-    # FP32 view (SURVEY-style per-segment estimate): 20 flop per box, 25 per
-    # sphere, 60 per shade; peak = 152 SMs x 128 lanes x 2 x max SM clock
+    # FP32 view (per-segment estimate): 20 flop per box, 25 per sphere, 60
+    # per shade; peak = 152 SMs x 128 lanes x 2 x max SM clock
     kflops = nodes * 20 + sph * 25 + (segs_c * 60 if fused else 0)
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
+    # DRAM traffic per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum
+    # per segment from a capture of the same kernel on a smaller case of the
+    # same scene (the queue traffic, which grows in proportion to the rays;
+    # the node set stays cache-resident), scaled to this launch's segments.
+    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.3 B) and
+    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (86.7 B).
+    # (c1's queues fit in L2: no figure for it.)
+    dram_per_seg = {"c2": 86.3, "c3": 86.7}.get(args.config) if fused else None
+    traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"]) if dram_per_seg else None
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-        "peak_kind": peak_kind, "traffic": None, "kernel": kernel,
+        "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel,
+        "traffic_per_segment": dram_per_seg,
         "bytes_per_segment": kbytes / max(1, segs_c),
         "nodes_per_segment": nodes / max(1, segs_c), "spheres_per_segment": sph / max(1, segs_c),
         "kernel_share": st["traverse_ms"] / max(1e-9, ms / args.steps),
-        "note": "algorithmic bytes; the node set of this scene is L1/L2-resident, so DRAM carries "
-                "only the ray queues and the kernel is issue-bound (see profiles/)",
+        "note": "achieved = algorithmic bytes (nodes, spheres, queues) per launch / event time; the node set "
+                "is L1/L2-resident, so DRAM carries only the ray queues (traffic, from ncu) and the kernel "
+                "is issue-bound on the ALU pipe (profiles/)",
         "fp32_tflops": kflops / (st["traverse_ms"] / 1000.0) / 1e12, "fp32_peak_tflops": fp32_peak,
     }
 

@@ -140,6 +140,19 @@ VENU_API void venu_camera_look_at(const float eye[3], const float lookat[3], flo
 /* Camera::UpdateUVW (Core/Camera.cpp:27-37) for a unit forward vector. */
 VENU_API void venu_camera_frame(const float eye[3], const float forward[3], float vfov_deg, float aspect,
                        float aperture, float focal, venu_camera* out);
+/* Camera::Pitch / Yaw / Roll (Core/camera.h:56-78): the unit forward vector
+ * rotated by `degrees` about `axis` (the camera's u, v or w) with GLM's
+ * quaternion semantics (forward * rotate(identity, radians(degrees), axis)),
+ * then normalised.  Host only; out may alias forward. */
+VENU_API void venu_camera_rotate(const float forward[3], const float axis[3], float degrees, float out[3]);
+
+/* ---- image files: the headless stand-in for the GL display
+ *      (Core/CUDAOutputBuffer.h:284-339, Core/Core.cpp:396-426).  Host
+ *      buffers in the renderer's pixel order (row 0 = bottom). ------------- */
+/* Binary PPM (P6), top row first, alpha dropped. */
+VENU_API venu_status venu_image_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height);
+/* PFM (RGB float32, little-endian, bottom row first), alpha dropped. */
+VENU_API venu_status venu_image_write_pfm(const char* path, const float* rgba32f, uint32_t width, uint32_t height);
 
 /* ---- scene: LBVH build (replaces Renderer::BuildAccelerationStructures,
  *      Core/Renderer.h:160-255, and CreateSBT's per-sphere records,
@@ -151,6 +164,19 @@ VENU_API venu_status venu_scene_create(const venu_sphere* spheres_host, uint32_t
 /* Same, from spheres already in device memory. */
 VENU_API venu_status venu_scene_create_device(const venu_sphere* spheres_dev, uint32_t n, void* stream,
                                      venu_scene** out);
+/* Moving spheres (no counterpart in the reference, which builds once in
+ * Renderer::Init, Core/Renderer.h:25-33): the scene's spheres replaced by `n` new ones (the same count and original order as at
+ * creation; centres, radii and materials may change) and the LBVH refit --
+ * same topology and slot order, boxes recomputed bottom-up -- instead of
+ * rebuilt.  Renders afterwards equal renders of a fresh build of the new
+ * spheres (the closest hit does not depend on the tree; ties between equal
+ * distances aside).  Quality degrades as spheres move far from where the
+ * tree was built: rebuild with venu_scene_create then.  The host variant
+ * uploads and returns when done; the device variant is asynchronous on
+ * `stream` and `spheres_dev` must stay valid until it completes. */
+VENU_API venu_status venu_scene_update(venu_scene* scene, const venu_sphere* spheres_host, uint32_t n, void* stream);
+VENU_API venu_status venu_scene_update_device(venu_scene* scene, const venu_sphere* spheres_dev, uint32_t n,
+                                              void* stream);
 VENU_API venu_status venu_scene_info_get(const venu_scene* scene, venu_scene_info* out);
 /* Copies the built LBVH to host buffers (any may be NULL): sorted Morton
  * codes [n], sorted original ids [n], internal nodes [(n-1) x 32 bytes:
@@ -206,7 +232,7 @@ VENU_API venu_status venu_trace(const venu_scene* scene, const float* rays_dev, 
 #define VENU_RENDERER_COUNT 1u   /* count nodes visited / spheres tested */
 #define VENU_RENDERER_PROFILE 2u /* CUDA events around every traverse / shade launch */
 
-/* max_paths: paths in flight per wave (0 = default 8 Mi). */
+/* max_paths: paths in flight per wave (0 = default 16 Mi, about 2 GB of queues). */
 VENU_API venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, venu_renderer** out);
 /* One Renderer::Draw: spp samples per pixel for every pixel, added to the
  * accumulator (VENU_ACCUM_FLOATS_PER_PIXEL floats per pixel, device), then
@@ -222,9 +248,9 @@ VENU_API venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* ou
  * autotuner, venusaur_gb300/tune.py; results do not depend on them). */
 typedef struct venu_tuning {
     uint32_t traverse_variant;       /* 0: each warp takes 32 rays and runs them to the end;
-                                        1: idle lanes take new rays (default);
+                                        1: idle lanes take new rays;
                                         2: as 0, then the warp shades its 32 hits in the same
-                                           kernel (no separate shade launch) */
+                                           kernel (no separate shade launch; default) */
     uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
@@ -285,6 +311,21 @@ VENU_API venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, uint
  * job; writes their ids (up to cap) and the count. */
 VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* finished_ids, uint32_t cap,
                                         uint32_t* count);
+/* Plan order of the admitted jobs: which job's new paths take free pool slots
+ * first.  FIFO (default): submission order.  SHORTEST_FIRST: fewest
+ * unfinished paths first (as of the last collect; ties by submission) --
+ * small jobs overtake large ones, which lowers typical latency; a steady
+ * stream of small jobs can delay a large one indefinitely.  Results do not
+ * depend on the order. */
+#define VENU_POLICY_FIFO 0u
+#define VENU_POLICY_SHORTEST_FIRST 1u
+VENU_API venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy);
+/* Sets (on != 0) or clears a flag in mapped host memory that the device loop
+ * reads once per iteration pair: while set, a running venu_batch_run ends at
+ * its next iteration boundary (and later runs after one iteration pair), so
+ * a host with new jobs can admit them without waiting for the run.  The only
+ * batch call that may be made from another host thread. */
+VENU_API venu_status venu_batch_interrupt(venu_batch* b, uint32_t on);
 VENU_API venu_status venu_batch_stats_get(venu_batch* b, venu_batch_stats* out);
 VENU_API venu_status venu_batch_destroy(venu_batch* b);
 
@@ -342,6 +383,10 @@ typedef struct venu_server_stats {
 VENU_API venu_status venu_server_create(uint64_t hbm_budget_bytes, uint32_t pool_paths, uint32_t max_jobs,
                                         uint32_t iterations_per_step, venu_server** out);
 VENU_API venu_status venu_server_submit(venu_server* s, const venu_request* req, uint64_t* request_id);
+/* Plan order of the admitted requests (VENU_POLICY_FIFO, the default, or
+ * VENU_POLICY_SHORTEST_FIRST; see venu_batch_set_policy); admission stays
+ * first come first served.  Takes effect at the server's next step. */
+VENU_API venu_status venu_server_set_policy(venu_server* s, uint32_t policy);
 /* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY). */
 VENU_API venu_status venu_server_wait(venu_server* s, uint64_t request_id, double timeout_s, venu_result* out);
 VENU_API venu_status venu_server_cancel(venu_server* s, uint64_t request_id);

@@ -122,13 +122,20 @@ class Scene {
 // Core/camera.h:9-100, Core/Camera.cpp:16-37
 class Camera {
    public:
-    Camera() = default;
+    Camera() { UpdateUVW(); }
     Camera(const vec3& origin, float vfov, float aspect, float aperture, float focalLength)
-        : m_position(origin), m_vfov(vfov), m_aspect(aspect), m_aperture(aperture), m_focalLength(focalLength) {}
+        : m_position(origin), m_vfov(vfov), m_aspect(aspect), m_aperture(aperture), m_focalLength(focalLength) {
+        UpdateUVW();
+    }
     void SetForward(vec3 d) {
-        float inv = 1.0f / std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
-        m_forward = vec3(d.x * inv, d.y * inv, d.z * inv);
+        m_forward = normalize(d);
         m_changed = true;
+    }
+    void UVWFrame(vec3& U, vec3& V, vec3& W) {
+        UpdateUVW();
+        U = m_u;
+        V = m_v;
+        W = m_w;
     }
     float GetLensRadius() const { return m_aperture * 0.5f; }
     const vec3& GetPosition() const { return m_position; }
@@ -140,10 +147,21 @@ class Camera {
         }
     }
     void MoveForward(float speed) {
-        m_position = vec3(m_position.x + m_forward.x * speed, m_position.y + m_forward.y * speed,
-                          m_position.z + m_forward.z * speed);
+        m_position = add_scaled(m_position, m_forward, speed);
         m_changed = true;
     }
+    // Core/camera.h:42-78; u/v/w are those of the last UVWFrame (or Draw).
+    void MoveRight(float speed) {
+        m_position = add_scaled(m_position, normalize(m_u), speed);
+        m_changed = true;
+    }
+    void MoveUp(float speed) {
+        m_position = add_scaled(m_position, normalize(m_v), speed);
+        m_changed = true;
+    }
+    void Pitch(float speed) { rotate(m_u, speed); }
+    void Yaw(float speed) { rotate(m_v, speed); }
+    void Roll(float speed) { rotate(m_w, speed); }
     bool Changed() {
         bool c = m_changed;
         m_changed = false;
@@ -157,10 +175,37 @@ class Camera {
         return c;
     }
 
+    // Renderer::Draw takes the frame through here, refreshing u/v/w as the
+    // reference's UVWFrame does.
+    venu_camera frame() {
+        venu_camera c = params();
+        m_u = vec3(c.u[0], c.u[1], c.u[2]);
+        m_v = vec3(c.v[0], c.v[1], c.v[2]);
+        m_w = vec3(c.w[0], c.w[1], c.w[2]);
+        return c;
+    }
+
    private:
+    static vec3 normalize(const vec3& d) {
+        float inv = 1.0f / std::sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+        return vec3(d.x * inv, d.y * inv, d.z * inv);
+    }
+    static vec3 add_scaled(const vec3& p, const vec3& d, float s) {
+        return vec3(p.x + d.x * s, p.y + d.y * s, p.z + d.z * s);
+    }
+    void UpdateUVW() { frame(); }
+    void rotate(const vec3& axis, float degrees) {
+        const float f[3] = {m_forward.x, m_forward.y, m_forward.z};
+        const float a[3] = {axis.x, axis.y, axis.z};
+        float o[3];
+        venu_camera_rotate(f, a, degrees, o);
+        m_forward = vec3(o[0], o[1], o[2]);
+        m_changed = true;
+    }
     vec3 m_position;
     vec3 m_forward{0.0f, 0.0f, -1.0f};
     float m_vfov = 45.0f, m_aspect = 1.6f, m_aperture = 0.0f, m_focalLength = 1.0f;
+    vec3 m_u, m_v, m_w;
     bool m_changed = true;
 };
 
@@ -190,6 +235,21 @@ class CUDAOutputBuffer {
         return h;
     }
     cudaStream_t stream() const { return m_stream; }
+    std::vector<float> getHostFloat() {
+        std::vector<float> h(4u * m_width * m_height);
+        cuda_check(cudaMemcpy(h.data(), m_pixels_f, h.size() * sizeof(float), cudaMemcpyDeviceToHost),
+                   "getHostFloat");
+        return h;
+    }
+    // Headless stand-ins for the GL display (Core/CUDAOutputBuffer.h:284-339).
+    void writePPM(const char* path) {
+        std::vector<uint8_t> h = getHostPointer();
+        check(venu_image_write_ppm(path, h.data(), (uint32_t)m_width, (uint32_t)m_height), "writePPM");
+    }
+    void writePFM(const char* path) {
+        std::vector<float> h = getHostFloat();
+        check(venu_image_write_pfm(path, h.data(), (uint32_t)m_width, (uint32_t)m_height), "writePFM");
+    }
 
    private:
     void release() {
@@ -216,10 +276,19 @@ class Renderer {
         check(venu_scene_create(recs.data(), (uint32_t)recs.size(), nullptr, &m_scene), "venu_scene_create");
         check(venu_renderer_create(m_max_paths, 0, &m_renderer), "venu_renderer_create");
     }
+    // Moving spheres (no reference counterpart): the same spheres re-posed;
+    // the LBVH is refit and the progressive accumulation restarts.
+    void Update(const Scene& scene) {
+        std::vector<venu_sphere> recs = scene.records();
+        check(venu_scene_update(m_scene, recs.data(), (uint32_t)recs.size(), nullptr), "venu_scene_update");
+        m_scene_changed = true;
+    }
     void Draw(Camera& camera, CUDAOutputBuffer& out) {
         const uint64_t npix = (uint64_t)out.width() * out.height();
         uint32_t flags = 0;
-        if (camera.Changed() || npix != m_accum_pixels) {
+        const bool scene_changed = m_scene_changed;
+        m_scene_changed = false;
+        if (camera.Changed() || scene_changed || npix != m_accum_pixels) {
             if (m_accum) cudaFree(m_accum);
             cuda_check(cudaMalloc(&m_accum, sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL * npix), "accum");
             m_accum_pixels = npix;
@@ -227,7 +296,7 @@ class Renderer {
             flags = VENU_FLAG_RESET_ACCUM;
         }
         ++m_subframe;
-        venu_camera cam = camera.params();
+        venu_camera cam = camera.frame();
         venu_render_opts o{(uint32_t)out.width(), (uint32_t)out.height(), m_spp, m_subframe, m_max_depth, flags};
         check(venu_render(m_renderer, m_scene, &cam, &o, m_accum, out.floatPixels(), out.map(), out.stream()),
               "venu_render");
@@ -251,6 +320,7 @@ class Renderer {
     float* m_accum = nullptr;
     uint64_t m_accum_pixels = 0;
     uint32_t m_subframe = 0;
+    bool m_scene_changed = false;
 };
 
 }  // namespace venu_core

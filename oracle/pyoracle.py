@@ -66,6 +66,7 @@ class Oracle:
         L.vo_scene_rtiow.restype = C.c_uint32
         L.vo_scene_random.restype = C.c_uint32
         L.vo_render.restype = C.c_uint64
+        L.vo_render_refit.restype = C.c_uint64
 
     # RNG ---------------------------------------------------------------
     def tea4(self, a: int, b: int) -> int:
@@ -113,6 +114,15 @@ class Oracle:
         return dict(keys=keys, ids=ids, nodes=nodes[: max(n - 1, 0)], bounds=bounds,
                     depth=int(depth[0]))
 
+    def lbvh_refit(self, spheres_build: np.ndarray, spheres_new: np.ndarray):
+        """Nodes of the LBVH built on spheres_build, moved to spheres_new and
+        refit (same topology, slot order and hoisted set)."""
+        n = len(spheres_build)
+        assert len(spheres_new) == n
+        nodes = np.zeros(max(n - 1, 1), NODE_DTYPE)
+        self.L.vo_lbvh_refit(_p(spheres_build), _p(spheres_new), C.c_uint32(n), _p(nodes))
+        return nodes[: max(n - 1, 0)]
+
     # closest hit -----------------------------------------------------------
     def trace_fp64(self, spheres, rays, tmin=0.001, tmax=1e16):
         rays = np.ascontiguousarray(rays, np.float32)
@@ -149,11 +159,13 @@ class Oracle:
 
     # render --------------------------------------------------------------
     def render(self, spheres, cam, width, height, spp, subframe=0, max_depth=4,
-               mode=MODE_GB300, accum=None, nthreads=0, rows=None, want_samples=False):
+               mode=MODE_GB300, accum=None, nthreads=0, rows=None, want_samples=False, built_from=None):
         """Returns dict(accum, image_f, image8, segments, samples, nodes, spheres).
 
         GB300 mode: accum is (H*W, 8) float32 {sum.rgb, n, comp.rgb, 0}, updated
         in place (zeros = reset).  REF mode: accum is (H*W, 4) {mean.rgb, 1}.
+        built_from: spheres the LBVH was built on before being refit to
+        `spheres` (moving spheres); None = built on `spheres`.
         """
         npx = width * height
         if accum is None:
@@ -166,8 +178,10 @@ class Oracle:
         o = _Opts(width, height, spp, subframe, max_depth, mode, nthreads, r0, r1)
         nv = np.zeros(1, np.uint64)
         ns = np.zeros(1, np.uint64)
-        segs = self.L.vo_render(_p(spheres), C.c_uint32(len(spheres)), _p(cam), C.byref(o),
-                                _p(accum), _p(image_f), _p(image8), _p(samples), _p(nv), _p(ns))
+        if built_from is not None:
+            assert len(built_from) == len(spheres)
+        segs = self.L.vo_render_refit(_p(built_from), _p(spheres), C.c_uint32(len(spheres)), _p(cam), C.byref(o),
+                                      _p(accum), _p(image_f), _p(image8), _p(samples), _p(nv), _p(ns))
         return dict(accum=accum, image_f=image_f, image8=image8, segments=int(segs),
                     samples=samples, nodes=int(nv[0]), spheres=int(ns[0]))
 

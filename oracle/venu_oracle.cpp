@@ -234,6 +234,74 @@ int delta(const std::vector<uint32_t>& k, int n, int i, int j) {
     return __builtin_clz(a ^ b);
 }
 
+// Refit: post-order DFS from the root; a node's box is the union of its
+// children's (leaf boxes from the slot's sphere, rounded outward).  Leaf words
+// may carry the hoisted flag.  Also records the tree depth.
+void refit_bvh(Bvh& B) {
+    const int N = (int)B.n;
+    if (N < 2) return;
+    struct Item { int node; int state; };
+    std::vector<Item> st;
+    st.push_back({0, 0});
+    uint32_t maxdepth = 0;
+    std::vector<uint32_t> dep(N - 1, 0);
+    dep[0] = 1;
+    auto child_box = [&](int c, float* blo, float* bhi) {
+        if (c & kLeaf) {
+            int k = c & kSlotMask;
+            float r = std::fabs(B.radius[k]);
+            blo[0] = sub_rd(B.center[k].x, r);
+            blo[1] = sub_rd(B.center[k].y, r);
+            blo[2] = sub_rd(B.center[k].z, r);
+            bhi[0] = add_ru(B.center[k].x, r);
+            bhi[1] = add_ru(B.center[k].y, r);
+            bhi[2] = add_ru(B.center[k].z, r);
+        } else {
+            for (int a = 0; a < 3; ++a) {
+                blo[a] = B.nodes[c].lo[a];
+                bhi[a] = B.nodes[c].hi[a];
+            }
+        }
+    };
+    while (!st.empty()) {
+        Item it = st.back();
+        st.pop_back();
+        vo_node& nd = B.nodes[it.node];
+        if (it.state == 0) {
+            st.push_back({it.node, 1});
+            for (int c : {nd.left, nd.right}) {
+                if (!(c & kLeaf)) {
+                    dep[c] = dep[it.node] + 1;
+                    st.push_back({c, 0});
+                } else {
+                    maxdepth = std::max(maxdepth, dep[it.node] + 1);
+                }
+            }
+        } else {
+            float l0[3], h0[3], l1[3], h1[3];
+            child_box(nd.left, l0, h0);
+            child_box(nd.right, l1, h1);
+            for (int a = 0; a < 3; ++a) {
+                nd.lo[a] = std::fmin(l0[a], l1[a]);
+                nd.hi[a] = std::fmax(h0[a], h1[a]);
+            }
+        }
+    }
+    B.depth = maxdepth;
+}
+
+// Moving spheres: the same topology, slot order and hoisted set, with every
+// slot's sphere taken from the new array (same original indices) and the
+// boxes refit bottom-up.  Mirrors venu_scene_update.
+void update_bvh(Bvh& B, const vo_sphere* s) {
+    for (uint32_t k = 0; k < B.n; ++k) {
+        const vo_sphere& sp = s[B.ids[k]];
+        B.center[k] = mk(sp.center[0], sp.center[1], sp.center[2]);
+        B.radius[k] = sp.radius;
+    }
+    refit_bvh(B);
+}
+
 void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
     B.n = n;
     B.keys.assign(n, 0);
@@ -305,55 +373,7 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
         if (left & kLeaf) parent_leaf[left & ~kLeaf] = i; else parent_internal[left] = i;
         if (right & kLeaf) parent_leaf[right & ~kLeaf] = i; else parent_internal[right] = i;
     }
-    // Refit: post-order DFS from the root; union of child boxes.
-    struct Item { int node; int state; };
-    std::vector<Item> st;
-    st.push_back({0, 0});
-    uint32_t maxdepth = 0;
-    std::vector<uint32_t> dep(N - 1, 0);
-    dep[0] = 1;
-    auto child_box = [&](int c, float* blo, float* bhi) {
-        if (c & kLeaf) {
-            int k = c & kSlotMask;
-            float r = std::fabs(B.radius[k]);
-            blo[0] = sub_rd(B.center[k].x, r);
-            blo[1] = sub_rd(B.center[k].y, r);
-            blo[2] = sub_rd(B.center[k].z, r);
-            bhi[0] = add_ru(B.center[k].x, r);
-            bhi[1] = add_ru(B.center[k].y, r);
-            bhi[2] = add_ru(B.center[k].z, r);
-        } else {
-            for (int a = 0; a < 3; ++a) {
-                blo[a] = B.nodes[c].lo[a];
-                bhi[a] = B.nodes[c].hi[a];
-            }
-        }
-    };
-    while (!st.empty()) {
-        Item it = st.back();
-        st.pop_back();
-        vo_node& nd = B.nodes[it.node];
-        if (it.state == 0) {
-            st.push_back({it.node, 1});
-            for (int c : {nd.left, nd.right}) {
-                if (!(c & kLeaf)) {
-                    dep[c] = dep[it.node] + 1;
-                    st.push_back({c, 0});
-                } else {
-                    maxdepth = std::max(maxdepth, dep[it.node] + 1);
-                }
-            }
-        } else {
-            float l0[3], h0[3], l1[3], h1[3];
-            child_box(nd.left, l0, h0);
-            child_box(nd.right, l1, h1);
-            for (int a = 0; a < 3; ++a) {
-                nd.lo[a] = std::fmin(l0[a], l1[a]);
-                nd.hi[a] = std::fmax(h0[a], h1[a]);
-            }
-        }
-    }
-    B.depth = maxdepth;
+    refit_bvh(B);
     // Hoisted spheres: the (at most 4) lowest huge slots, if there are at
     // most 64 huge spheres; their leaf words are flagged.
     std::vector<int32_t> cand;
@@ -924,6 +944,14 @@ int vo_lbvh_build(const vo_sphere* s, uint32_t n, uint32_t* morton_sorted, uint3
     return 0;
 }
 
+int vo_lbvh_refit(const vo_sphere* s_build, const vo_sphere* s_new, uint32_t n, vo_node* nodes) {
+    Bvh B;
+    build_bvh(s_build, n, B);
+    update_bvh(B, s_new);
+    if (nodes && n > 1) std::memcpy(nodes, B.nodes.data(), sizeof(vo_node) * (size_t)(n - 1));
+    return 0;
+}
+
 void vo_trace_fp64(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n, float tmin,
                    float tmax, int32_t* id, double* t, double* disc_rel, double* t_second) {
     for (uint32_t i = 0; i < n; ++i) {
@@ -1006,12 +1034,20 @@ void vo_trace_ref(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n
 uint64_t vo_render(const vo_sphere* s, uint32_t ns, const vo_camera* cam, const vo_render_opts* opts,
                    float* accum, float* image_f, uint8_t* image8, float* samples_out,
                    uint64_t* nodes_visited, uint64_t* spheres_tested) {
+    return vo_render_refit(nullptr, s, ns, cam, opts, accum, image_f, image8, samples_out, nodes_visited,
+                           spheres_tested);
+}
+
+uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t ns, const vo_camera* cam,
+                         const vo_render_opts* opts, float* accum, float* image_f, uint8_t* image8,
+                         float* samples_out, uint64_t* nodes_visited, uint64_t* spheres_tested) {
     Scene S;
     S.s = s;
     S.n = ns;
     const bool gb = opts->mode == VO_MODE_GB300;
     if (gb) {
-        build_bvh(s, ns, S.bvh);
+        build_bvh(s_build ? s_build : s, ns, S.bvh);
+        if (s_build) update_bvh(S.bvh, s);
         S.sorted.resize(ns);
         for (uint32_t k = 0; k < ns; ++k) S.sorted[k] = s[S.bvh.ids[k]];
     }

@@ -88,6 +88,10 @@ void vo_camera_look_at(const float eye[3], const float lookat[3], float vfov_deg
 int vo_lbvh_build(const vo_sphere* s, uint32_t n, uint32_t* morton_sorted,
                   uint32_t* sorted_ids, vo_node* nodes, float bounds[6],
                   uint32_t* depth_out);
+/* Build on s_build, then move every sphere to s_new (same count and original
+ * indices) keeping topology, slot order and hoisted set, and refit the boxes
+ * (the product's venu_scene_update). */
+int vo_lbvh_refit(const vo_sphere* s_build, const vo_sphere* s_new, uint32_t n, vo_node* nodes);
 
 /* --- closest hit --- */
 /* rays: n x 6 floats (ox,oy,oz,dx,dy,dz).  FP64 brute force over the float
@@ -116,6 +120,12 @@ uint64_t vo_render(const vo_sphere* s, uint32_t ns, const vo_camera* cam,
                    const vo_render_opts* opts, float* accum, float* image_f,
                    uint8_t* image8, float* samples_out, uint64_t* nodes_visited,
                    uint64_t* spheres_tested);
+/* vo_render of spheres s through the LBVH built on s_build and refit to s
+ * (vo_lbvh_refit); s_build = NULL is vo_render. */
+uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t ns,
+                         const vo_camera* cam, const vo_render_opts* opts, float* accum,
+                         float* image_f, uint8_t* image8, float* samples_out,
+                         uint64_t* nodes_visited, uint64_t* spheres_tested);
 
 /* sRGB encode of linear RGB (Core/RayTracer.cu:16-47). */
 void vo_make_color(const float* rgb, uint32_t n, uint8_t* out4);

@@ -1,8 +1,8 @@
 // Headless replacement of the reference's main loop (Core/Core.cpp:239-438)
 // written against include/venu_core.hpp: Init, two Draws, read back, write a
-// binary PPM and the raw RGBA8 bytes.  Used by tests/test_cpp_dropin.py.
+// binary PPM, the raw RGBA8 bytes and optionally a PFM.  Used by tests/test_cpp_dropin.py.
 //
-//   render_main <width> <height> <spp> <max_depth> <out.ppm> <out.rgba>
+//   render_main <width> <height> <spp> <max_depth> <out.ppm> <out.rgba> [out.pfm]
 #include <cstdio>
 #include <cstdlib>
 
@@ -29,13 +29,9 @@ int main(int argc, char** argv) {
         renderer.Draw(camera, out);
         renderer.Draw(camera, out);
         std::vector<uint8_t> px = out.getHostPointer();
+        out.writePPM(argv[5]);
+        if (argc > 7) out.writePFM(argv[7]);
         renderer.Cleanup();
-        FILE* f = std::fopen(argv[5], "wb");
-        if (!f) return 3;
-        std::fprintf(f, "P6\n%d %d\n255\n", W, H);
-        for (int y = H - 1; y >= 0; --y)  // row 0 is the bottom of the image
-            for (int x = 0; x < W; ++x) std::fwrite(&px[4 * ((size_t)y * W + x)], 1, 3, f);
-        std::fclose(f);
         FILE* g = std::fopen(argv[6], "wb");
         if (!g) return 3;
         std::fwrite(px.data(), 1, px.size(), g);

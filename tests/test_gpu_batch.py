@@ -136,3 +136,56 @@ def test_batch_stop_on_finish(venu, oracle, cuda):
     torch.cuda.synchronize()
     for s in sub:
         assert np.array_equal(s["acc"].cpu().numpy().view(np.uint32), s["want"]["accum"].view(np.uint32))
+
+
+def _one(venu, torch, oracle, b, scene, eye, W, H, spp, depth, sub=1):
+    cam, want = _want(oracle, dict(scene=scene, eye=eye, W=W, H=H, spp=spp, depth=depth, sub=sub))
+    ds = venu.DeviceScene(scene)
+    acc = venu.new_accum(W, H)
+    jid = b.submit(ds, cam, W, H, spp, acc, subframe=sub, max_depth=depth)
+    return dict(id=jid, ds=ds, acc=acc, want=want)
+
+
+@pytest.mark.parametrize("shortest_first", [False, True])
+def test_batch_policy(venu, oracle, cuda, shortest_first):
+    """A small job submitted behind a large one: shortest-first generates its
+    paths at once (it finishes within a few iterations), FIFO only after the
+    large job's paths are all generated.  Results are exact either way."""
+    torch = cuda
+    b = venu.Batch(pool_paths=4096, max_jobs=4)
+    b.set_policy(shortest_first)
+    sp = oracle.scene_rtiow(0)
+    big = _one(venu, torch, oracle, b, sp, (13, 2, 3), 64, 64, 16, 4)
+    small = _one(venu, torch, oracle, b, sp, (13, 2, 3), 8, 6, 1, 4)
+    b.run(stop_on_finish=True)
+    first = b.collect()
+    it = b.stats()["iterations"]
+    if shortest_first:
+        assert first == [small["id"]] and it <= 8
+    else:
+        assert it >= 18  # 65536 paths through a 4096-path pool (>= 16 iterations) before the small job starts
+    b.run()
+    rest = b.collect()
+    torch.cuda.synchronize()
+    assert sorted(first + rest) == sorted([big["id"], small["id"]])
+    for j in (big, small):
+        assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))
+
+
+def test_batch_interrupt(venu, oracle, cuda):
+    """While the interrupt flag is set a run ends after one iteration pair;
+    cleared, the run goes to the end.  Results are exact."""
+    torch = cuda
+    b = venu.Batch(pool_paths=2048, max_jobs=2)
+    j = _one(venu, torch, oracle, b, oracle.scene_rtiow(0), (13, 2, 3), 40, 30, 4, 8)
+    b.interrupt(True)
+    b.run()
+    assert b.collect() == []
+    assert b.stats()["iterations"] == 2
+    b.run()
+    assert b.stats()["iterations"] == 4
+    b.interrupt(False)
+    b.run()
+    assert b.collect() == [j["id"]]
+    torch.cuda.synchronize()
+    assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))

@@ -84,3 +84,21 @@ def test_server_rejects_malformed(venu, oracle, cuda):
     with pytest.raises(venu.VenuError):
         srv.submit(cam, 8, 8, 1, spheres=oracle.scene_rtiow(0), max_depth=0)
     srv.close()
+
+
+def test_server_shortest_first(venu, oracle, cuda):
+    """Shortest-first plan order: same images, every request completes."""
+    srv = venu.Server(hbm_budget_bytes=1 << 30, pool_paths=1500, max_jobs=8, iterations_per_step=64,
+                      shortest_first=True)
+    big = _case(oracle, 0, 48, 32, 8)
+    small = _case(oracle, 1, 12, 8, 1)
+    rb = srv.submit(big[1], 48, 32, 8, spheres=big[0], max_depth=6)
+    rs = srv.submit(small[1], 12, 8, 1, spheres=small[0], max_depth=6)
+    for rid, (_, _, want) in ((rb, big), (rs, small)):
+        r = srv.wait(rid)
+        assert r["status"] == 0
+        assert np.abs(r["image"].astype(int) - want["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    srv.set_policy(False)
+    r = srv.wait(srv.submit(small[1], 12, 8, 1, spheres=small[0], max_depth=6))
+    assert r["status"] == 0
+    srv.close()

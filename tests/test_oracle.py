@@ -164,3 +164,41 @@ def test_scene_generators_match_product(oracle, venu):
 def test_camera_matches_product(oracle, venu):
     for args in (((13, 2, 3), (0, 0, 0), 20.0, 16 / 9, 0.1, 10.0), ((60, 15, 60), (0, 0, 0), 20.0, 1.0, 0.1, 10.0)):
         assert venu.Camera.look_at(*args).tobytes() == oracle.camera(*args).tobytes()
+
+
+def _moved(spheres, seed, scale=1.0):
+    rng = np.random.default_rng(seed)
+    out = spheres.copy()
+    for a in range(3):
+        out["center"][1:, a] += (rng.normal(size=len(out) - 1) * scale).astype(np.float32)
+    out["radius"][1:] *= rng.uniform(0.5, 1.5, size=len(out) - 1).astype(np.float32)
+    return out
+
+
+def test_refit_identity_and_moved(oracle):
+    """Refit to the same spheres reproduces the build; after moving the
+    spheres the refit tree still bounds every sphere, and rendering through
+    it gives the same image as a fresh build (closest hit does not depend on
+    the tree, ties aside)."""
+    sp = oracle.scene_random(3000, 21)
+    built = oracle.lbvh(sp)
+    assert np.array_equal(oracle.lbvh_refit(sp, sp).view(np.uint32), built["nodes"].view(np.uint32))
+    mv = _moved(sp, 5, scale=3.0)
+    nodes = oracle.lbvh_refit(sp, mv)
+    ids = built["ids"]
+    # every leaf box inside its parent's box, children boxes inside parents
+    lo, hi = nodes["lo"], nodes["hi"]
+    for i, nd in enumerate(nodes):
+        for c in (int(nd["left"]), int(nd["right"])):
+            if c & 0x80000000:
+                k = c & 0x3FFFFFFF
+                s = mv[ids[k]]
+                r = abs(float(s["radius"]))
+                assert np.all(lo[i] <= s["center"] - r) and np.all(hi[i] >= s["center"] + r)
+            else:
+                assert np.all(lo[i] <= lo[c]) and np.all(hi[i] >= hi[c])
+    cam = oracle.camera((60, 15, 60), (0, 0, 0), 20.0, 1.5, 0.1, 10.0)
+    a = oracle.render(mv, cam, 36, 24, 2, subframe=3, max_depth=8, built_from=sp)
+    b = oracle.render(mv, cam, 36, 24, 2, subframe=3, max_depth=8)
+    assert np.array_equal(a["accum"].view(np.uint32), b["accum"].view(np.uint32))
+    assert a["segments"] == b["segments"]

@@ -100,6 +100,8 @@ class ServerStats(C.Structure):
 
 BATCH_NO_GRAPH = 1
 RUN_STOP_ON_FINISH = 1
+POLICY_FIFO = 0
+POLICY_SHORTEST_FIRST = 1
 INJECT_ALLOC = 1
 INJECT_SCENE = 2
 
@@ -125,8 +127,18 @@ def lib() -> C.CDLL:
     L.venu_camera_look_at.argtypes = [vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
     L.venu_camera_frame.restype = None
     L.venu_camera_frame.argtypes = [vp, vp, C.c_float, C.c_float, C.c_float, C.c_float, vp]
+    L.venu_camera_rotate.restype = None
+    L.venu_image_write_ppm.restype = C.c_int
+    L.venu_image_write_ppm.argtypes = [C.c_char_p, vp, C.c_uint32, C.c_uint32]
+    L.venu_image_write_pfm.restype = C.c_int
+    L.venu_image_write_pfm.argtypes = [C.c_char_p, vp, C.c_uint32, C.c_uint32]
+    L.venu_camera_rotate.argtypes = [vp, vp, C.c_float, vp]
     L.venu_device_check.argtypes = [vp, vp, vp]
     L.venu_scene_create.argtypes = [vp, u32, vp, C.POINTER(vp)]
+    L.venu_scene_update.restype = C.c_int
+    L.venu_scene_update.argtypes = [vp, vp, C.c_uint32, vp]
+    L.venu_scene_update_device.restype = C.c_int
+    L.venu_scene_update_device.argtypes = [vp, vp, C.c_uint32, vp]
     L.venu_scene_create_device.argtypes = [vp, u32, vp, C.POINTER(vp)]
     L.venu_scene_info_get.argtypes = [vp, C.POINTER(SceneInfo)]
     L.venu_scene_export_bvh.argtypes = [vp, vp, vp, vp]
@@ -153,14 +165,19 @@ def lib() -> C.CDLL:
     L.venu_batch_collect.argtypes = [vp, vp, vp, u32, C.POINTER(u32)]
     L.venu_batch_stats_get.argtypes = [vp, C.POINTER(BatchStats)]
     L.venu_batch_destroy.argtypes = [vp]
+    L.venu_batch_set_policy.argtypes = [vp, u32]
+    L.venu_batch_interrupt.argtypes = [vp, u32]
+    L.venu_server_set_policy.argtypes = [vp, u32]
     L.venu_renderer_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.venu_renderer_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
     for name in ("venu_device_check", "venu_scene_generate_random", "venu_scene_create",
-                 "venu_scene_create_device", "venu_scene_info_get", "venu_scene_export_bvh",
+                 "venu_scene_create_device", "venu_scene_update", "venu_scene_update_device",
+                 "venu_scene_info_get", "venu_scene_export_bvh",
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
                  "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
                  "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit",
                  "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy",
+                 "venu_batch_set_policy", "venu_batch_interrupt", "venu_server_set_policy",
                  "venu_server_create", "venu_server_submit", "venu_server_wait", "venu_server_cancel",
                  "venu_server_release", "venu_server_inject", "venu_server_stats_get", "venu_server_destroy"):
         getattr(L, name).restype = C.c_int

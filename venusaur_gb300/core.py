@@ -9,6 +9,7 @@ compute runs in libvenusaur_gb300.so.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -173,12 +174,16 @@ class Camera:
         self.m_aperture = np.float32(aperture)
         self.m_focalLength = np.float32(focalLength)
         self.m_changed = True
+        self._update_uvw()
+
+    @staticmethod
+    def _normalize(d):
+        d = np.asarray(d, np.float32)
+        dot = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+        return (d * (np.float32(1.0) / np.sqrt(dot))).astype(np.float32)
 
     def SetForward(self, direction) -> None:
-        d = np.asarray(direction, np.float32)
-        dot = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
-        inv = np.float32(1.0) / np.sqrt(dot)
-        self.m_forward = (d * inv).astype(np.float32)
+        self.m_forward = self._normalize(direction)
         self.m_changed = True
 
     def GetLensRadius(self) -> float:
@@ -199,6 +204,33 @@ class Camera:
         self.m_position = (self.m_position + self.m_forward * np.float32(speed)).astype(np.float32)
         self.m_changed = True
 
+    # Core/camera.h:42-78.  As in the reference, the u/v/w axes used here are
+    # those of the last UVWFrame (constructor, params() or UVWFrame()).
+    def MoveRight(self, speed: float) -> None:
+        self.m_position = (self.m_position + self._normalize(self.m_u) * np.float32(speed)).astype(np.float32)
+        self.m_changed = True
+
+    def MoveUp(self, speed: float) -> None:
+        self.m_position = (self.m_position + self._normalize(self.m_v) * np.float32(speed)).astype(np.float32)
+        self.m_changed = True
+
+    def _rotate(self, axis, degrees: float) -> None:
+        f = np.ascontiguousarray(self.m_forward, np.float32)
+        a = np.ascontiguousarray(axis, np.float32)
+        out = np.zeros(3, np.float32)
+        lib().venu_camera_rotate(ptr(f), ptr(a), float(degrees), ptr(out))
+        self.m_forward = out
+        self.m_changed = True
+
+    def Pitch(self, speed: float) -> None:
+        self._rotate(self.m_u, speed)
+
+    def Yaw(self, speed: float) -> None:
+        self._rotate(self.m_v, speed)
+
+    def Roll(self, speed: float) -> None:
+        self._rotate(self.m_w, speed)
+
     def Changed(self) -> bool:
         c = self.m_changed
         self.m_changed = False
@@ -211,11 +243,15 @@ class Camera:
         f = np.ascontiguousarray(self.m_forward, np.float32)
         lib().venu_camera_frame(ptr(e), ptr(f), float(self.m_vfov), float(self.m_aspect),
                                 float(self.m_aperture), float(self.m_focalLength), ptr(cam))
+        self.m_u, self.m_v, self.m_w = cam[0]["u"].copy(), cam[0]["v"].copy(), cam[0]["w"].copy()
         return cam
 
+    def _update_uvw(self) -> None:
+        self.params()
+
     def UVWFrame(self):
-        c = self.params()[0]
-        return c["u"].copy(), c["v"].copy(), c["w"].copy()
+        self.params()
+        return self.m_u.copy(), self.m_v.copy(), self.m_w.copy()
 
     @staticmethod
     def look_at(eye, lookat, vfov, aspect, aperture, focal) -> np.ndarray:
@@ -248,6 +284,18 @@ class DeviceScene:
         check(lib().venu_scene_create_device(ptr(spheres_dev), n, _stream_handle(stream), C.byref(h)))
         self.handle = h
         return self
+
+    def update(self, spheres, stream=None) -> None:
+        """Moving spheres: the same count in the same order, new centres /
+        radii / materials; the LBVH is refit, not rebuilt (venu_scene_update)."""
+        arr = spheres.spheres if isinstance(spheres, Scene) else np.ascontiguousarray(spheres, SPHERE_DTYPE)
+        check(lib().venu_scene_update(self.handle, ptr(arr), len(arr), _stream_handle(stream)))
+        self.spheres = arr
+
+    def update_device(self, spheres_dev, n: int, stream=None) -> None:
+        """As update(), from a device buffer of venu_sphere records (asynchronous)."""
+        check(lib().venu_scene_update_device(self.handle, ptr(spheres_dev), n, _stream_handle(stream)))
+        self.spheres = None
 
     def info(self) -> dict:
         si = SceneInfo()
@@ -339,6 +387,23 @@ class Wavefront:
             pass
 
 
+def write_ppm(path: str, rgba8, width: int, height: int) -> None:
+    """Binary PPM of a host RGBA8 image in the renderer's pixel order (row 0 =
+    bottom): the headless stand-in for the reference's GL display."""
+    a = np.ascontiguousarray(np.asarray(rgba8, np.uint8).reshape(-1))
+    if a.size != 4 * width * height:
+        raise ValueError("write_ppm: image size does not match width x height x 4")
+    check(lib().venu_image_write_ppm(os.fsencode(path), ptr(a), width, height))
+
+
+def write_pfm(path: str, rgbaf, width: int, height: int) -> None:
+    """PFM (RGB float32, little-endian) of a host RGBA32F image."""
+    a = np.ascontiguousarray(np.asarray(rgbaf, np.float32).reshape(-1))
+    if a.size != 4 * width * height:
+        raise ValueError("write_pfm: image size does not match width x height x 4")
+    check(lib().venu_image_write_pfm(os.fsencode(path), ptr(a), width, height))
+
+
 def new_accum(width: int, height: int, device="cuda"):
     torch = _torch()
     return torch.zeros((height * width, _lib.ACCUM_FLOATS), dtype=torch.float32, device=device)
@@ -380,6 +445,12 @@ class CUDAOutputBuffer:
     def getHostFloat(self) -> np.ndarray:
         return self.pixels_f.cpu().numpy()
 
+    def writePPM(self, path: str) -> None:
+        write_ppm(path, self.getHostPointer(), self.m_width, self.m_height)
+
+    def writePFM(self, path: str) -> None:
+        write_pfm(path, self.getHostFloat(), self.m_width, self.m_height)
+
 
 class Renderer:
     """Renderer::Init / Draw / Cleanup over the wavefront kernels.
@@ -403,11 +474,19 @@ class Renderer:
         """ptxSource is accepted for signature parity and ignored (no PTX JIT)."""
         self.scene = DeviceScene(scene)
         self.wave = Wavefront(self.max_paths)
+        self._scene_changed = False
+
+    def Update(self, scene: Scene) -> None:
+        """Moving spheres (no reference counterpart): the same spheres
+        re-posed; the LBVH is refit and the progressive accumulation restarts."""
+        self.scene.update(scene)
+        self._scene_changed = True
 
     def Draw(self, camera: Camera, outputBuffer: CUDAOutputBuffer) -> None:
         W, H = outputBuffer.width(), outputBuffer.height()
         reset = False
-        if camera.Changed() or self.accum is None or self.accum.shape[0] != W * H:
+        scene_changed, self._scene_changed = getattr(self, "_scene_changed", False), False
+        if camera.Changed() or scene_changed or self.accum is None or self.accum.shape[0] != W * H:
             self.accum = new_accum(W, H, outputBuffer.m_device)
             self.subframe_index = 0
             reset = True
@@ -476,6 +555,15 @@ class Batch:
         flags = _lib.RUN_STOP_ON_FINISH if stop_on_finish else 0
         check(lib().venu_batch_run(self.handle, max_iterations, flags, _stream_handle(stream)))
 
+    def set_policy(self, shortest_first: bool) -> None:
+        """Plan order: submission order (False) or fewest unfinished paths first."""
+        pol = _lib.POLICY_SHORTEST_FIRST if shortest_first else _lib.POLICY_FIFO
+        check(lib().venu_batch_set_policy(self.handle, pol))
+
+    def interrupt(self, on: bool = True) -> None:
+        """Ends a running run() at its next iteration boundary while set."""
+        check(lib().venu_batch_interrupt(self.handle, 1 if on else 0))
+
     def collect(self, stream=None) -> list:
         ids = (C.c_uint32 * self.max_jobs)()
         n = C.c_uint32()
@@ -504,11 +592,17 @@ class Server:
     rendered together in one shared path pool by the server's own thread."""
 
     def __init__(self, hbm_budget_bytes: int, pool_paths: int = 0, max_jobs: int = 64,
-                 iterations_per_step: int = 8):
+                 iterations_per_step: int = 8, shortest_first: bool = False):
         h = C.c_void_p()
         check(lib().venu_server_create(int(hbm_budget_bytes), pool_paths, max_jobs, iterations_per_step,
                                        C.byref(h)))
         self.handle = h
+        if shortest_first:
+            self.set_policy(True)
+
+    def set_policy(self, shortest_first: bool) -> None:
+        pol = _lib.POLICY_SHORTEST_FIRST if shortest_first else _lib.POLICY_FIFO
+        check(lib().venu_server_set_policy(self.handle, pol))
 
     def submit(self, camera: np.ndarray, width: int, height: int, spp: int, spheres=None, scene_key: int = 0,
                subframe: int = 1, max_depth: int = 50, tag: int = 0) -> int:

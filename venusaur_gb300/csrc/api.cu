@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <random>
@@ -253,6 +254,108 @@ extern "C" void venu_camera_frame(const float eye[3], const float forward[3], fl
     out->lens_radius = aperture * 0.5f;
 }
 
+extern "C" void venu_camera_rotate(const float forward[3], const float axis[3], float degrees, float out[3]) {
+    // Camera::Pitch / Yaw / Roll (Core/camera.h:56-78):
+    //   q = glm::rotate(quat(1,0,0,0), glm::radians(degrees), axis)
+    //   forward = normalize(forward * q)
+    // restated from GLM's published quaternion functions: rotate() normalises
+    // the axis only when its length is off 1 by more than 0.001 and builds
+    // q = (cos(a/2), axis*sin(a/2)) (the product with the identity is exact);
+    // vec3 * quat rotates by inverse(q) = conjugate(q) / dot(q, q), applied as
+    // v + 2*(cross(qv, v)*w + cross(qv, cross(qv, v))).
+    float ax[3] = {axis[0], axis[1], axis[2]};
+    const float len = std::sqrt(dot3(ax, ax));
+    if (std::fabs(len - 1.0f) > 0.001f) {
+        const float inv = 1.0f / len;
+        ax[0] *= inv;
+        ax[1] *= inv;
+        ax[2] *= inv;
+    }
+    const float a = degrees * 0.01745329251994329576923690768489f;
+    const float sh = std::sin(a * 0.5f), ch = std::cos(a * 0.5f);
+    const float qw = ch, qx = ax[0] * sh, qy = ax[1] * sh, qz = ax[2] * sh;
+    const float d = (qw * qw + qx * qx) + (qy * qy + qz * qz);
+    const float iw = qw / d, ix = -qx / d, iy = -qy / d, iz = -qz / d;
+    const float v[3] = {forward[0], forward[1], forward[2]};
+    const float uv[3] = {iy * v[2] - v[1] * iz, iz * v[0] - v[2] * ix, ix * v[1] - v[0] * iy};
+    const float uuv[3] = {iy * uv[2] - uv[1] * iz, iz * uv[0] - uv[2] * ix, ix * uv[1] - uv[0] * iy};
+    float r[3];
+    for (int i = 0; i < 3; ++i) r[i] = v[i] + (uv[i] * iw + uuv[i]) * 2.0f;
+    norm3(r);
+    out[0] = r[0];
+    out[1] = r[1];
+    out[2] = r[2];
+}
+
+// ---- image files (the headless replacement of the GL display path,
+// Core/CUDAOutputBuffer.h:284-339 and Core/Core.cpp:396-426) --------------
+extern "C" venu_status venu_image_write_ppm(const char* path, const uint8_t* rgba8, uint32_t width, uint32_t height) {
+    if (!path || (!rgba8 && width && height)) {
+        set_error("venu_image_write_ppm: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("venu_image_write_ppm: cannot open ") + path);
+        return VENU_ERR_INVALID;
+    }
+    std::fprintf(f, "P6\n%u %u\n255\n", width, height);
+    std::vector<uint8_t> row(3u * (size_t)width);
+    bool ok = true;
+    for (uint32_t y = height; y-- > 0 && ok;) {  // pixel row 0 is the bottom of the image
+        const uint8_t* src = rgba8 + 4u * (size_t)y * width;
+        for (uint32_t x = 0; x < width; ++x) {
+            row[3 * x] = src[4 * x];
+            row[3 * x + 1] = src[4 * x + 1];
+            row[3 * x + 2] = src[4 * x + 2];
+        }
+        ok = std::fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error(std::string("venu_image_write_ppm: write failed: ") + path);
+        return VENU_ERR_INVALID;
+    }
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_image_write_pfm(const char* path, const float* rgba32f, uint32_t width, uint32_t height) {
+    if (!path || (!rgba32f && width && height)) {
+        set_error("venu_image_write_pfm: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    FILE* f = std::fopen(path, "wb");
+    if (!f) {
+        set_error(std::string("venu_image_write_pfm: cannot open ") + path);
+        return VENU_ERR_INVALID;
+    }
+    // PFM: "PF", size, negative scale = little-endian floats, rows bottom to
+    // top (the pixel order of the buffers); byte order fixed explicitly.
+    std::fprintf(f, "PF\n%u %u\n-1.0\n", width, height);
+    std::vector<uint8_t> row(12u * (size_t)width);
+    bool ok = true;
+    for (uint32_t y = 0; y < height && ok; ++y) {
+        const float* src = rgba32f + 4u * (size_t)y * width;
+        for (uint32_t x = 0; x < width; ++x)
+            for (int c = 0; c < 3; ++c) {
+                uint32_t b;
+                std::memcpy(&b, &src[4 * x + c], 4);
+                uint8_t* d = &row[12 * x + 4 * c];
+                d[0] = (uint8_t)b;
+                d[1] = (uint8_t)(b >> 8);
+                d[2] = (uint8_t)(b >> 16);
+                d[3] = (uint8_t)(b >> 24);
+            }
+        ok = std::fwrite(row.data(), 1, row.size(), f) == row.size();
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) {
+        set_error(std::string("venu_image_write_pfm: write failed: ") + path);
+        return VENU_ERR_INVALID;
+    }
+    return VENU_OK;
+}
+
 extern "C" venu_status venu_scene_create_device(const venu_sphere* spheres_dev, uint32_t n, void* stream,
                                                 venu_scene** out) {
     if (!out || (!spheres_dev && n)) {
@@ -295,6 +398,43 @@ extern "C" venu_status venu_scene_create(const venu_sphere* spheres_host, uint32
     venu_status rc = venu_scene_create_device(d, n, stream, out);
     cudaStreamSynchronize(st);
     cudaFree(d);
+    return rc;
+}
+
+extern "C" venu_status venu_scene_update_device(venu_scene* scene, const venu_sphere* spheres_dev, uint32_t n,
+                                                void* stream) {
+    if (!scene || (!spheres_dev && n)) {
+        set_error("venu_scene_update: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    if (n != scene->n) {
+        set_error("venu_scene_update: sphere count differs from the scene's (" + std::to_string(n) + " vs " +
+                  std::to_string(scene->n) + "); a different count needs venu_scene_create");
+        return VENU_ERR_INVALID;
+    }
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    return update_scene(scene, spheres_dev, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" venu_status venu_scene_update(venu_scene* scene, const venu_sphere* spheres_host, uint32_t n,
+                                         void* stream) {
+    if (!scene || (!spheres_host && n)) {
+        set_error("venu_scene_update: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    if (n != scene->n) return venu_scene_update_device(scene, nullptr, n, stream);  // reports the mismatch
+    venu_status ds = require_device();
+    if (ds != VENU_OK) return ds;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (n == 0) return VENU_OK;
+    venu_sphere* d = nullptr;
+    VENU_CUDA(cudaMallocAsync(&d, sizeof(venu_sphere) * n, st));
+    cudaError_t e = cudaMemcpyAsync(d, spheres_host, sizeof(venu_sphere) * n, cudaMemcpyHostToDevice, st);
+    venu_status rc = e == cudaSuccess ? update_scene(scene, d, st) : cuda_fail(e, "venu_scene_update: upload");
+    cudaFreeAsync(d, st);
+    cudaError_t se = cudaStreamSynchronize(st);
+    if (rc == VENU_OK && se != cudaSuccess) rc = cuda_fail(se, "venu_scene_update");
     return rc;
 }
 

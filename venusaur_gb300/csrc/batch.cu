@@ -130,7 +130,7 @@ __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restri
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_trace_shade_multi(const DevJob* __restrict__ jobs,
+__global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
                                                            unsigned long long* __restrict__ job_done, LoopCtl* ctl,
                                                            Queue qin, Queue qout, int in) {
     extern __shared__ unsigned char smem[];
@@ -184,8 +184,10 @@ __global__ void __launch_bounds__(256) k_trace_shade_multi(const DevJob* __restr
     if (overflow) atomicOr(&ctl->err, 1u);
 }
 
-__global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, cudaGraphConditionalHandle handle,
-                            int use_handle) {
+// interrupt: a word in mapped host memory (venu_batch_interrupt), read once
+// per iteration pair; volatile so every read goes to the host's copy.
+__global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, const volatile uint32_t* interrupt,
+                            cudaGraphConditionalHandle handle, int use_handle) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const uint32_t it = ctl->iter + 2u;
     ctl->iter = it;
@@ -193,6 +195,7 @@ __global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, cudaGr
     uint32_t more = (ctl->cnt[0] > 0u || ctl->more_gen) ? 1u : 0u;
     if (run->max_iter && it >= run->max_iter) more = 0u;
     if (run->stop_on_finish && ctl->job_finished) more = 0u;  // hand finished jobs to the host now
+    if (*interrupt) more = 0u;                                 // the host has new work to admit
     ctl->running = more;
     if (use_handle) cudaGraphSetConditional(handle, more);
 }
@@ -235,6 +238,8 @@ struct JobHost {
     bool active = false;
     venu_job_desc desc{};
     uint64_t total = 0, bytes = 0;
+    uint64_t seq = 0;        // submission number
+    uint64_t remaining = 0;  // paths not finished at the last collect
     uint32_t* seeds = nullptr;
     float4* slots = nullptr;
 };
@@ -253,7 +258,11 @@ struct venu_batch {
     RunCtl* d_run = nullptr;
     CollectEntry* d_collect = nullptr;
     std::vector<JobHost> jobs;
-    std::vector<uint32_t> order;  // active job slots, submission order
+    std::vector<uint32_t> order;  // active job slots in plan order (policy)
+    uint32_t policy = VENU_POLICY_FIFO;
+    uint64_t next_seq = 0;
+    uint32_t* h_interrupt = nullptr;  // mapped host word
+    uint32_t* d_interrupt = nullptr;  // its device address
     venu_tuning tune = {2u, 8u, 256u, 0u, 256u, 0u};
     int trav_blocks = 0, regen_blocks = 0;
     cudaStream_t cap = nullptr;
@@ -292,7 +301,7 @@ cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
         k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
                                                  b->q[out]);
     }
-    k_loop_cond<<<1, 32, 0, st>>>(b->d_ctl, b->d_run, b->handle, use_handle ? 1 : 0);
+    k_loop_cond<<<1, 32, 0, st>>>(b->d_ctl, b->d_run, b->d_interrupt, b->handle, use_handle ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -348,10 +357,22 @@ void free_batch(venu_batch* b) {
     cudaFree(b->d_ctl);
     cudaFree(b->d_run);
     cudaFree(b->d_collect);
+    if (b->h_interrupt) cudaFreeHost(b->h_interrupt);
     if (b->cap) cudaStreamDestroy(b->cap);
 }
 
+// Plan order: submission order (FIFO), or fewest unfinished paths first
+// (shortest remaining first; ties by submission).  The order decides only
+// which job's new paths take free pool slots first -- never the results.
 venu_status upload_order(venu_batch* b, cudaStream_t st) {
+    if (b->policy == VENU_POLICY_SHORTEST_FIRST)
+        std::stable_sort(b->order.begin(), b->order.end(), [b](uint32_t x, uint32_t y) {
+            const JobHost &X = b->jobs[x], &Y = b->jobs[y];
+            return X.remaining != Y.remaining ? X.remaining < Y.remaining : X.seq < Y.seq;
+        });
+    else
+        std::stable_sort(b->order.begin(), b->order.end(),
+                         [b](uint32_t x, uint32_t y) { return b->jobs[x].seq < b->jobs[y].seq; });
     if (!b->order.empty())
         VENU_CUDA(cudaMemcpyAsync(b->d_order, b->order.data(), sizeof(uint32_t) * b->order.size(),
                                   cudaMemcpyHostToDevice, st));
@@ -404,6 +425,11 @@ extern "C" venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs,
     if (e == cudaSuccess) e = cudaMemset(b->d_run, 0, sizeof(RunCtl));
     if (e == cudaSuccess) e = cudaMemset(b->d_jobs, 0, sizeof(DevJob) * max_jobs);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaHostAlloc(&b->h_interrupt, sizeof(uint32_t), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+        *b->h_interrupt = 0u;
+        e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&b->d_interrupt), b->h_interrupt, 0);
+    }
     if (e == cudaSuccess) e = batch_configure(b);
     if (e != cudaSuccess) {
         venu_status s = cuda_fail(e, "venu_batch_create");
@@ -471,6 +497,8 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     J.active = true;
     J.desc = *job;
     J.total = total;
+    J.remaining = total;
+    J.seq = b->next_seq++;
     J.bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel);
     DevJob dj;
     std::memset(&dj, 0, sizeof(dj));
@@ -521,7 +549,7 @@ extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, ui
             uint32_t running = 0;
             VENU_CUDA(cudaMemcpyAsync(&running, &b->d_ctl->running, sizeof(running), cudaMemcpyDeviceToHost, st));
             VENU_CUDA(cudaStreamSynchronize(st));
-            if (!running) break;
+            if (!running || __atomic_load_n(b->h_interrupt, __ATOMIC_ACQUIRE)) break;
         }
         return VENU_OK;
     }
@@ -551,6 +579,7 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
     uint32_t pix_off = 0;
     for (uint32_t slot : b->order) {
         JobHost& J = b->jobs[slot];
+        J.remaining = J.total - std::min<uint64_t>(done[slot], J.total);
         if (done[slot] < J.total) continue;
         const venu_render_opts& o = J.desc.opts;
         CollectEntry c;
@@ -581,6 +610,8 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
         for (uint32_t slot : b->order)
             if (b->jobs[slot].active) keep.push_back(slot);
         b->order.swap(keep);
+    }
+    if (!ent.empty() || b->policy == VENU_POLICY_SHORTEST_FIRST) {
         venu_status us = upload_order(b, st);
         if (us != VENU_OK) return us;
     }
@@ -592,6 +623,24 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
         set_error("venu_batch: traversal stack overflow");
         return VENU_ERR_STACK;
     }
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy) {
+    if (!b || policy > VENU_POLICY_SHORTEST_FIRST) {
+        set_error("venu_batch_set_policy: NULL batch or unknown policy");
+        return VENU_ERR_INVALID;
+    }
+    b->policy = policy;
+    return upload_order(b, nullptr);
+}
+
+extern "C" venu_status venu_batch_interrupt(venu_batch* b, uint32_t on) {
+    if (!b) {
+        set_error("venu_batch_interrupt: NULL batch");
+        return VENU_ERR_INVALID;
+    }
+    __atomic_store_n(b->h_interrupt, on ? 1u : 0u, __ATOMIC_RELEASE);
     return VENU_OK;
 }
 

@@ -46,6 +46,7 @@ struct LbvhCtl {
     uint32_t nhoist;      // hoisted (<= kMaxHoisted), 0 if more than kHoistCandidates
     int32_t hoist[kMaxHoisted];
     uint32_t hoist_buf[64];
+    uint32_t bad_words;   // child words k_trav_layout had to replace (never, for a sound build)
 };
 constexpr uint32_t kHoistCandidates = 64;
 
@@ -66,6 +67,7 @@ __global__ void k_lbvh_init(LbvhCtl* c) {
         }
         c->hoist_cnt = 0;
         c->nhoist = 0;
+        c->bad_words = 0;
     }
 }
 
@@ -298,13 +300,16 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, int n, float4* __res
 // Leaf boxes + bottom-up refit.  The second thread to arrive at a node
 // computes its box; a __threadfence before each arrival publishes the
 // children's boxes, and they are read back through L2 (__ldcg).
-__global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __restrict__ vals, int n,
+// ids[k] & id_mask = original index of the sphere in slot k (the sorted
+// values during a build, the meta words during a refit of moved spheres).
+// Leaf words may carry the hoisted flag (refit after a build).
+__global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __restrict__ ids, uint32_t id_mask, int n,
                         float4* nodes, const int32_t* __restrict__ parent_int,
                         const int32_t* __restrict__ parent_leaf, float4* leafbox,
                         uint32_t* __restrict__ arrive) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    const venu_sphere& sp = s[vals[k]];
+    const venu_sphere& sp = s[ids[k] & id_mask];
     float r = fabsf(sp.radius);
     // An exactly-zero difference rounds down to -0.0; "+ 0.0f" makes it +0.0
     // (still a lower bound) so boxes never carry a signed zero.
@@ -322,24 +327,27 @@ __global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __res
         __threadfence();
         int32_t cl = __float_as_int(__ldcg(&nodes[2 * p].w));
         int32_t cr = __float_as_int(__ldcg(&nodes[2 * p + 1].w));
-        const bool ok_l = (cl & kLeaf) ? (cl & ~kLeaf) < n : cl < n - 1;
-        const bool ok_r = (cr & kLeaf) ? (cr & ~kLeaf) < n : cr < n - 1;
+        const bool ok_l = (cl & kLeaf) ? (cl & kSlotMask) < n : cl < n - 1;
+        const bool ok_r = (cr & kLeaf) ? (cr & kSlotMask) < n : cr < n - 1;
         if (!ok_l || !ok_r) return;
-        float4 l0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf)) : __ldcg(nodes + 2 * cl);
-        float4 h0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & ~kLeaf) + 1) : __ldcg(nodes + 2 * cl + 1);
-        float4 l1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & ~kLeaf)) : __ldcg(nodes + 2 * cr);
-        float4 h1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & ~kLeaf) + 1) : __ldcg(nodes + 2 * cr + 1);
+        float4 l0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & kSlotMask)) : __ldcg(nodes + 2 * cl);
+        float4 h0 = (cl & kLeaf) ? __ldcg(leafbox + 2 * (cl & kSlotMask) + 1) : __ldcg(nodes + 2 * cl + 1);
+        float4 l1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & kSlotMask)) : __ldcg(nodes + 2 * cr);
+        float4 h1 = (cr & kLeaf) ? __ldcg(leafbox + 2 * (cr & kSlotMask) + 1) : __ldcg(nodes + 2 * cr + 1);
         nodes[2 * p] = make_float4(fminf(l0.x, l1.x), fminf(l0.y, l1.y), fminf(l0.z, l1.z), __int_as_float(cl));
         nodes[2 * p + 1] = make_float4(fmaxf(h0.x, h1.x), fmaxf(h0.y, h1.y), fmaxf(h0.z, h1.z), __int_as_float(cr));
         p = parent_int[p];
     }
 }
 
-__global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* __restrict__ vals, uint32_t n,
-                         float4* __restrict__ sph, float4* __restrict__ mat, uint32_t* __restrict__ meta) {
+// Slot-ordered sphere / material / meta records.  ids may alias meta (a
+// refit regathers from the meta words): each thread reads its slot's word
+// before writing it.
+__global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* ids, uint32_t id_mask, uint32_t n,
+                         float4* __restrict__ sph, float4* __restrict__ mat, uint32_t* meta) {
     uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    uint32_t id = vals[k];
+    uint32_t id = ids[k] & id_mask;
     const venu_sphere& sp = s[id];
     uint32_t type = sp.material > 2u ? 2u : sp.material;
     sph[k] = make_float4(sp.center[0], sp.center[1], sp.center[2], sp.radius);
@@ -356,21 +364,30 @@ __global__ void k_gather(const venu_sphere* __restrict__ s, const uint32_t* __re
 // A step of the traversal then reads one record instead of two boxes or
 // spheres at two addresses.  Runs after k_hoist_finalize, so the flags are
 // final; the canonical nodes array stays the exported form.
+//
+// Every word written here is in range by construction -- an internal child
+// in [1, n-1), a leaf slot below n -- so the traversal needs no per-step
+// index checks: a word that is not (which a sound build never produces) is
+// replaced by a skipped leaf and counted in *bad.
 __global__ void k_trav_layout(const float4* __restrict__ nodes, const float4* __restrict__ sph, uint32_t n,
-                              float4* __restrict__ trav) {
+                              float4* __restrict__ trav, uint32_t* bad) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 2u * (n - 1u)) return;
     const uint32_t p = i >> 1, c = i & 1u;
-    const int32_t w = __float_as_int(nodes[2 * p + c].w);
+    int32_t w = __float_as_int(nodes[2 * p + c].w);
+    const bool ok = (w & kLeaf) ? (uint32_t)(w & kSlotMask) < n && !(w & ~(kLeaf | kHoisted | kSlotMask))
+                                : (uint32_t)w - 1u < n - 2u;  // 1 <= w < n-1 (the root is nobody's child)
+    if (!ok) {
+        w = kLeaf | kHoisted;  // slot 0, never tested
+        if (bad) atomicAdd(bad, 1u);
+    }
     float4 a, b;
     if (w & kLeaf) {
-        const uint32_t k = (uint32_t)(w & kSlotMask);
-        const float4 s4 = k < n ? sph[k] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float4 s4 = sph[w & kSlotMask];
         a = make_float4(s4.x, s4.y, s4.z, __int_as_float(w));
         b = make_float4(s4.w, 0.0f, 0.0f, 0.0f);
     } else {
-        const uint32_t q = (uint32_t)w < n - 1u ? (uint32_t)w : 0u;
-        const float4 lo = nodes[2 * q], hi = nodes[2 * q + 1];
+        const float4 lo = nodes[2 * w], hi = nodes[2 * w + 1];
         a = make_float4(lo.x, lo.y, lo.z, __int_as_float(w));
         b = make_float4(hi.x, hi.y, hi.z, 0.0f);
     }
@@ -416,13 +433,14 @@ cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const
     // four passes: the sorted codes / ids are back in B.keys / B.vals
     if (n > 1) {
         k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(B.keys, (int)n, B.nodes, B.pint, B.pleaf);
-        k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, (int)n, B.nodes, B.pint, B.pleaf, B.leafbox, B.arrive);
+        k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, 0xffffffffu, (int)n, B.nodes, B.pint, B.pleaf, B.leafbox,
+                                              B.arrive);
     }
-    k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, n, B.sph, B.mat, B.meta);
+    k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, 0xffffffffu, n, B.sph, B.mat, B.meta);
     if (n > 1) {
         k_hoist_collect<<<cdiv(n, 256), 256, 0, st>>>(B.sph, n, B.ctl);
         k_hoist_finalize<<<1, 32, 0, st>>>(B.ctl, B.pleaf, B.nodes, n);
-        if (B.trav) k_trav_layout<<<cdiv(2 * (n - 1), 256), 256, 0, st>>>(B.nodes, B.sph, n, B.trav);
+        if (B.trav) k_trav_layout<<<cdiv(2 * (n - 1), 256), 256, 0, st>>>(B.nodes, B.sph, n, B.trav, &B.ctl->bad_words);
     }
     return cudaGetLastError();
 }
@@ -437,6 +455,8 @@ void free_scene(venu_scene* s) {
     cudaFree(s->mat);
     cudaFree(s->meta);
     cudaFree(s->keys);
+    cudaFree(s->parents);
+    s->parents = nullptr;
     s->nodes = s->trav = nullptr;
     s->sph = s->mat = nullptr;
     s->meta = s->keys = nullptr;
@@ -463,6 +483,7 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     VENU_CUDA(alloc((void**)&S->mat, sizeof(float4) * n));
     VENU_CUDA(alloc((void**)&S->meta, sizeof(uint32_t) * n));
     VENU_CUDA(alloc((void**)&S->keys, sizeof(uint32_t) * n));
+    VENU_CUDA(alloc((void**)&S->parents, sizeof(int32_t) * ((size_t)nint + n)));
     S->bytes = bytes;
     LbvhBuffers B{};
     B.nodes = S->nodes;
@@ -471,6 +492,8 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     B.mat = S->mat;
     B.meta = S->meta;
     B.keys = S->keys;
+    B.pint = S->parents;
+    B.pleaf = S->parents + nint;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     venu_status rc = VENU_OK;
     LbvhCtl hc;
@@ -488,8 +511,6 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
     STEP(cudaMalloc(&B.vals_alt, sizeof(uint32_t) * n));
     STEP(cudaMalloc(&B.hist, sizeof(uint32_t) * hist_n));
     STEP(cudaMalloc(&B.arrive, sizeof(uint32_t) * nint));
-    STEP(cudaMalloc(&B.pint, sizeof(int32_t) * nint));
-    STEP(cudaMalloc(&B.pleaf, sizeof(int32_t) * n));
     STEP(cudaMalloc(&B.leafbox, sizeof(float4) * 2 * n));
     STEP(cudaEventCreate(&e0));
     STEP(cudaEventCreate(&e1));
@@ -505,6 +526,11 @@ venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t
         std::memcpy(S->bounds, hc.bounds, sizeof(S->bounds));
         S->nhoist = n > 1 ? hc.nhoist : 0u;
         for (int i = 0; i < kMaxHoisted; ++i) S->hoist[i] = hc.hoist[i];
+        if (n > 1 && hc.bad_words) {
+            set_error("venu_scene_create: the LBVH build produced " + std::to_string(hc.bad_words) +
+                      " out-of-range child words");
+            rc = VENU_ERR_INVALID;
+        }
     }
 #undef STEP
 done:
@@ -514,12 +540,37 @@ done:
     cudaFree(B.vals_alt);
     cudaFree(B.hist);
     cudaFree(B.arrive);
-    cudaFree(B.pint);
-    cudaFree(B.pleaf);
     cudaFree(B.leafbox);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     return rc;
+}
+
+venu_status update_scene(venu_scene* S, const venu_sphere* s, cudaStream_t st) {
+    const uint32_t n = S->n;
+    if (n == 0) return VENU_OK;
+    // New sphere records into the same slots (meta holds each slot's
+    // original index), then the boxes bottom-up over the kept parent links,
+    // then the traversal records.  Topology, slot order and the hoisted set
+    // stay those of the build.
+    k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, S->meta, 0x3fffffffu, n, S->sph, S->mat, S->meta);
+    VENU_CUDA(cudaGetLastError());
+    if (n == 1) return VENU_OK;
+    float4* leafbox = nullptr;
+    uint32_t* arrive = nullptr;
+    VENU_CUDA(cudaMallocAsync(&leafbox, sizeof(float4) * 2 * n, st));
+    cudaError_t e = cudaMallocAsync(&arrive, sizeof(uint32_t) * (n - 1), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(arrive, 0, sizeof(uint32_t) * (n - 1), st);
+    if (e == cudaSuccess) {
+        k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, S->meta, 0x3fffffffu, (int)n, S->nodes, S->parents,
+                                              S->parents + (n - 1), leafbox, arrive);
+        k_trav_layout<<<cdiv(2 * (n - 1), 256), 256, 0, st>>>(S->nodes, S->sph, n, S->trav, nullptr);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(leafbox, st);
+    if (arrive) cudaFreeAsync(arrive, st);
+    if (e != cudaSuccess) return cuda_fail(e, "venu_scene_update");
+    return VENU_OK;
 }
 
 }  // namespace venu

@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
 // continuing paths with one ballot and one atomic.  Saves the hit record
 // round trip, the second read of the rays and one launch per bounce.
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+__global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
                                                      uint32_t* __restrict__ work, Queue qout,
                                                      uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                      uint32_t* __restrict__ err,
@@ -337,7 +337,7 @@ struct venu_renderer {
     uint32_t* work = nullptr;  // [65]
     uint32_t* err = nullptr;
     unsigned long long* stats = nullptr;  // segments, nodes, spheres
-    venu_tuning tune = {1u, 8u, 128u, 0u, 256u, 0u};
+    venu_tuning tune = {2u, 32u, 128u, 0u, 128u, 0u};
     int trav_blocks = 0, shade_blocks = 0;
     venu_render_stats last = {};
     // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
@@ -422,7 +422,7 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     *out = nullptr;
     venu_status ds = require_device();
     if (ds != VENU_OK) return ds;
-    if (max_paths == 0) max_paths = 8u << 20;
+    if (max_paths == 0) max_paths = 16u << 20;
     if (max_paths > (1u << 27)) {
         set_error("venu_renderer_create: max_paths above 2^27");
         return VENU_ERR_TOO_LARGE;

@@ -11,6 +11,7 @@
 #include "venu_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -82,6 +83,8 @@ struct venu_server {
     uint64_t resident_shared = 0;
     venu_status fatal = VENU_OK;
     std::string fatal_msg;
+    std::atomic<uint32_t> policy{VENU_POLICY_FIFO};  // plan order, applied by the server thread
+    uint32_t applied_policy = VENU_POLICY_FIFO;
 
     // owned by the server thread
     std::thread th;
@@ -230,6 +233,16 @@ void server_loop(venu_server* s) {
     cudaSetDevice(s->device);
     std::vector<uint32_t> fin(s->max_jobs);
     for (;;) {
+        // Clear the interrupt before looking at the queue: a request queued
+        // after this point sets it again and ends the next run early.
+        venu_batch_interrupt(s->batch, 0u);
+        {
+            const uint32_t pol = s->policy.load();
+            if (pol != s->applied_policy) {
+                venu_batch_set_policy(s->batch, pol);
+                s->applied_policy = pol;
+            }
+        }
         // admission, first come first served
         for (;;) {
             Request* R = nullptr;
@@ -407,7 +420,18 @@ extern "C" venu_status venu_server_submit(venu_server* s, const venu_request* re
     s->pending.push_back(id);
     ++s->submitted;
     s->cv_work.notify_all();
+    venu_batch_interrupt(s->batch, 1u);  // end the running step early: admit this request sooner
     if (request_id) *request_id = id;
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_server_set_policy(venu_server* s, uint32_t policy) {
+    if (!s || policy > VENU_POLICY_SHORTEST_FIRST) {
+        set_error("venu_server_set_policy: NULL server or unknown policy");
+        return VENU_ERR_INVALID;
+    }
+    s->policy.store(policy);
+    venu_batch_interrupt(s->batch, 1u);  // applied at the start of the next step
     return VENU_OK;
 }
 

@@ -13,6 +13,18 @@
 
 #include "../../include/venu.h"
 
+#ifndef VENU_MINMAX3
+#define VENU_MINMAX3 1
+#endif
+// Launch bounds of the fused traverse+shade kernels: at most 256 threads a
+// block, and VENU_TRACE_MINB (if set) resident 256-thread blocks per SM asked
+// of the register allocator (budget 65536 / (256 x VENU_TRACE_MINB)).
+#if defined(VENU_TRACE_MINB) && VENU_TRACE_MINB > 0
+#define VENU_TRACE_BOUNDS __launch_bounds__(256, VENU_TRACE_MINB)
+#else
+#define VENU_TRACE_BOUNDS __launch_bounds__(256)
+#endif
+
 namespace venu {
 
 // ---------------------------------------------------------------------------
@@ -179,6 +191,28 @@ __device__ __forceinline__ RayPre prep(f3 o, f3 d) {
     return R;
 }
 
+// Three-input min / max (one instruction on sm_100 and later).  The slab
+// test never feeds them a NaN (the direction guard keeps 1/d finite), and on
+// non-NaN inputs they equal the two-input chains exactly.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+#if VENU_MINMAX3
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+#if VENU_MINMAX3
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
+#endif
+}
+
 // Robust slab test: conservative by a relative 2^-20 plus an absolute slack
 // proportional to |o / d|, so rounding never drops a box the ray touches.
 __device__ __forceinline__ bool box_test(const RayPre& R, float4 lo, float4 hi, float tmin,
@@ -186,8 +220,8 @@ __device__ __forceinline__ bool box_test(const RayPre& R, float4 lo, float4 hi, 
     float t0x = fmaf(lo.x, R.inv.x, R.noi.x), t1x = fmaf(hi.x, R.inv.x, R.noi.x);
     float t0y = fmaf(lo.y, R.inv.y, R.noi.y), t1y = fmaf(hi.y, R.inv.y, R.noi.y);
     float t0z = fmaf(lo.z, R.inv.z, R.noi.z), t1z = fmaf(hi.z, R.inv.z, R.noi.z);
-    float tn = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), tmin));
-    float tf = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tcap));
+    float tn = fmax3(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fmin3(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fminf(fmaxf(t0z, t1z), tcap));
     tnear = tn;
     return tn <= fmaf(tf, 1.00000095367431640625f, R.slack);
 }
@@ -359,8 +393,8 @@ struct Tracer {
         if (!box_test(R, rlo, rhi, tmin, best_t, tn)) return false;
         cur = 0;
         // A tree has n-1 internal nodes and each step expands a different one;
-        // the guard and the index checks turn a corrupt tree into an error
-        // flag instead of a hang.
+        // the guard turns a cyclic (corrupt) tree into an error flag instead
+        // of a hang.
         guard = 2u * n + 8u;
         return true;
     }
@@ -369,18 +403,15 @@ struct Tracer {
     // kShared in shared memory.
     __device__ __forceinline__ bool step(const SceneView& S, StackSmem sm, uint32_t tid, uint32_t bdim,
                                          int* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
-        const uint32_t n = S.n;
-        if (--guard == 0u || (uint32_t)cur >= n - 1u) {
+        // Every word of the traversal records is in range (checked when the
+        // records are written), so only termination needs guarding here.
+        if (--guard == 0u) {
             overflow = true;
             return false;
         }
         const float4* T = S.trav + 4 * (size_t)cur;
         const float4 a0 = __ldg(T), b0 = __ldg(T + 1), a1 = __ldg(T + 2), b1 = __ldg(T + 3);
         const int32_t w0 = __float_as_int(a0.w), w1 = __float_as_int(a1.w);
-        if (((w0 & kLeaf) && (uint32_t)(w0 & kSlotMask) >= n) || ((w1 & kLeaf) && (uint32_t)(w1 & kSlotMask) >= n)) {
-            overflow = true;
-            return false;
-        }
         bool h0 = false, h1 = false;
         float tn0 = 0.0f, tn1 = 0.0f;
         if (w0 & kLeaf) {

@@ -32,6 +32,7 @@ struct venu_scene {
     float4* mat = nullptr;
     uint32_t* meta = nullptr;  // original id | material << 30
     uint32_t* keys = nullptr;  // sorted Morton codes
+    int32_t* parents = nullptr;  // [n-1] parent of each internal node, then [n] of each leaf (for refits)
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     uint32_t nhoist = 0;          // huge spheres tested before traversal
     int32_t hoist[4] = {0, 0, 0, 0};
@@ -43,4 +44,7 @@ namespace venu {
 // Builds the LBVH for `n` device spheres into `s` (allocates its buffers).
 venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t stream, venu_scene* s);
 void free_scene(venu_scene* s);
+// Moves the scene's spheres to `spheres_dev` (same count, original order) and
+// refits the boxes on `stream` (asynchronous).
+venu_status update_scene(venu_scene* s, const venu_sphere* spheres_dev, cudaStream_t stream);
 }  // namespace venu
