@@ -217,12 +217,14 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
     }
 
 
-def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=16 << 20, iters=64):
+def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=16 << 20, iters=64,
+               express_paths=4 << 20):
     """Serving: a Poisson request stream at ~80 % of the server's capacity;
-    the render server (continuous batching, resident BVHs, 150 GB HBM budget;
-    FIFO and shortest-first plan order) against the plain method serving the
-    same stream one job at a time.  All scenes are resident before the
-    streams start, for every method."""
+    the render server (continuous batching, resident BVHs, 150 GB HBM budget)
+    with one lane in FIFO and in shortest-first plan order, and with the
+    express lane for requests of at most 4 Mi paths, against the plain method
+    serving the same stream one job at a time.  All scenes are resident
+    before the streams start, for every method."""
     import threading
 
     from venusaur_gb300 import workloads
@@ -289,9 +291,13 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
                 "failed": int(sum(r["status"] != 0 for r in res))}, segs
 
     out = {}
-    for name, sf in (("server_fifo", False), ("server_shortest_first", True)):
+    for name, sf, xp in (("server_fifo", False, 0), ("server_shortest_first", True, 0),
+                         ("server_express", False, express_paths)):
         srv.set_policy(sf)
+        srv.set_express(xp)
         out[name], segs = stream()
+        if xp:
+            out[name]["express_paths"] = xp
     srv.close()
 
     # the plain method: one job at a time, same arrivals, resident BVHs

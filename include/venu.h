@@ -321,8 +321,8 @@ VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* f
 #define VENU_POLICY_SHORTEST_FIRST 1u
 VENU_API venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy);
 /* Sets (on != 0) or clears a flag in mapped host memory that the device loop
- * reads once per iteration pair: while set, a running venu_batch_run ends at
- * its next iteration boundary (and later runs after one iteration pair), so
+ * reads once per iteration: while set, a running venu_batch_run ends at its
+ * next iteration boundary (and later runs after one iteration), so
  * a host with new jobs can admit them without waiting for the run.  The only
  * batch call that may be made from another host thread. */
 VENU_API venu_status venu_batch_interrupt(venu_batch* b, uint32_t on);
@@ -387,6 +387,12 @@ VENU_API venu_status venu_server_submit(venu_server* s, const venu_request* req,
  * VENU_POLICY_SHORTEST_FIRST; see venu_batch_set_policy); admission stays
  * first come first served.  Takes effect at the server's next step. */
 VENU_API venu_status venu_server_set_policy(venu_server* s, uint32_t policy);
+/* Express lane: requests of at most max_paths paths (width x height x spp)
+ * admitted from now on run in a second, small pool (2 Mi paths) that the
+ * server advances ahead of the bulk pool at every step; 0 (the default)
+ * turns it off.  A small request then waits for at most one iteration of
+ * the bulk pool instead of sharing every bounce with the large jobs. */
+VENU_API venu_status venu_server_set_express(venu_server* s, uint64_t max_paths);
 /* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY). */
 VENU_API venu_status venu_server_wait(venu_server* s, uint64_t request_id, double timeout_s, venu_result* out);
 VENU_API venu_status venu_server_cancel(venu_server* s, uint64_t request_id);

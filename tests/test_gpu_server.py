@@ -102,3 +102,21 @@ def test_server_shortest_first(venu, oracle, cuda):
     r = srv.wait(srv.submit(small[1], 12, 8, 1, spheres=small[0], max_depth=6))
     assert r["status"] == 0
     srv.close()
+
+
+def test_server_express_lane(venu, oracle, cuda):
+    """Requests at or below the express threshold run in the second pool;
+    every image is the same as the oracle's whichever lane rendered it."""
+    srv = venu.Server(hbm_budget_bytes=1 << 30, pool_paths=3000, max_jobs=8, iterations_per_step=64,
+                      express_paths=12 * 8 * 2)
+    cases = [(_case(oracle, 0, 48, 32, 6), (48, 32, 6)), (_case(oracle, 1, 12, 8, 2), (12, 8, 2)),
+             (_case(oracle, 2, 40, 24, 4), (40, 24, 4)), (_case(oracle, 3, 12, 8, 1), (12, 8, 1))]
+    ids = [srv.submit(c[1], *wh, spheres=c[0], max_depth=6) for c, wh in cases]
+    for rid, (c, _) in zip(ids, cases):
+        r = srv.wait(rid)
+        assert r["status"] == 0
+        assert np.abs(r["image"].astype(int) - c[2]["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    st = srv.stats()
+    assert st["completed"] == 4 and st["failed"] == 0
+    assert st["segments"] == sum(c[2]["segments"] for c, _ in cases)
+    srv.close()

@@ -592,13 +592,19 @@ class Server:
     rendered together in one shared path pool by the server's own thread."""
 
     def __init__(self, hbm_budget_bytes: int, pool_paths: int = 0, max_jobs: int = 64,
-                 iterations_per_step: int = 8, shortest_first: bool = False):
+                 iterations_per_step: int = 8, shortest_first: bool = False, express_paths: int = 0):
         h = C.c_void_p()
         check(lib().venu_server_create(int(hbm_budget_bytes), pool_paths, max_jobs, iterations_per_step,
                                        C.byref(h)))
         self.handle = h
         if shortest_first:
             self.set_policy(True)
+        if express_paths:
+            self.set_express(express_paths)
+
+    def set_express(self, max_paths: int) -> None:
+        """Requests of at most max_paths paths run in the express lane (0: off)."""
+        check(lib().venu_server_set_express(self.handle, int(max_paths)))
 
     def set_policy(self, shortest_first: bool) -> None:
         pol = _lib.POLICY_SHORTEST_FIRST if shortest_first else _lib.POLICY_FIFO

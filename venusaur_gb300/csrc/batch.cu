@@ -9,12 +9,14 @@
 //                survivors compacted into the other queue (the job index
 //                rides in the upper bits of the depth word);
 //   plan         one thread hands the free queue slots to the admitted jobs
-//                in submission order (oldest first);
+//                in plan order (submission order, or shortest first);
 //   regen        new camera rays for the planned (job, sample, pixel)
 //                triples, from each job's precomputed raygen seed table;
 //
 // repeated under a device-side while condition, so the whole loop is one
-// CUDA graph launch.  Paths finish into per-job sample slots; a job whose
+// CUDA graph launch.  Which of the two queues is the input alternates each
+// iteration through a parity word in device memory, so one iteration is one
+// pass of the loop body and a run can end after any iteration.  Paths finish into per-job sample slots; a job whose
 // paths are all done is accumulated (Kahan, sample order) and resolved by
 // venu_batch_collect.  The seed table holds, for every (sample, pixel), the
 // raygen RNG state at the start of that sample (Core/RayTracer.cu:169-177),
@@ -42,6 +44,8 @@ struct LoopCtl {  // device-owned loop state
     uint32_t cnt[2], work[2];
     uint32_t iter, running, more_gen, take_total, out_base, plan_n, err;
     uint32_t job_finished;  // set when a job's last path finishes (reset per run)
+    uint32_t parity;        // the queue traced in this iteration; flipped by k_loop_cond
+    uint32_t pad;
     unsigned long long segments, paths_done, iterations;
 };
 
@@ -76,9 +80,9 @@ __global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t s
 __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
                        const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
                        uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
-                       uint32_t* __restrict__ plan_off, uint32_t Q, int out) {
+                       uint32_t* __restrict__ plan_off, uint32_t Q) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int in = 1 - out;
+    const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const uint32_t survivors = ctl->cnt[out];
     const uint32_t free = survivors < Q ? Q - survivors : 0u;
     const uint32_t na = run->nactive;
@@ -107,8 +111,9 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
 
 __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restrict__ ctl,
                         const uint32_t* __restrict__ plan_job, const unsigned long long* __restrict__ plan_start,
-                        const uint32_t* __restrict__ plan_off, Queue q) {
+                        const uint32_t* __restrict__ plan_off, Queue q0, Queue q1) {
     const uint32_t total = ctl->take_total, base = ctl->out_base, np = ctl->plan_n;
+    const Queue q = (ctl->parity & 1u) ? q0 : q1;  // the output queue of this iteration
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         // last plan entry i with plan_off[i] <= t (entries may be empty)
         uint32_t lo = 0, hi = np;  // invariant: plan_off[lo] <= t < plan_off[hi]
@@ -132,12 +137,13 @@ __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restri
 template <bool COUNT>
 __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
                                                            unsigned long long* __restrict__ job_done, LoopCtl* ctl,
-                                                           Queue qin, Queue qout, int in) {
+                                                           Queue q0, Queue q1) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
     sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
-    const int out = 1 - in;
+    const int in = (int)(ctl->parity & 1u), out = 1 - in;
+    const Queue qin = in ? q1 : q0, qout = in ? q0 : q1;
     const uint32_t n = ctl->cnt[in];
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctl->segments, (unsigned long long)n);
@@ -185,14 +191,16 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
 }
 
 // interrupt: a word in mapped host memory (venu_batch_interrupt), read once
-// per iteration pair; volatile so every read goes to the host's copy.
+// per iteration; volatile so every read goes to the host copy.
 __global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, const volatile uint32_t* interrupt,
                             cudaGraphConditionalHandle handle, int use_handle) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const uint32_t it = ctl->iter + 2u;
+    const uint32_t it = ctl->iter + 1u;
     ctl->iter = it;
-    ctl->iterations += 2u;
-    uint32_t more = (ctl->cnt[0] > 0u || ctl->more_gen) ? 1u : 0u;
+    ctl->iterations += 1u;
+    const uint32_t next = (ctl->parity & 1u) ^ 1u;  // the queue the next iteration traces
+    ctl->parity = next;
+    uint32_t more = (ctl->cnt[next] > 0u || ctl->more_gen) ? 1u : 0u;
     if (run->max_iter && it >= run->max_iter) more = 0u;
     if (run->stop_on_finish && ctl->job_finished) more = 0u;  // hand finished jobs to the host now
     if (*interrupt) more = 0u;                                 // the host has new work to admit
@@ -289,18 +297,16 @@ cudaError_t batch_configure(venu_batch* b) {
     return cudaSuccess;
 }
 
-// One iteration pair of the path loop (queue 0 -> 1 -> 0) + the condition.
+// One iteration of the path loop (trace the parity queue, plan, regenerate
+// into the other) + the condition, which flips the parity.
 cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
     const size_t sm = traverse_smem((int)b->tune.traverse_block);
-    for (int in = 0; in < 2; ++in) {
-        const int out = 1 - in;
-        k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
-                                                                                      b->q[in], b->q[out], in);
-        k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
-                                 b->d_plan_start, b->d_plan_off, b->Q, out);
-        k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
-                                                 b->q[out]);
-    }
+    k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
+                                                                                  b->q[0], b->q[1]);
+    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_order, b->d_run, b->d_ctl, b->d_plan_job, b->d_plan_start,
+                             b->d_plan_off, b->Q);
+    k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
+                                             b->q[0], b->q[1]);
     k_loop_cond<<<1, 32, 0, st>>>(b->d_ctl, b->d_run, b->d_interrupt, b->handle, use_handle ? 1 : 0);
     return cudaGetLastError();
 }

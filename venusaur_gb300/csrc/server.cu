@@ -3,11 +3,18 @@
 // One host thread per server.  Requests are queued first-come first-served
 // and admitted while their device memory (scene BVH unless already resident,
 // the job's seed table and sample slots, accumulator and image) fits the HBM
-// budget; admitted jobs advance together in the shared path pool a few
+// budget; admitted jobs advance together in a shared path pool a few
 // iterations per step; finished jobs are collected, their images copied to
 // host memory and their buffers released.  Scene BVHs stay resident across
 // requests with the same scene_key and are evicted least-recently-used when
 // the budget needs room.
+//
+// Two lanes, each its own venu_batch: requests of at most express_paths
+// paths (when set) go to a small express pool, the rest to the bulk pool.
+// Each step runs the express lane first when it has work, then the bulk
+// lane; a submit interrupts the running step at its next iteration, so a
+// small request waits for at most one bulk iteration instead of sharing
+// every bounce with the large jobs in the bulk pool.
 #include "venu_internal.h"
 
 #include <algorithm>
@@ -42,6 +49,7 @@ struct Request {
     std::vector<uint8_t> image;
     // while admitted
     uint64_t scene_key = 0;
+    int lane = 0;
     float* accum = nullptr;
     uint8_t* image8 = nullptr;
     uint64_t job_bytes = 0;
@@ -55,6 +63,7 @@ struct SceneEntry {
 };
 
 constexpr uint64_t kPrivateKey = 1ull << 63;  // scenes of requests without a key
+constexpr uint32_t kExpressPool = 2u << 20;    // paths in flight in the express lane
 
 uint64_t scene_estimate(uint32_t n) { return (uint64_t)n * 72u + 256u; }
 uint64_t image_bytes(const venu_render_opts& o) {
@@ -86,13 +95,17 @@ struct venu_server {
     std::atomic<uint32_t> policy{VENU_POLICY_FIFO};  // plan order, applied by the server thread
     uint32_t applied_policy = VENU_POLICY_FIFO;
 
+    std::atomic<uint64_t> express_paths{0};  // 0: one lane
     // owned by the server thread
     std::thread th;
-    venu_batch* batch = nullptr;
+    venu_batch* batch = nullptr;    // bulk lane
+    venu_batch* express = nullptr;  // express lane
     cudaStream_t st = nullptr;
     std::unordered_map<uint64_t, SceneEntry> scenes;
-    std::unordered_map<uint32_t, uint64_t> active;  // batch job id -> request id
+    std::unordered_map<uint32_t, uint64_t> active[2];  // per lane: batch job id -> request id
     uint64_t resident = 0, use_clock = 0;
+    size_t n_active_all() const { return active[0].size() + active[1].size(); }
+    venu_batch* lane(int l) const { return l ? express : batch; }
 };
 
 namespace {
@@ -191,6 +204,9 @@ void admit(venu_server* s, Request& R) {
         complete(s, R, VENU_ERR_OOM);
         return;
     }
+    const uint64_t paths = (uint64_t)o.width * o.height * o.samples_per_pixel;
+    const uint64_t xp = s->express_paths.load();
+    R.lane = (xp && paths <= xp) ? 1 : 0;
     venu_job_desc d{};
     d.scene = it->second.scene;
     d.camera = R.req.camera;
@@ -199,7 +215,7 @@ void admit(venu_server* s, Request& R) {
     d.accum = R.accum;
     d.image8 = R.image8;
     uint32_t jid = 0;
-    venu_status bs = venu_batch_submit(s->batch, &d, s->st, &jid);
+    venu_status bs = venu_batch_submit(s->lane(R.lane), &d, s->st, &jid);
     if (bs != VENU_OK) {
         cudaFreeAsync(R.accum, s->st);
         cudaFreeAsync(R.image8, s->st);
@@ -212,21 +228,59 @@ void admit(venu_server* s, Request& R) {
     R.scene_key = key;
     R.job_bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel) + image_bytes(o);
     s->resident += R.job_bytes;
-    s->active[jid] = R.id;
+    s->active[R.lane][jid] = R.id;
     std::lock_guard<std::mutex> lock(s->mu);
     R.t_admit = seconds_since(s->t0);
 }
 
 void fail_all_active(venu_server* s, venu_status st) {
-    for (auto& kv : s->active) {
+    for (auto& act : s->active) {
+        for (auto& kv : act) {
+            Request* R;
+            {
+                std::lock_guard<std::mutex> lock(s->mu);
+                R = s->reqs[kv.second].get();
+            }
+            complete(s, *R, st);
+        }
+        act.clear();
+    }
+}
+
+// One step of one lane: run (ends when a job finishes, after max_iter
+// iterations, or at an interrupt), collect, hand finished images back.
+venu_status run_lane(venu_server* s, int l, uint32_t max_iter, std::vector<uint32_t>& fin) {
+    venu_batch* b = s->lane(l);
+    venu_status rs = venu_batch_run(b, max_iter, VENU_RUN_STOP_ON_FINISH, s->st);
+    uint32_t nfin = 0;
+    if (rs == VENU_OK) rs = venu_batch_collect(b, s->st, fin.data(), (uint32_t)fin.size(), &nfin);
+    if (rs != VENU_OK) return rs;
+    std::vector<Request*> done;
+    for (uint32_t i = 0; i < nfin; ++i) {
+        auto it = s->active[l].find(fin[i]);
+        if (it == s->active[l].end()) continue;
         Request* R;
         {
             std::lock_guard<std::mutex> lock(s->mu);
-            R = s->reqs[kv.second].get();
+            R = s->reqs[it->second].get();
         }
-        complete(s, *R, st);
+        s->active[l].erase(it);
+        const uint64_t npix = (uint64_t)R->req.opts.width * R->req.opts.height;
+        R->image.resize(npix * 4u);
+        cudaMemcpyAsync(R->image.data(), R->image8, npix * 4u, cudaMemcpyDeviceToHost, s->st);
+        done.push_back(R);
     }
-    s->active.clear();
+    cudaError_t ce = cudaStreamSynchronize(s->st);
+    for (Request* R : done) {
+        cudaFreeAsync(R->accum, s->st);
+        cudaFreeAsync(R->image8, s->st);
+        R->accum = nullptr;
+        R->image8 = nullptr;
+        s->resident -= R->job_bytes;
+        release_scene(s, R->scene_key);
+        complete(s, *R, ce == cudaSuccess ? VENU_OK : VENU_ERR_CUDA);
+    }
+    return VENU_OK;
 }
 
 void server_loop(venu_server* s) {
@@ -236,10 +290,12 @@ void server_loop(venu_server* s) {
         // Clear the interrupt before looking at the queue: a request queued
         // after this point sets it again and ends the next run early.
         venu_batch_interrupt(s->batch, 0u);
+        venu_batch_interrupt(s->express, 0u);
         {
             const uint32_t pol = s->policy.load();
             if (pol != s->applied_policy) {
                 venu_batch_set_policy(s->batch, pol);
+                venu_batch_set_policy(s->express, pol);
                 s->applied_policy = pol;
             }
         }
@@ -273,7 +329,7 @@ void server_loop(venu_server* s) {
                 continue;
             }
             if (s->resident + need > s->budget) evict_for(s, need);
-            if (s->resident + need > s->budget || s->active.size() >= s->max_jobs) break;  // wait for room
+            if (s->resident + need > s->budget || s->n_active_all() >= s->max_jobs) break;  // wait for room
             {
                 std::lock_guard<std::mutex> lock(s->mu);
                 s->pending.pop_front();
@@ -282,10 +338,10 @@ void server_loop(venu_server* s) {
         }
         {
             std::lock_guard<std::mutex> lock(s->mu);
-            s->n_active = (uint32_t)s->active.size();
+            s->n_active = (uint32_t)s->n_active_all();
             s->resident_shared = s->resident;
         }
-        if (s->active.empty()) {
+        if (s->n_active_all() == 0) {
             std::unique_lock<std::mutex> lock(s->mu);
             if (s->stop) break;
             if (s->pending.empty()) s->cv_work.wait_for(lock, std::chrono::milliseconds(20));
@@ -293,9 +349,14 @@ void server_loop(venu_server* s) {
             continue;
         }
         const Clock::time_point tb = Clock::now();
-        venu_status rs = venu_batch_run(s->batch, s->iters, VENU_RUN_STOP_ON_FINISH, s->st);
-        uint32_t nfin = 0;
-        if (rs == VENU_OK) rs = venu_batch_collect(s->batch, s->st, fin.data(), (uint32_t)fin.size(), &nfin);
+        // The express lane first.  The bulk lane gets one iteration per step
+        // while express work remains (so small requests wait at most one bulk
+        // iteration, and a stream of them cannot stall the bulk lane), and
+        // up to `iters` when there is none.
+        venu_status rs = VENU_OK;
+        const bool express_work = !s->active[1].empty();
+        if (express_work) rs = run_lane(s, 1, s->iters, fin);
+        if (rs == VENU_OK && !s->active[0].empty()) rs = run_lane(s, 0, express_work ? 1u : s->iters, fin);
         if (rs != VENU_OK) {
             std::string msg = venu_last_error();
             fail_all_active(s, rs);
@@ -305,37 +366,13 @@ void server_loop(venu_server* s) {
             s->stop = true;
             break;
         }
-        std::vector<Request*> done;
-        for (uint32_t i = 0; i < nfin; ++i) {
-            auto it = s->active.find(fin[i]);
-            if (it == s->active.end()) continue;
-            Request* R;
-            {
-                std::lock_guard<std::mutex> lock(s->mu);
-                R = s->reqs[it->second].get();
-            }
-            s->active.erase(it);
-            const uint64_t npix = (uint64_t)R->req.opts.width * R->req.opts.height;
-            R->image.resize(npix * 4u);
-            cudaMemcpyAsync(R->image.data(), R->image8, npix * 4u, cudaMemcpyDeviceToHost, s->st);
-            done.push_back(R);
-        }
-        cudaError_t ce = cudaStreamSynchronize(s->st);
-        for (Request* R : done) {
-            cudaFreeAsync(R->accum, s->st);
-            cudaFreeAsync(R->image8, s->st);
-            R->accum = nullptr;
-            R->image8 = nullptr;
-            s->resident -= R->job_bytes;
-            release_scene(s, R->scene_key);
-            complete(s, *R, ce == cudaSuccess ? VENU_OK : VENU_ERR_CUDA);
-        }
-        venu_batch_stats bst{};
+        venu_batch_stats bst{}, bsx{};
         venu_batch_stats_get(s->batch, &bst);
+        venu_batch_stats_get(s->express, &bsx);
         std::lock_guard<std::mutex> lock(s->mu);
         s->busy += seconds_since(tb);
-        s->segments = bst.segments;
-        if (s->stop && s->active.empty()) break;
+        s->segments = bst.segments + bsx.segments;
+        if (s->stop && s->n_active_all() == 0) break;
     }
     // shut down: fail what is left
     fail_all_active(s, VENU_ERR_CANCELLED);
@@ -381,8 +418,15 @@ extern "C" venu_status venu_server_create(uint64_t hbm_budget_bytes, uint32_t po
         delete s;
         return bs;
     }
+    bs = venu_batch_create(kExpressPool, max_jobs, 0, &s->express);
+    if (bs != VENU_OK) {
+        venu_batch_destroy(s->batch);
+        delete s;
+        return bs;
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
+        venu_batch_destroy(s->express);
         venu_batch_destroy(s->batch);
         delete s;
         return cuda_fail(e, "venu_server_create");
@@ -421,6 +465,7 @@ extern "C" venu_status venu_server_submit(venu_server* s, const venu_request* re
     ++s->submitted;
     s->cv_work.notify_all();
     venu_batch_interrupt(s->batch, 1u);  // end the running step early: admit this request sooner
+    venu_batch_interrupt(s->express, 1u);
     if (request_id) *request_id = id;
     return VENU_OK;
 }
@@ -432,6 +477,15 @@ extern "C" venu_status venu_server_set_policy(venu_server* s, uint32_t policy) {
     }
     s->policy.store(policy);
     venu_batch_interrupt(s->batch, 1u);  // applied at the start of the next step
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_server_set_express(venu_server* s, uint64_t max_paths) {
+    if (!s) {
+        set_error("venu_server_set_express: NULL server");
+        return VENU_ERR_INVALID;
+    }
+    s->express_paths.store(max_paths);  // requests admitted from now on
     return VENU_OK;
 }
 
@@ -543,6 +597,7 @@ extern "C" venu_status venu_server_destroy(venu_server* s) {
     }
     if (s->th.joinable()) s->th.join();
     venu_batch_destroy(s->batch);
+    venu_batch_destroy(s->express);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return VENU_OK;
