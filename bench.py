@@ -217,19 +217,18 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
     }
 
 
-def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, pool_paths=16 << 20, iters=64,
-               express_paths=4 << 20):
-    """Serving: a Poisson request stream at ~80 % of the server's capacity;
-    the render server (continuous batching, resident BVHs, 150 GB HBM budget)
-    with one lane in FIFO and in shortest-first plan order, and with the
-    express lane for requests of at most 4 Mi paths, against the plain method
-    serving the same stream one job at a time.  All scenes are resident
-    before the streams start, for every method."""
+def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, iters=64):
+    """Serving: a Poisson request stream at ~80 % of the server's capacity
+    through the render server (continuous batching, resident BVHs, 150 GB HBM
+    budget) in two configurations -- one lane, FIFO, 16 Mi-path pool; and an
+    express lane for requests of at most 4 Mi paths ahead of a sequential
+    8 Mi-path bulk lane -- against the plain method serving the same stream
+    one job at a time.  All scenes are resident before each stream starts,
+    for every method."""
     import threading
 
     from venusaur_gb300 import workloads
 
-    srv = venu.Server(budget, pool_paths=pool_paths, max_jobs=256, iterations_per_step=iters)
     scenes = {}
 
     def skey(j):
@@ -243,31 +242,43 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     def cam_of(j):
         return venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
 
-    keys = {}
+    class Client:
+        def __init__(self, srv):
+            self.srv, self.keys = srv, {}
 
-    def submit(j):
-        k = keys.get(skey(j))
-        if k is None:
-            k = keys[skey(j)] = 1 + len(keys)
-            return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=spheres_of(j), scene_key=k,
-                              max_depth=j["depth"])
-        return srv.submit(cam_of(j), j["W"], j["H"], j["spp"], scene_key=k, max_depth=j["depth"])
+        def submit(self, j):
+            k = self.keys.get(skey(j))
+            if k is None:
+                k = self.keys[skey(j)] = 1 + len(self.keys)
+                return self.srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=spheres_of(j), scene_key=k,
+                                       max_depth=j["depth"])
+            return self.srv.submit(cam_of(j), j["W"], j["H"], j["spp"], scene_key=k, max_depth=j["depth"])
 
-    # capacity: a burst of requests all at once (FIFO)
+        def warm(self, jobs):  # every scene resident
+            for j in jobs:
+                self.srv.wait(self.submit(dict(j, W=16, H=16, spp=1)))
+
+    # capacity: a burst of requests all at once through the one-lane server
+    srv = venu.Server(budget, pool_paths=16 << 20, max_jobs=256, iterations_per_step=iters)
+    cl = Client(srv)
     calib = workloads.serving_jobs(24, rate_per_s=1.0, seed=2)
-    for j in calib:  # scenes resident first
-        srv.wait(submit(dict(j, W=16, H=16, spp=1)))
+    cl.warm(calib)
     t0 = time.perf_counter()
-    ids = [submit(j) for j in calib]
+    ids = [cl.submit(j) for j in calib]
     for i in ids:
         assert srv.wait(i)["status"] == 0
     cap_jobs_per_s = len(calib) / (time.perf_counter() - t0)
     lam = util * cap_jobs_per_s
     jobs = workloads.serving_jobs(n_requests, rate_per_s=lam, seed=3)
-    for j in jobs:
-        srv.wait(submit(dict(j, W=16, H=16, spp=1)))
+    small = np.array([j["W"] * j["H"] * j["spp"] <= (4 << 20) for j in jobs])
 
-    def stream():
+    def split(lat):
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "p50_ms_small": float(np.percentile(lat[small], 50)),
+                "p50_ms_large": float(np.percentile(lat[~small], 50))}
+
+    def stream(cl):
+        srv = cl.srv
         seg0 = srv.stats()["segments"]
         ids = [None] * len(jobs)
         start = time.perf_counter()
@@ -277,7 +288,7 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
                 dt = start + j["arrival"] - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
-                ids[k] = submit(j)
+                ids[k] = cl.submit(j)
 
         th = threading.Thread(target=client)
         th.start()
@@ -286,18 +297,23 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
         makespan = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
         lat = np.array([r["latency_ms"] for r in res])
         segs = srv.stats()["segments"] - seg0
-        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "value": segs / makespan, "unit": UNIT, "makespan_s": makespan,
-                "failed": int(sum(r["status"] != 0 for r in res))}, segs
+        out = split(lat)
+        out.update({"value": segs / makespan, "unit": UNIT, "makespan_s": makespan,
+                    "failed": int(sum(r["status"] != 0 for r in res))})
+        return out, segs
 
     out = {}
-    for name, sf, xp in (("server_fifo", False, 0), ("server_shortest_first", True, 0),
-                         ("server_express", False, express_paths)):
-        srv.set_policy(sf)
-        srv.set_express(xp)
-        out[name], segs = stream()
-        if xp:
-            out[name]["express_paths"] = xp
+    cl.warm(jobs)
+    out["server_fifo"], segs = stream(cl)
+    out["server_fifo"]["config"] = "one lane, FIFO plan order, 16 Mi-path pool"
+    srv.close()
+    srv = venu.Server(budget, pool_paths=8 << 20, max_jobs=256, iterations_per_step=iters, express_paths=4 << 20)
+    srv.set_policy("sequential")
+    cl = Client(srv)
+    cl.warm(jobs)
+    out["server_express"], segs = stream(cl)
+    out["server_express"]["config"] = ("express lane (2 Mi-path pool) for requests of <= 4 Mi paths, "
+                                       "sequential bulk lane with an 8 Mi-path pool")
     srv.close()
 
     # the plain method: one job at a time, same arrivals, resident BVHs
@@ -321,13 +337,13 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
         plain_lat.append(1000.0 * (tfree - j["arrival"]))
     plat = np.array(plain_lat)
     plain_makespan = tfree - jobs[0]["arrival"]
-    out["plain"] = {"p50_ms": float(np.percentile(plat, 50)), "p99_ms": float(np.percentile(plat, 99)),
-                    "value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
-                    "method": "venu_render one job at a time (FIFO), same arrivals"}
+    out["plain"] = split(plat)
+    out["plain"].update({"value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
+                         "method": "venu_render one job at a time (FIFO), same arrivals"})
     out["workload"] = (f"{n_requests} requests, Poisson arrivals at {lam:.2f}/s (~{int(100 * util)} % of the "
                        f"server's measured capacity {cap_jobs_per_s:.2f} jobs/s), scenes from 16 resident scenes "
                        "with 100..200000 spheres, resolutions {256x256, 512x512, 640x360, 1024x1024}, spp "
-                       f"{{8, 16, 32, 64, 128}}, depth 50, HBM budget 150 GB, pool {pool_paths >> 20} Mi paths")
+                       "{8, 16, 32, 64, 128}, depth 50, HBM budget 150 GB; small = at most 4 Mi paths")
     return out
 
 
@@ -396,6 +412,17 @@ def main():
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     spheres = make_scene(venu, cfg["scene"])
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    # CPU baseline first, on an idle host (rank 0, single process only): the
+    # oracle port on a bounded row sample of the same workload, every core.
+    cpu_baseline = None
+    if not args.no_cpu and world == 1:
+        from oracle import pyoracle
+
+        pyoracle.build()
+        O = pyoracle.Oracle()
+        nt = os.cpu_count() or 1
+        rate, dt, sample, _ = cpu_sample(O, spheres, cam, cfg, nt)
+        cpu_baseline = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample, "seconds": dt}
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
@@ -468,20 +495,19 @@ def main():
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
     segs_c, paths_c = sc["segments"], sc["paths"]
     fused = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"]) == 2
-    # Algorithmic bytes of the dominant kernel per render.  Traversal: each
-    # step reads one 64-byte record holding both children of a node (box or
-    # inline sphere each), i.e. 32 B per child tested, box or sphere; 32 B ray
-    # read.  Separate traversal kernel: + 8 B hit write.  Fused
-    # traverse+shade kernel: + 16 B throughput/seed read, 36 B
-    # sphere+material+meta read, 48 B continuation write per continuing
-    # segment, 16 B radiance slot per finished path.
-    trav_bytes = (nodes + sph) * 32 + segs_c * 32
+    # Algorithmic bytes of the dominant kernel per render, by the per-segment
+    # figure: 32 B per node (box) tested + 16 B per sphere tested + the ray
+    # state queue traffic: 112 B per segment for the fused traverse+shade
+    # kernel (28 B ray write + read, 12 B hit write + read, 16 B
+    # throughput/seed/pixel read + write), 40 B for the separate traversal
+    # kernel (28 B ray read, 12 B hit write).
+    trav_bytes = nodes * 32 + sph * 16
     if fused:
         kernel = "k_trace_shade"
-        kbytes = trav_bytes + segs_c * (16 + 36) + (segs_c - paths_c) * 48 + paths_c * 16
+        kbytes = trav_bytes + segs_c * 112
     else:
         kernel = "k_traverse"
-        kbytes = trav_bytes + segs_c * 8
+        kbytes = trav_bytes + segs_c * 40
     per_launch_bytes = kbytes / max(1, st["traverse_launches"])
     avg_launch_ms = st["traverse_ms"] / max(1, st["traverse_launches"])
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
@@ -566,15 +592,8 @@ def main():
         line["batched"] = run_batched(venu, torch, tuning, max_paths)
         line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True)
         line["served"] = run_served(venu, torch, tuning)
-    if not args.no_cpu:
-        from oracle import pyoracle
-
-        pyoracle.build()
-        O = pyoracle.Oracle()
-        nt = os.cpu_count() or 1
-        rate, dt, sample, _ = cpu_sample(O, spheres, cam, cfg, nt)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample,
-                                "seconds": dt}
+    if cpu_baseline is not None:
+        line["cpu_baseline"] = cpu_baseline
     print(json.dumps(line), flush=True)
 
 

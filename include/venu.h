@@ -315,10 +315,14 @@ VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* f
  * first.  FIFO (default): submission order.  SHORTEST_FIRST: fewest
  * unfinished paths first (as of the last collect; ties by submission) --
  * small jobs overtake large ones, which lowers typical latency; a steady
- * stream of small jobs can delay a large one indefinitely.  Results do not
- * depend on the order. */
+ * stream of small jobs can delay a large one indefinitely.  SEQUENTIAL:
+ * submission order, and a job gets slots only once every earlier job has
+ * finished all its paths (no overlap: a job's last bounces are not slowed
+ * by the next job's rays; the pool runs part-empty meanwhile).  Results do
+ * not depend on the order. */
 #define VENU_POLICY_FIFO 0u
 #define VENU_POLICY_SHORTEST_FIRST 1u
+#define VENU_POLICY_SEQUENTIAL 2u
 VENU_API venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy);
 /* Sets (on != 0) or clears a flag in mapped host memory that the device loop
  * reads once per iteration: while set, a running venu_batch_run ends at its
@@ -383,8 +387,9 @@ typedef struct venu_server_stats {
 VENU_API venu_status venu_server_create(uint64_t hbm_budget_bytes, uint32_t pool_paths, uint32_t max_jobs,
                                         uint32_t iterations_per_step, venu_server** out);
 VENU_API venu_status venu_server_submit(venu_server* s, const venu_request* req, uint64_t* request_id);
-/* Plan order of the admitted requests (VENU_POLICY_FIFO, the default, or
- * VENU_POLICY_SHORTEST_FIRST; see venu_batch_set_policy); admission stays
+/* Plan order of the bulk lane (VENU_POLICY_FIFO, the default,
+ * VENU_POLICY_SHORTEST_FIRST or VENU_POLICY_SEQUENTIAL; see
+ * venu_batch_set_policy); the express lane is always FIFO and admission
  * first come first served.  Takes effect at the server's next step. */
 VENU_API venu_status venu_server_set_policy(venu_server* s, uint32_t policy);
 /* Express lane: requests of at most max_paths paths (width x height x spp)

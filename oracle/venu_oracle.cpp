@@ -290,6 +290,178 @@ void refit_bvh(Bvh& B) {
     B.depth = maxdepth;
 }
 
+// Treelet restructuring: one bottom-up pass over the Karras tree after the
+// refit (Karras & Aila, "Fast Parallel Construction of High-Quality Bounding
+// Volume Hierarchies", HPG 2013).  At every internal node N (children before
+// parents) a treelet of up to 7 leaves is grown from N's two children by
+// repeatedly opening the internal treelet leaf with the largest surface area
+// (first such on ties); a dynamic program over all subsets of the treelet
+// leaves finds the binary topology with the least total internal surface
+// area, and the treelet is rewired that way when that is strictly less than
+// its current total.  The leaves keep their Morton slots; N stays the
+// treelet root; its internal nodes are reused in the order they were opened,
+// handed out in depth-first order of the new topology.  Mirrors
+// k_treelets in lbvh.cu operation for operation.
+struct TBox {
+    float lo[3], hi[3];
+};
+float tbox_area(const TBox& b) {
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return 2.0f * ((dx * dy + dy * dz) + dz * dx);
+}
+TBox tbox_of(const Bvh& B, int32_t c) {
+    TBox b;
+    if (c & kLeaf) {
+        const int k = c & kSlotMask;
+        const float r = std::fabs(B.radius[k]);
+        const float cc[3] = {B.center[k].x, B.center[k].y, B.center[k].z};
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = sub_rd(cc[a], r);
+            b.hi[a] = add_ru(cc[a], r);
+        }
+    } else {
+        for (int a = 0; a < 3; ++a) {
+            b.lo[a] = B.nodes[c].lo[a];
+            b.hi[a] = B.nodes[c].hi[a];
+        }
+    }
+    return b;
+}
+
+void restructure_treelet(Bvh& B, int32_t N, std::vector<int32_t>& parent_internal,
+                         std::vector<int32_t>& parent_leaf) {
+    constexpr int kMaxTreeletLeaves = 7;
+    int32_t L[kMaxTreeletLeaves];
+    int32_t internals[kMaxTreeletLeaves - 1];
+    int nl = 0, ni = 0;
+    L[nl++] = B.nodes[N].left;
+    L[nl++] = B.nodes[N].right;
+    internals[ni++] = N;
+    while (nl < kMaxTreeletLeaves) {
+        int pick = -1;
+        float pa = -1.0f;
+        for (int i = 0; i < nl; ++i)
+            if (!(L[i] & kLeaf)) {
+                const float a = tbox_area(tbox_of(B, L[i]));
+                if (a > pa) {
+                    pa = a;
+                    pick = i;
+                }
+            }
+        if (pick < 0) break;
+        const int32_t c = L[pick];
+        internals[ni++] = c;
+        L[pick] = B.nodes[c].left;
+        L[nl++] = B.nodes[c].right;
+    }
+    if (nl < 3) return;
+    const int full = (1 << nl) - 1;
+    TBox bx[kMaxTreeletLeaves];
+    for (int i = 0; i < nl; ++i) bx[i] = tbox_of(B, L[i]);
+    float area[1 << kMaxTreeletLeaves], cost[1 << kMaxTreeletLeaves];
+    uint8_t split[1 << kMaxTreeletLeaves];
+    for (int S = 1; S <= full; ++S) {
+        TBox u;
+        for (int a = 0; a < 3; ++a) {
+            u.lo[a] = INFINITY;
+            u.hi[a] = -INFINITY;
+        }
+        for (int i = 0; i < nl; ++i)
+            if (S >> i & 1)
+                for (int a = 0; a < 3; ++a) {
+                    u.lo[a] = std::fmin(u.lo[a], bx[i].lo[a]);
+                    u.hi[a] = std::fmax(u.hi[a], bx[i].hi[a]);
+                }
+        area[S] = tbox_area(u);
+    }
+    for (int S = 1; S <= full; ++S) {
+        split[S] = 0;
+        if ((S & (S - 1)) == 0) {
+            cost[S] = 0.0f;
+            continue;
+        }
+        const int low = S & -S, rest = S ^ low;
+        float bc = INFINITY;
+        int bp = 0;
+        // P = low | Q over the subsets Q of rest except rest itself,
+        // enumerated from the largest down
+        for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {
+            const int P = Q | low;
+            const float c = cost[P] + cost[S ^ P];
+            if (c < bc) {
+                bc = c;
+                bp = P;
+            }
+            if (Q == 0) break;
+        }
+        cost[S] = area[S] + bc;
+        split[S] = (uint8_t)bp;
+    }
+    float current = 0.0f;
+    for (int i = 0; i < ni; ++i) current = current + tbox_area(tbox_of(B, internals[i]));
+    if (!(cost[full] < current)) return;
+    // Rewire.  The treelet's internal nodes are handed out in depth-first
+    // preorder of the chosen splits (left part first); children are wired in
+    // that order and boxes computed in the reverse order (children first).
+    int order[kMaxTreeletLeaves - 1];
+    int32_t node_of[1 << kMaxTreeletLeaves];
+    int no = 0;
+    {
+        int stack[kMaxTreeletLeaves];
+        int sp = 0;
+        stack[sp++] = full;
+        while (sp > 0) {
+            const int S = stack[--sp];
+            if ((S & (S - 1)) == 0) continue;
+            node_of[S] = internals[no];
+            order[no++] = S;
+            stack[sp++] = S ^ split[S];
+            stack[sp++] = split[S];
+        }
+    }
+    auto word = [&](int T) { return (T & (T - 1)) == 0 ? L[__builtin_ctz(T)] : node_of[T]; };
+    for (int i = 0; i < no; ++i) {
+        const int S = order[i];
+        const int32_t me = node_of[S], l = word(split[S]), r = word(S ^ split[S]);
+        B.nodes[me].left = l;
+        B.nodes[me].right = r;
+        for (int32_t c : {l, r}) {
+            if (c & kLeaf) parent_leaf[c & kSlotMask] = me;
+            else parent_internal[c] = me;
+        }
+    }
+    for (int i = no - 1; i >= 0; --i) {
+        const int32_t me = node_of[order[i]];
+        const TBox bl = tbox_of(B, B.nodes[me].left), br = tbox_of(B, B.nodes[me].right);
+        for (int a = 0; a < 3; ++a) {
+            B.nodes[me].lo[a] = std::fmin(bl.lo[a], br.lo[a]);
+            B.nodes[me].hi[a] = std::fmax(bl.hi[a], br.hi[a]);
+        }
+    }
+}
+
+// One pass over every internal node, children before parents (post-order).
+void optimize_treelets(Bvh& B, std::vector<int32_t>& parent_internal, std::vector<int32_t>& parent_leaf) {
+    if (B.n < 3) return;
+    struct Item {
+        int32_t node;
+        bool expanded;
+    };
+    std::vector<Item> st;
+    st.push_back({0, false});
+    while (!st.empty()) {
+        Item it = st.back();
+        st.pop_back();
+        if (it.expanded) {
+            restructure_treelet(B, it.node, parent_internal, parent_leaf);
+            continue;
+        }
+        st.push_back({it.node, true});
+        for (int32_t c : {B.nodes[it.node].right, B.nodes[it.node].left})
+            if (!(c & kLeaf)) st.push_back({c, false});
+    }
+}
+
 // Moving spheres: the same topology, slot order and hoisted set, with every
 // slot's sphere taken from the new array (same original indices) and the
 // boxes refit bottom-up.  Mirrors venu_scene_update.
@@ -374,6 +546,8 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
         if (right & kLeaf) parent_leaf[right & ~kLeaf] = i; else parent_internal[right] = i;
     }
     refit_bvh(B);
+    optimize_treelets(B, parent_internal, parent_leaf);
+    refit_bvh(B);  // boxes unchanged; the depth of the rewired tree
     // Hoisted spheres: the (at most 4) lowest huge slots, if there are at
     // most 64 huge spheres; their leaf words are flagged.
     std::vector<int32_t> cand;

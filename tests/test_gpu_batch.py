@@ -146,24 +146,27 @@ def _one(venu, torch, oracle, b, scene, eye, W, H, spp, depth, sub=1):
     return dict(id=jid, ds=ds, acc=acc, want=want)
 
 
-@pytest.mark.parametrize("shortest_first", [False, True])
-def test_batch_policy(venu, oracle, cuda, shortest_first):
+@pytest.mark.parametrize("policy", ["fifo", "shortest_first", "sequential"])
+def test_batch_policy(venu, oracle, cuda, policy):
     """A small job submitted behind a large one: shortest-first generates its
-    paths at once (it finishes within a few iterations), FIFO only after the
-    large job's paths are all generated.  Results are exact either way."""
+    paths at once (it finishes within a few iterations); FIFO only after the
+    large job's paths are all generated; sequential only after the large job
+    has finished.  Results are exact whatever the order."""
     torch = cuda
     b = venu.Batch(pool_paths=4096, max_jobs=4)
-    b.set_policy(shortest_first)
+    b.set_policy(policy)
     sp = oracle.scene_rtiow(0)
     big = _one(venu, torch, oracle, b, sp, (13, 2, 3), 64, 64, 16, 4)
     small = _one(venu, torch, oracle, b, sp, (13, 2, 3), 8, 6, 1, 4)
     b.run(stop_on_finish=True)
     first = b.collect()
     it = b.stats()["iterations"]
-    if shortest_first:
+    if policy == "shortest_first":
         assert first == [small["id"]] and it <= 8
-    else:
+    elif policy == "fifo":
         assert it >= 18  # 65536 paths through a 4096-path pool (>= 16 iterations) before the small job starts
+    else:
+        assert first == [big["id"]]  # the small job cannot start before the big one is done
     b.run()
     rest = b.collect()
     torch.cuda.synchronize()

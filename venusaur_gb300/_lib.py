@@ -102,6 +102,8 @@ BATCH_NO_GRAPH = 1
 RUN_STOP_ON_FINISH = 1
 POLICY_FIFO = 0
 POLICY_SHORTEST_FIRST = 1
+POLICY_SEQUENTIAL = 2
+POLICIES = {"fifo": POLICY_FIFO, "shortest_first": POLICY_SHORTEST_FIRST, "sequential": POLICY_SEQUENTIAL}
 INJECT_ALLOC = 1
 INJECT_SCENE = 2
 

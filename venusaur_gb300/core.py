@@ -516,6 +516,12 @@ def _camera_c(camera: np.ndarray) -> "_lib.CameraC":
     return cc
 
 
+def _policy(policy) -> int:
+    if isinstance(policy, bool):
+        return _lib.POLICY_SHORTEST_FIRST if policy else _lib.POLICY_FIFO
+    return _lib.POLICIES[policy]
+
+
 class Batch:
     """A venu_batch: jobs admitted with submit(), advanced together by run(),
     finished ones accumulated and released by collect()."""
@@ -555,10 +561,10 @@ class Batch:
         flags = _lib.RUN_STOP_ON_FINISH if stop_on_finish else 0
         check(lib().venu_batch_run(self.handle, max_iterations, flags, _stream_handle(stream)))
 
-    def set_policy(self, shortest_first: bool) -> None:
-        """Plan order: submission order (False) or fewest unfinished paths first."""
-        pol = _lib.POLICY_SHORTEST_FIRST if shortest_first else _lib.POLICY_FIFO
-        check(lib().venu_batch_set_policy(self.handle, pol))
+    def set_policy(self, policy) -> None:
+        """Plan order: "fifo", "shortest_first" or "sequential" (a bool selects
+        shortest_first / fifo)."""
+        check(lib().venu_batch_set_policy(self.handle, _policy(policy)))
 
     def interrupt(self, on: bool = True) -> None:
         """Ends a running run() at its next iteration boundary while set."""
@@ -598,7 +604,7 @@ class Server:
                                        C.byref(h)))
         self.handle = h
         if shortest_first:
-            self.set_policy(True)
+            self.set_policy("shortest_first")
         if express_paths:
             self.set_express(express_paths)
 
@@ -606,9 +612,9 @@ class Server:
         """Requests of at most max_paths paths run in the express lane (0: off)."""
         check(lib().venu_server_set_express(self.handle, int(max_paths)))
 
-    def set_policy(self, shortest_first: bool) -> None:
-        pol = _lib.POLICY_SHORTEST_FIRST if shortest_first else _lib.POLICY_FIFO
-        check(lib().venu_server_set_policy(self.handle, pol))
+    def set_policy(self, policy) -> None:
+        """Plan order of the bulk lane: "fifo", "shortest_first" or "sequential"."""
+        check(lib().venu_server_set_policy(self.handle, _policy(policy)))
 
     def submit(self, camera: np.ndarray, width: int, height: int, spp: int, spheres=None, scene_key: int = 0,
                subframe: int = 1, max_depth: int = 50, tag: int = 0) -> int:

@@ -50,7 +50,7 @@ struct LoopCtl {  // device-owned loop state
 };
 
 struct RunCtl {  // host-written before each run
-    uint32_t max_iter, nactive, stop_on_finish, pad;
+    uint32_t max_iter, nactive, stop_on_finish, sequential;
 };
 
 struct CollectEntry {
@@ -77,7 +77,10 @@ __global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t s
     }
 }
 
+// sequential: a job gets slots only once every job before it in the order
+// has finished all its paths (one job at a time, as rendering them in turn).
 __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
+                       const unsigned long long* __restrict__ job_done,
                        const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
                        uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
                        uint32_t* __restrict__ plan_off, uint32_t Q) {
@@ -86,12 +89,15 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
     const uint32_t survivors = ctl->cnt[out];
     const uint32_t free = survivors < Q ? Q - survivors : 0u;
     const uint32_t na = run->nactive;
+    const bool sequential = run->sequential != 0u;
     uint32_t off = 0, more = 0;
+    bool blocked = false;
     for (uint32_t i = 0; i < na; ++i) {
         const uint32_t j = order[i];
         const unsigned long long total = jobs[j].total, nx = job_next[j];
         const unsigned long long rem = total - nx;
-        const uint32_t take = (uint32_t)min(rem, (unsigned long long)(free - off));
+        const uint32_t take = blocked ? 0u : (uint32_t)min(rem, (unsigned long long)(free - off));
+        if (sequential && job_done[j] < total) blocked = true;
         plan_job[i] = j;
         plan_start[i] = nx;
         plan_off[i] = off;
@@ -303,7 +309,7 @@ cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
     const size_t sm = traverse_smem((int)b->tune.traverse_block);
     k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
                                                                                   b->q[0], b->q[1]);
-    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_order, b->d_run, b->d_ctl, b->d_plan_job, b->d_plan_start,
+    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_order, b->d_run, b->d_ctl, b->d_plan_job, b->d_plan_start,
                              b->d_plan_off, b->Q);
     k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
                                              b->q[0], b->q[1]);
@@ -543,7 +549,7 @@ extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, ui
     rc.max_iter = max_iterations;
     rc.nactive = (uint32_t)b->order.size();
     rc.stop_on_finish = (flags & VENU_RUN_STOP_ON_FINISH) ? 1u : 0u;
-    rc.pad = 0;
+    rc.sequential = b->policy == VENU_POLICY_SEQUENTIAL ? 1u : 0u;
     VENU_CUDA(cudaMemcpyAsync(b->d_run, &rc, sizeof(rc), cudaMemcpyHostToDevice, st));
     VENU_CUDA(cudaMemsetAsync(&b->d_ctl->iter, 0, sizeof(uint32_t), st));
     VENU_CUDA(cudaMemsetAsync(&b->d_ctl->job_finished, 0, sizeof(uint32_t), st));
@@ -633,7 +639,7 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
 }
 
 extern "C" venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy) {
-    if (!b || policy > VENU_POLICY_SHORTEST_FIRST) {
+    if (!b || policy > VENU_POLICY_SEQUENTIAL) {
         set_error("venu_batch_set_policy: NULL batch or unknown policy");
         return VENU_ERR_INVALID;
     }

@@ -340,6 +340,176 @@ __global__ void k_refit(const venu_sphere* __restrict__ s, const uint32_t* __res
     }
 }
 
+// ---------------------------------------------------------------------------
+// Treelet restructuring (Karras & Aila, HPG 2013), one bottom-up pass after
+// the refit: at every internal node N, once both of its subtrees are final,
+// a treelet of up to 7 leaves is grown from N's children by opening the
+// internal treelet leaf with the largest surface area (first on ties); a
+// dynamic program over the 2^7 subsets finds the topology with the least
+// total internal surface area, and the treelet is rewired that way if that
+// is strictly less than its current total.  Leaves keep their Morton slots,
+// N stays the treelet root, the treelet's internal nodes are reused in the
+// order they were opened and handed out in depth-first order of the new
+// topology.  Same arithmetic, same order as the host LBVH of the oracle, so
+// the tree stays bit-exact.  One thread per leaf walks up as in k_refit;
+// the second thread to reach a node restructures it.
+// ---------------------------------------------------------------------------
+constexpr int kTreeletLeaves = 7;
+
+struct TBox {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float tbox_area(const TBox& b) {
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return 2.0f * ((dx * dy + dy * dz) + dz * dx);
+}
+
+__device__ __forceinline__ TBox tbox_of(const float4* nodes, const float4* leafbox, int32_t c) {
+    const float4 lo = (c & kLeaf) ? __ldcg(leafbox + 2 * (c & kSlotMask)) : __ldcg(nodes + 2 * c);
+    const float4 hi = (c & kLeaf) ? __ldcg(leafbox + 2 * (c & kSlotMask) + 1) : __ldcg(nodes + 2 * c + 1);
+    TBox b;
+    b.lo[0] = lo.x;
+    b.lo[1] = lo.y;
+    b.lo[2] = lo.z;
+    b.hi[0] = hi.x;
+    b.hi[1] = hi.y;
+    b.hi[2] = hi.z;
+    return b;
+}
+
+__device__ __forceinline__ int32_t child_word(const float4* nodes, int32_t p, int side) {
+    return __float_as_int(__ldcg(&nodes[2 * p + side].w));
+}
+
+__device__ void restructure_treelet(int32_t N, int n, float4* nodes, int32_t* parent_int, int32_t* parent_leaf,
+                                    const float4* leafbox) {
+    int32_t L[kTreeletLeaves], internals[kTreeletLeaves - 1];
+    int nl = 0, ni = 0;
+    L[nl++] = child_word(nodes, N, 0);
+    L[nl++] = child_word(nodes, N, 1);
+    internals[ni++] = N;
+    while (nl < kTreeletLeaves) {
+        int pick = -1;
+        float pa = -1.0f;
+        for (int i = 0; i < nl; ++i)
+            if (!(L[i] & kLeaf)) {
+                const float a = tbox_area(tbox_of(nodes, leafbox, L[i]));
+                if (a > pa) {
+                    pa = a;
+                    pick = i;
+                }
+            }
+        if (pick < 0) break;
+        const int32_t c = L[pick];
+        if ((uint32_t)c >= (uint32_t)(n - 1)) return;  // never for a sound tree
+        internals[ni++] = c;
+        L[pick] = child_word(nodes, c, 0);
+        L[nl++] = child_word(nodes, c, 1);
+    }
+    for (int i = 0; i < nl; ++i)
+        if ((L[i] & kLeaf) ? (L[i] & kSlotMask) >= n : (uint32_t)L[i] >= (uint32_t)(n - 1)) return;
+    if (nl < 3) return;
+    const int full = (1 << nl) - 1;
+    TBox bx[kTreeletLeaves];
+    for (int i = 0; i < nl; ++i) bx[i] = tbox_of(nodes, leafbox, L[i]);
+    float cost[1 << kTreeletLeaves];
+    uint8_t split[1 << kTreeletLeaves];
+    for (int S = 1; S <= full; ++S) {
+        split[S] = 0;
+        if ((S & (S - 1)) == 0) {
+            cost[S] = 0.0f;
+            continue;
+        }
+        TBox u;
+        for (int a = 0; a < 3; ++a) {
+            u.lo[a] = INFINITY;
+            u.hi[a] = -INFINITY;
+        }
+        for (int i = 0; i < nl; ++i)
+            if (S >> i & 1)
+                for (int a = 0; a < 3; ++a) {
+                    u.lo[a] = fminf(u.lo[a], bx[i].lo[a]);
+                    u.hi[a] = fmaxf(u.hi[a], bx[i].hi[a]);
+                }
+        const float area = tbox_area(u);
+        const int low = S & -S, rest = S ^ low;
+        float bc = INFINITY;
+        int bp = 0;
+        for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {  // the subsets of rest but rest, largest first
+            const int P = Q | low;
+            const float c = cost[P] + cost[S ^ P];
+            if (c < bc) {
+                bc = c;
+                bp = P;
+            }
+            if (Q == 0) break;
+        }
+        cost[S] = area + bc;
+        split[S] = (uint8_t)bp;
+    }
+    float current = 0.0f;
+    for (int i = 0; i < ni; ++i) current = current + tbox_area(tbox_of(nodes, leafbox, internals[i]));
+    if (!(cost[full] < current)) return;
+    // order[i]: the subset of the i-th internal node in depth-first preorder;
+    // it is given internals[i]
+    int order[kTreeletLeaves - 1];
+    int no = 0;
+    {
+        int stack[kTreeletLeaves];
+        int sp = 0;
+        stack[sp++] = full;
+        while (sp > 0) {
+            const int S = stack[--sp];
+            if ((S & (S - 1)) == 0) continue;
+            order[no++] = S;
+            stack[sp++] = S ^ split[S];
+            stack[sp++] = split[S];
+        }
+    }
+    auto word = [&](int T) -> int32_t {
+        if ((T & (T - 1)) == 0) return L[__ffs(T) - 1];
+        for (int i = 0; i < no; ++i)
+            if (order[i] == T) return internals[i];
+        return internals[0];  // unreachable: every internal subset is in order[]
+    };
+    for (int i = 0; i < no; ++i) {
+        const int S = order[i];
+        const int32_t me = internals[i];
+        const int32_t l = word(split[S]), r = word(S ^ split[S]);
+        nodes[2 * me].w = __int_as_float(l);
+        nodes[2 * me + 1].w = __int_as_float(r);
+        if (l & kLeaf) parent_leaf[l & kSlotMask] = me;
+        else parent_int[l] = me;
+        if (r & kLeaf) parent_leaf[r & kSlotMask] = me;
+        else parent_int[r] = me;
+    }
+    for (int i = no - 1; i >= 0; --i) {
+        const int32_t me = internals[i];
+        const TBox bl = tbox_of(nodes, leafbox, child_word(nodes, me, 0));
+        const TBox br = tbox_of(nodes, leafbox, child_word(nodes, me, 1));
+        const int32_t lw = child_word(nodes, me, 0), rw = child_word(nodes, me, 1);
+        nodes[2 * me] = make_float4(fminf(bl.lo[0], br.lo[0]), fminf(bl.lo[1], br.lo[1]), fminf(bl.lo[2], br.lo[2]),
+                                    __int_as_float(lw));
+        nodes[2 * me + 1] = make_float4(fmaxf(bl.hi[0], br.hi[0]), fmaxf(bl.hi[1], br.hi[1]),
+                                        fmaxf(bl.hi[2], br.hi[2]), __int_as_float(rw));
+    }
+}
+
+__global__ void k_treelets(int n, float4* nodes, int32_t* parent_int, int32_t* parent_leaf,
+                           const float4* __restrict__ leafbox, uint32_t* __restrict__ arrive) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int p = parent_leaf[k];
+    for (int level = 0; p >= 0 && p < n - 1 && level < 128; ++level) {
+        __threadfence();
+        if (atomicAdd(arrive + p, 1u) == 0u) return;  // the other subtree is not final yet
+        __threadfence();
+        restructure_treelet(p, n, nodes, parent_int, parent_leaf, leafbox);
+        p = __ldcg(parent_int + p);
+    }
+}
+
 // Slot-ordered sphere / material / meta records.  ids may alias meta (a
 // refit regathers from the meta words): each thread reads its slot's word
 // before writing it.
@@ -435,6 +605,9 @@ cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const
         k_karras<<<cdiv(n - 1, 256), 256, 0, st>>>(B.keys, (int)n, B.nodes, B.pint, B.pleaf);
         k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, 0xffffffffu, (int)n, B.nodes, B.pint, B.pleaf, B.leafbox,
                                               B.arrive);
+        e = cudaMemsetAsync(B.arrive, 0, sizeof(uint32_t) * nint, st);
+        if (e != cudaSuccess) return e;
+        k_treelets<<<cdiv(n, 128), 128, 0, st>>>((int)n, B.nodes, B.pint, B.pleaf, B.leafbox, B.arrive);
     }
     k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, 0xffffffffu, n, B.sph, B.mat, B.meta);
     if (n > 1) {

@@ -294,8 +294,7 @@ void server_loop(venu_server* s) {
         {
             const uint32_t pol = s->policy.load();
             if (pol != s->applied_policy) {
-                venu_batch_set_policy(s->batch, pol);
-                venu_batch_set_policy(s->express, pol);
+                venu_batch_set_policy(s->batch, pol);  // the express lane stays FIFO
                 s->applied_policy = pol;
             }
         }
@@ -471,7 +470,7 @@ extern "C" venu_status venu_server_submit(venu_server* s, const venu_request* re
 }
 
 extern "C" venu_status venu_server_set_policy(venu_server* s, uint32_t policy) {
-    if (!s || policy > VENU_POLICY_SHORTEST_FIRST) {
+    if (!s || policy > VENU_POLICY_SEQUENTIAL) {
         set_error("venu_server_set_policy: NULL server or unknown policy");
         return VENU_ERR_INVALID;
     }
