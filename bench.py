@@ -388,6 +388,7 @@ def main():
     ap.add_argument("--spp", type=int, default=0, help="override the config's samples per pixel (small profiling cases)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--tuning", default="", help="JSON launch shapes to use instead of the autotuner's")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
@@ -427,7 +428,9 @@ def main():
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
     max_paths = args.max_paths
-    if not args.no_autotune:
+    if args.tuning:
+        tuning = json.loads(args.tuning)
+    elif not args.no_autotune:
         from venusaur_gb300 import tune
 
         tuning, best_mp, tune_log = tune.autotune(
@@ -494,7 +497,8 @@ def main():
     del acc2
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
     segs_c, paths_c = sc["segments"], sc["paths"]
-    fused = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"]) == 2
+    variant = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"])
+    fused = variant == 2
     # Algorithmic bytes of the dominant kernel per render, by the per-segment
     # figure: 32 B per node (box) tested + 16 B per sphere tested + the ray
     # state queue traffic: 112 B per segment for the fused traverse+shade
@@ -520,10 +524,10 @@ def main():
     # per segment from a capture of the same kernel on a smaller case of the
     # same scene (the queue traffic, which grows in proportion to the rays;
     # the node set stays cache-resident), scaled to this launch's segments.
-    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.3 B) and
-    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (86.7 B).
+    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.6 B) and
+    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (87.2 B).
     # (c1's queues fit in L2: no figure for it.)
-    dram_per_seg = {"c2": 86.3, "c3": 86.7}.get(args.config) if fused else None
+    dram_per_seg = {"c2": 86.6, "c3": 87.2}.get(args.config) if variant == 2 else None
     traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"]) if dram_per_seg else None
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -582,7 +586,8 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "segments_per_step": segs_step, "paths_per_step": st["paths"],
                    "tuning": dict(wf.tuning(), max_paths=max_paths),
-                   "autotune_candidates": len(tune_log)},
+                   "autotune_candidates": len(tune_log),
+                   "lbvh": {"build_ms": ds.info()["build_ms"], "device_bytes": ds.info()["device_bytes"]}},
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": e2e,

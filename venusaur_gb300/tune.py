@@ -25,12 +25,14 @@ def candidates(space=None):
     seen = set()
     for v, r, tb, sb in itertools.product(space["traverse_variant"], space["refill_min"],
                                           space["traverse_block"], space["shade_block"]):
-        key = (v, r if v == 1 else 32, tb, sb)
+        # the refill threshold matters to the dynamic-fetch variant only, the
+        # shade block to the variants with a separate shade kernel only
+        key = (v, r if v == 1 else 32, tb, sb if v in (0, 1) else 256)
         if key in seen:
             continue
         seen.add(key)
         yield dict(traverse_variant=v, refill_min=key[1], traverse_block=tb, traverse_blocks_per_sm=0,
-                   shade_block=sb, shade_blocks_per_sm=0)
+                   shade_block=key[3], shade_blocks_per_sm=0)
 
 
 def time_render(wf: Wavefront, scene: DeviceScene, cam, W, H, spp, depth, accum, reps=2):
