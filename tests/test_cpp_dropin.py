@@ -35,8 +35,8 @@ def test_cpp_dropin_renders(tmp_path, venu, oracle, cuda):
 
     exe = build_exe(tmp_path, venu)
     W, H, spp, depth = 48, 30, 3, 5
-    ppm, raw = str(tmp_path / "o.ppm"), str(tmp_path / "o.rgba")
-    r = subprocess.run([exe, str(W), str(H), str(spp), str(depth), ppm, raw], capture_output=True, text=True)
+    ppm, raw, pfm = str(tmp_path / "o.ppm"), str(tmp_path / "o.rgba"), str(tmp_path / "o.pfm")
+    r = subprocess.run([exe, str(W), str(H), str(spp), str(depth), ppm, raw, pfm], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     got = np.fromfile(raw, np.uint8).reshape(-1, 4)
     sp = oracle.scene_rtiow(0)
@@ -45,3 +45,6 @@ def test_cpp_dropin_renders(tmp_path, venu, oracle, cuda):
     b = oracle.render(sp, cam, W, H, spp, subframe=2, max_depth=depth, mode=pyoracle.MODE_GB300, accum=a["accum"])
     assert np.abs(got.astype(int) - b["image8"].astype(int)).max() <= 1
     assert open(ppm, "rb").read(2) == b"P6"
+    head = f"PF\n{W} {H}\n-1.0\n".encode()
+    data = open(pfm, "rb").read()
+    assert data[: len(head)] == head and len(data) == len(head) + W * H * 12
