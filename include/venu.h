@@ -355,8 +355,15 @@ typedef struct venu_request {
     uint32_t reserved;
     uint64_t scene_key;         /* != 0: requests with the same key share one resident BVH */
     venu_camera camera;
-    venu_render_opts opts;      /* accumulation is reset per request */
+    venu_render_opts opts;      /* accumulation is reset per request, except in a session */
     uint64_t tag;               /* returned with the result */
+    uint64_t session;           /* != 0: a progressive session (Renderer::Draw served over
+                                   requests, Core/Renderer.h:35-78): the samples are added to
+                                   the session's resident accumulator and the image is the
+                                   running mean, unless opts.flags has VENU_FLAG_RESET_ACCUM or
+                                   the size changed (then it restarts); the caller advances
+                                   opts.subframe_index.  Requests of one session run one at a
+                                   time in submission order. */
 } venu_request;
 
 typedef struct venu_result {
@@ -398,6 +405,9 @@ VENU_API venu_status venu_server_set_policy(venu_server* s, uint32_t policy);
  * turns it off.  A small request then waits for at most one iteration of
  * the bulk pool instead of sharing every bounce with the large jobs. */
 VENU_API venu_status venu_server_set_express(venu_server* s, uint64_t max_paths);
+/* Frees a progressive session's accumulator (after its admitted request, if
+ * any, completes); a later request with the same id starts a new session. */
+VENU_API venu_status venu_server_end_session(venu_server* s, uint64_t session);
 /* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY). */
 VENU_API venu_status venu_server_wait(venu_server* s, uint64_t request_id, double timeout_s, venu_result* out);
 VENU_API venu_status venu_server_cancel(venu_server* s, uint64_t request_id);

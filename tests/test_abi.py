@@ -87,3 +87,33 @@ def test_host_generators(venu):
     cam.SetForward(np.float32([-13, -2, -3]))
     u, v, w = cam.UVWFrame()
     assert abs(float(np.dot(w, w)) - 100.0) < 1e-3
+
+
+def test_ctypes_mirrors_match_the_header(venu, tmp_path):
+    """Every ctypes structure of the Python binding has the size and field
+    offsets of its C declaration (compiled here with gcc)."""
+    from venusaur_gb300 import _lib
+
+    pairs = {"venu_render_opts": _lib.RenderOpts, "venu_scene_info": _lib.SceneInfo,
+             "venu_render_stats": _lib.RenderStats, "venu_tuning": _lib.Tuning, "venu_camera": _lib.CameraC,
+             "venu_job_desc": _lib.JobDesc, "venu_batch_stats": _lib.BatchStats, "venu_request": _lib.Request,
+             "venu_result": _lib.Result, "venu_server_stats": _lib.ServerStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "venu.h"', "int main(void) {"]
+    for cname, cls in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in cls._fields_:
+            lines.append(f'  printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines.append("  return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    want = []
+    for cname, cls in pairs.items():
+        want.append(f"{cname} size {C.sizeof(cls)}")
+        for f in cls._fields_:
+            want.append(f"{cname} {f[0]} {getattr(cls, f[0]).offset}")
+    assert [g for g in got if g] == want

@@ -120,3 +120,35 @@ def test_server_express_lane(venu, oracle, cuda):
     assert st["completed"] == 4 and st["failed"] == 0
     assert st["segments"] == sum(c[2]["segments"] for c, _ in cases)
     srv.close()
+
+
+def test_server_progressive_session(venu, oracle, cuda):
+    """Requests of one session add to its resident accumulator (the running
+    mean of Renderer::Draw); a reset or a new size restarts it; end_session
+    frees it.  Images equal the oracle's progressive accumulation."""
+    srv = venu.Server(hbm_budget_bytes=1 << 30, pool_paths=2000, max_jobs=8, iterations_per_step=8,
+                      express_paths=1000)
+    sp = oracle.scene_rtiow(0)
+    W, H, spp, depth = 24, 16, 2, 6
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    acc = None
+    ids = []
+    for sub in (1, 2, 3):
+        ids.append(srv.submit(cam, W, H, spp, spheres=sp, scene_key=5, max_depth=depth, subframe=sub, session=42))
+    for sub, rid in zip((1, 2, 3), ids):
+        want = oracle.render(sp, cam, W, H, spp, subframe=sub, max_depth=depth, mode=pyoracle.MODE_GB300, accum=acc)
+        acc = want["accum"]
+        r = srv.wait(rid)
+        assert r["status"] == 0
+        assert np.abs(r["image"].astype(int) - want["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    # an explicit reset restarts the session at subframe 7
+    r = srv.wait(srv.submit(cam, W, H, spp, scene_key=5, max_depth=depth, subframe=7, session=42, reset=True))
+    want = oracle.render(sp, cam, W, H, spp, subframe=7, max_depth=depth, mode=pyoracle.MODE_GB300)
+    assert np.abs(r["image"].astype(int) - want["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    # ending the session: the next request of that id starts from zero
+    srv.end_session(42)
+    r = srv.wait(srv.submit(cam, W, H, spp, scene_key=5, max_depth=depth, subframe=2, session=42))
+    want = oracle.render(sp, cam, W, H, spp, subframe=2, max_depth=depth, mode=pyoracle.MODE_GB300)
+    assert np.abs(r["image"].astype(int) - want["image8"].reshape(r["image"].shape).astype(int)).max() <= 1
+    assert srv.stats()["failed"] == 0
+    srv.close()

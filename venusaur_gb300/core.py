@@ -608,6 +608,9 @@ class Server:
         if express_paths:
             self.set_express(express_paths)
 
+    def end_session(self, session: int) -> None:
+        check(lib().venu_server_end_session(self.handle, session))
+
     def set_express(self, max_paths: int) -> None:
         """Requests of at most max_paths paths run in the express lane (0: off)."""
         check(lib().venu_server_set_express(self.handle, int(max_paths)))
@@ -617,7 +620,9 @@ class Server:
         check(lib().venu_server_set_policy(self.handle, _policy(policy)))
 
     def submit(self, camera: np.ndarray, width: int, height: int, spp: int, spheres=None, scene_key: int = 0,
-               subframe: int = 1, max_depth: int = 50, tag: int = 0) -> int:
+               subframe: int = 1, max_depth: int = 50, tag: int = 0, session: int = 0, reset: bool = False) -> int:
+        """session != 0: add to that progressive session's accumulator (reset=True
+        restarts it); the image returned is the running mean."""
         r = _lib.Request()
         arr = None
         if spheres is not None:
@@ -626,8 +631,9 @@ class Server:
             r.num_spheres = len(arr)
         r.scene_key = scene_key
         r.camera = _camera_c(camera)
-        r.opts = RenderOpts(width, height, spp, subframe, max_depth, 0)
+        r.opts = RenderOpts(width, height, spp, subframe, max_depth, _lib.FLAG_RESET_ACCUM if reset else 0)
         r.tag = tag
+        r.session = session
         rid = C.c_uint64()
         check(lib().venu_server_submit(self.handle, C.byref(r), C.byref(rid)))
         return int(rid.value)

@@ -50,9 +50,20 @@ struct Request {
     // while admitted
     uint64_t scene_key = 0;
     int lane = 0;
+    bool session_accum = false;  // accum belongs to a progressive session, not to the request
     float* accum = nullptr;
     uint8_t* image8 = nullptr;
     uint64_t job_bytes = 0;
+};
+
+// A progressive session (Renderer::Draw served over requests): its
+// accumulator stays on the device between requests.
+struct Session {
+    float* accum = nullptr;
+    uint32_t width = 0, height = 0;
+    bool busy = false;         // a request of the session is admitted
+    bool end_pending = false;  // ended while busy: freed when that request completes
+    uint64_t bytes = 0;
 };
 
 struct SceneEntry {
@@ -103,6 +114,8 @@ struct venu_server {
     cudaStream_t st = nullptr;
     std::unordered_map<uint64_t, SceneEntry> scenes;
     std::unordered_map<uint32_t, uint64_t> active[2];  // per lane: batch job id -> request id
+    std::unordered_map<uint64_t, Session> sessions;
+    std::vector<uint64_t> sessions_to_end;  // guarded by mu; ended by the server thread
     uint64_t resident = 0, use_clock = 0;
     size_t n_active_all() const { return active[0].size() + active[1].size(); }
     venu_batch* lane(int l) const { return l ? express : batch; }
@@ -151,6 +164,25 @@ void evict_for(venu_server* s, uint64_t need) {
     }
 }
 
+// The request's accumulator: freed if it is the request's own; a session's
+// stays (and the session is free for its next request).
+void release_accum(venu_server* s, Request& R) {
+    if (R.session_accum) {
+        auto it = s->sessions.find(R.req.session);
+        if (it != s->sessions.end()) {
+            it->second.busy = false;
+            if (it->second.end_pending) {
+                if (it->second.accum) cudaFreeAsync(it->second.accum, s->st);
+                s->resident -= it->second.bytes;
+                s->sessions.erase(it);
+            }
+        }
+    } else if (R.accum) {
+        cudaFreeAsync(R.accum, s->st);
+    }
+    R.accum = nullptr;
+}
+
 // Admits one request; on failure it is completed with its status.
 void admit(venu_server* s, Request& R) {
     const venu_render_opts& o = R.req.opts;
@@ -195,11 +227,38 @@ void admit(venu_server* s, Request& R) {
     it->second.refs += 1;
     it->second.last_use = ++s->use_clock;
     const uint64_t npix = (uint64_t)o.width * o.height;
-    cudaError_t e = cudaMallocAsync(&R.accum, npix * sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL, s->st);
+    const uint64_t accum_bytes = npix * sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL;
+    bool reset = true;
+    cudaError_t e = cudaSuccess;
+    if (R.req.session) {
+        // continue the session's accumulator unless it is new, resized or reset
+        Session& S = s->sessions[R.req.session];
+        reset = !S.accum || S.width != o.width || S.height != o.height || (o.flags & VENU_FLAG_RESET_ACCUM);
+        if (S.accum && (S.width != o.width || S.height != o.height)) {
+            cudaFreeAsync(S.accum, s->st);
+            s->resident -= S.bytes;
+            S.accum = nullptr;
+        }
+        if (!S.accum) {
+            e = cudaMallocAsync(&S.accum, accum_bytes, s->st);
+            if (e == cudaSuccess) {
+                S.width = o.width;
+                S.height = o.height;
+                S.bytes = accum_bytes;
+                s->resident += accum_bytes;
+            } else {
+                S.accum = nullptr;
+            }
+        }
+        R.accum = S.accum;
+        R.session_accum = true;
+        S.busy = e == cudaSuccess;
+    } else {
+        e = cudaMallocAsync(&R.accum, accum_bytes, s->st);
+    }
     if (e == cudaSuccess) e = cudaMallocAsync(&R.image8, npix * 4u, s->st);
     if (e != cudaSuccess) {
-        if (R.accum) cudaFreeAsync(R.accum, s->st);
-        R.accum = nullptr;
+        release_accum(s, R);
         release_scene(s, key);
         complete(s, R, VENU_ERR_OOM);
         return;
@@ -211,26 +270,42 @@ void admit(venu_server* s, Request& R) {
     d.scene = it->second.scene;
     d.camera = R.req.camera;
     d.opts = o;
-    d.opts.flags |= VENU_FLAG_RESET_ACCUM;
+    if (reset) d.opts.flags |= VENU_FLAG_RESET_ACCUM;
+    else d.opts.flags &= ~VENU_FLAG_RESET_ACCUM;
     d.accum = R.accum;
     d.image8 = R.image8;
     uint32_t jid = 0;
     venu_status bs = venu_batch_submit(s->lane(R.lane), &d, s->st, &jid);
     if (bs != VENU_OK) {
-        cudaFreeAsync(R.accum, s->st);
+        release_accum(s, R);
         cudaFreeAsync(R.image8, s->st);
-        R.accum = nullptr;
         R.image8 = nullptr;
         release_scene(s, key);
         complete(s, R, bs);
         return;
     }
     R.scene_key = key;
-    R.job_bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel) + image_bytes(o);
+    R.job_bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel) + image_bytes(o) -
+                  (R.session_accum ? accum_bytes : 0u);  // a session's accumulator is counted with the session
     s->resident += R.job_bytes;
     s->active[R.lane][jid] = R.id;
     std::lock_guard<std::mutex> lock(s->mu);
     R.t_admit = seconds_since(s->t0);
+}
+
+void free_session(venu_server* s, std::unordered_map<uint64_t, Session>::iterator it) {
+    if (it->second.accum) cudaFreeAsync(it->second.accum, s->st);
+    s->resident -= it->second.bytes;
+    s->sessions.erase(it);
+}
+
+// Frees a session's accumulator, now or -- while one of its requests is
+// admitted -- when that request completes.
+void end_session(venu_server* s, uint64_t id) {
+    auto it = s->sessions.find(id);
+    if (it == s->sessions.end()) return;
+    if (it->second.busy) it->second.end_pending = true;
+    else free_session(s, it);
 }
 
 void fail_all_active(venu_server* s, venu_status st) {
@@ -272,9 +347,8 @@ venu_status run_lane(venu_server* s, int l, uint32_t max_iter, std::vector<uint3
     }
     cudaError_t ce = cudaStreamSynchronize(s->st);
     for (Request* R : done) {
-        cudaFreeAsync(R->accum, s->st);
+        release_accum(s, *R);
         cudaFreeAsync(R->image8, s->st);
-        R->accum = nullptr;
         R->image8 = nullptr;
         s->resident -= R->job_bytes;
         release_scene(s, R->scene_key);
@@ -301,19 +375,30 @@ void server_loop(venu_server* s) {
         // admission, first come first served
         for (;;) {
             Request* R = nullptr;
+            bool skipped = false;
+            std::vector<uint64_t> ending;
             {
                 std::lock_guard<std::mutex> lock(s->mu);
-                if (s->pending.empty()) break;
-                R = s->reqs[s->pending.front()].get();
-                if (R->cancelled) {
-                    s->pending.pop_front();
-                    R = nullptr;
+                // session ends requested before this request was submitted
+                // apply to it: take them in the same critical section
+                ending.swap(s->sessions_to_end);
+                if (!s->pending.empty()) {
+                    R = s->reqs[s->pending.front()].get();
+                    if (R->cancelled) {
+                        s->pending.pop_front();
+                        R = nullptr;
+                        skipped = true;
+                    }
                 }
             }
-            if (!R) {
-                continue;
-            }
+            for (uint64_t id : ending) end_session(s, id);
+            if (skipped) continue;
+            if (!R) break;
             if (R->cancelled) continue;
+            if (R->req.session) {  // one request of a session at a time, in order
+                auto si = s->sessions.find(R->req.session);
+                if (si != s->sessions.end() && si->second.busy) break;
+            }
             const venu_render_opts& o = R->req.opts;
             const uint64_t key = R->req.scene_key ? R->req.scene_key : (kPrivateKey | R->id);
             const bool cached = s->scenes.count(key) != 0;
@@ -373,8 +458,12 @@ void server_loop(venu_server* s) {
         s->segments = bst.segments + bsx.segments;
         if (s->stop && s->n_active_all() == 0) break;
     }
-    // shut down: fail what is left
+    // shut down: fail what is left, drop the sessions
     fail_all_active(s, VENU_ERR_CANCELLED);
+    for (auto& kv : s->sessions)
+        if (kv.second.accum) cudaFreeAsync(kv.second.accum, s->st);
+    s->sessions.clear();
+    cudaStreamSynchronize(s->st);
     std::deque<uint64_t> left;
     {
         std::lock_guard<std::mutex> lock(s->mu);
@@ -476,6 +565,17 @@ extern "C" venu_status venu_server_set_policy(venu_server* s, uint32_t policy) {
     }
     s->policy.store(policy);
     venu_batch_interrupt(s->batch, 1u);  // applied at the start of the next step
+    return VENU_OK;
+}
+
+extern "C" venu_status venu_server_end_session(venu_server* s, uint64_t session) {
+    if (!s || session == 0) {
+        set_error("venu_server_end_session: NULL server or session 0");
+        return VENU_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->sessions_to_end.push_back(session);
+    s->cv_work.notify_all();
     return VENU_OK;
 }
 
