@@ -144,6 +144,39 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     return rate, dt, sample, res["segments"]
 
 
+def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, subframe):
+    """The same render as one job of the batch engine: one pool of 16 Mi
+    paths regenerated continuously (no waves, no tails), one graph launch.
+    The accumulator must equal the plain renderer's bit for bit."""
+    b = venu.Batch(pool_paths=16 << 20, max_jobs=1)
+    if tuning:
+        b.set_tuning(**tuning)
+    acc_b, acc_p = venu.new_accum(W, H), venu.new_accum(W, H)
+    wf = venu.Wavefront(16 << 20)
+    if tuning:
+        wf.set_tuning(**tuning)
+    wf.render(ds, cam, W, H, spp, acc_p, subframe=subframe, max_depth=depth, reset=True)
+
+    def one():
+        b.submit(ds, cam, W, H, spp, acc_b, subframe=subframe, max_depth=depth, reset=True)
+        b.run()
+        assert len(b.collect()) == 1
+
+    one()  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    one()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    same = bool(torch.equal(acc_b, acc_p))
+    b.close()
+    return {"value": segs_step / (ms / 1000.0), "unit": UNIT, "ms": ms, "identical_accumulator": same,
+            "method": "the headline render as one job of the batch engine: continuous path regeneration in a "
+                      "16 Mi-path pool, one graph launch (includes its seed-table kernel)"}
+
+
 def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
     """The plain method (one venu_render per job, in sequence) against the
     batched engine (all jobs in one shared pool, one graph launch) on the
@@ -594,6 +627,8 @@ def main():
         "roofline": roofline,
     }
     if not args.no_batched and world == 1:
+        line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step,
+                                                    args.warmup + args.steps)
         line["batched"] = run_batched(venu, torch, tuning, max_paths)
         line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True)
         line["served"] = run_served(venu, torch, tuning)

@@ -44,7 +44,7 @@ struct LoopCtl {  // device-owned loop state
     uint32_t cnt[2], work[2];
     uint32_t iter, running, more_gen, take_total, out_base, plan_n, err;
     uint32_t job_finished;  // set when a job's last path finishes (reset per run)
-    uint32_t parity;        // the queue traced in this iteration; flipped by k_loop_cond
+    uint32_t parity;        // the queue traced in this iteration; flipped by k_plan
     uint32_t pad;
     unsigned long long segments, paths_done, iterations;
 };
@@ -77,13 +77,19 @@ __global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t s
     }
 }
 
-// sequential: a job gets slots only once every job before it in the order
-// has finished all its paths (one job at a time, as rendering them in turn).
+// Plans the next iteration and decides whether there is one.  sequential:
+// a job gets slots only once every job before it in the order has finished
+// all its paths (one job at a time, as rendering them in turn).  The loop
+// condition: more rays or paths to generate, and none of the iteration cap,
+// "a job just finished" (stop-on-finish) or the host's interrupt word (mapped
+// host memory, read volatile).  Flips the queue parity: the queue filled
+// now is the one the next iteration traces.
 __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
                        const unsigned long long* __restrict__ job_done,
                        const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
                        uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
-                       uint32_t* __restrict__ plan_off, uint32_t Q) {
+                       uint32_t* __restrict__ plan_off, uint32_t Q, const volatile uint32_t* interrupt,
+                       cudaGraphConditionalHandle handle, int use_handle) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const uint32_t survivors = ctl->cnt[out];
@@ -113,13 +119,23 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
     ctl->more_gen = more;
     ctl->cnt[in] = 0;   // the next trace writes into the other queue
     ctl->work[out] = 0; // and fetches from this one
+    ctl->parity = (uint32_t)out;
+    const uint32_t it = ctl->iter + 1u;
+    ctl->iter = it;
+    ctl->iterations += 1u;
+    uint32_t go = (survivors + off > 0u || more) ? 1u : 0u;
+    if (run->max_iter && it >= run->max_iter) go = 0u;
+    if (run->stop_on_finish && ctl->job_finished) go = 0u;  // hand finished jobs to the host now
+    if (*interrupt) go = 0u;                                 // the host has new work to admit
+    ctl->running = go;
+    if (use_handle) cudaGraphSetConditional(handle, go);
 }
 
 __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restrict__ ctl,
                         const uint32_t* __restrict__ plan_job, const unsigned long long* __restrict__ plan_start,
                         const uint32_t* __restrict__ plan_off, Queue q0, Queue q1) {
     const uint32_t total = ctl->take_total, base = ctl->out_base, np = ctl->plan_n;
-    const Queue q = (ctl->parity & 1u) ? q0 : q1;  // the output queue of this iteration
+    const Queue q = (ctl->parity & 1u) ? q1 : q0;  // filled now, traced next (k_plan flipped the parity)
     for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         // last plan entry i with plan_off[i] <= t (entries may be empty)
         uint32_t lo = 0, hi = np;  // invariant: plan_off[lo] <= t < plan_off[hi]
@@ -196,23 +212,6 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
     if (overflow) atomicOr(&ctl->err, 1u);
 }
 
-// interrupt: a word in mapped host memory (venu_batch_interrupt), read once
-// per iteration; volatile so every read goes to the host copy.
-__global__ void k_loop_cond(LoopCtl* ctl, const RunCtl* __restrict__ run, const volatile uint32_t* interrupt,
-                            cudaGraphConditionalHandle handle, int use_handle) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const uint32_t it = ctl->iter + 1u;
-    ctl->iter = it;
-    ctl->iterations += 1u;
-    const uint32_t next = (ctl->parity & 1u) ^ 1u;  // the queue the next iteration traces
-    ctl->parity = next;
-    uint32_t more = (ctl->cnt[next] > 0u || ctl->more_gen) ? 1u : 0u;
-    if (run->max_iter && it >= run->max_iter) more = 0u;
-    if (run->stop_on_finish && ctl->job_finished) more = 0u;  // hand finished jobs to the host now
-    if (*interrupt) more = 0u;                                 // the host has new work to admit
-    ctl->running = more;
-    if (use_handle) cudaGraphSetConditional(handle, more);
-}
 
 // Accumulate (Kahan, sample order) and resolve finished jobs: one thread per
 // pixel of the listed jobs.
@@ -303,17 +302,17 @@ cudaError_t batch_configure(venu_batch* b) {
     return cudaSuccess;
 }
 
-// One iteration of the path loop (trace the parity queue, plan, regenerate
-// into the other) + the condition, which flips the parity.
+// One iteration of the path loop: trace the parity queue, plan (which also
+// sets the loop condition and flips the parity), regenerate into the queue
+// the next iteration traces.
 cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
     const size_t sm = traverse_smem((int)b->tune.traverse_block);
     k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
                                                                                   b->q[0], b->q[1]);
-    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_order, b->d_run, b->d_ctl, b->d_plan_job, b->d_plan_start,
-                             b->d_plan_off, b->Q);
+    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
+                             b->d_plan_start, b->d_plan_off, b->Q, b->d_interrupt, b->handle, use_handle ? 1 : 0);
     k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
                                              b->q[0], b->q[1]);
-    k_loop_cond<<<1, 32, 0, st>>>(b->d_ctl, b->d_run, b->d_interrupt, b->handle, use_handle ? 1 : 0);
     return cudaGetLastError();
 }
 
