@@ -144,18 +144,19 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     return rate, dt, sample, res["segments"]
 
 
-def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, subframe):
-    """The same render as one job of the batch engine: one pool of 16 Mi
-    paths regenerated continuously (no waves, no tails), one graph launch.
-    The accumulator must equal the plain renderer's bit for bit."""
-    b = venu.Batch(pool_paths=16 << 20, max_jobs=1)
+def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, subframe, pool):
+    """The same render as one job of the batch engine: one pool of paths
+    regenerated continuously (no waves, no tails), one graph launch.  The
+    accumulator must equal the plain renderer's bit for bit."""
+    b = venu.Batch(pool_paths=pool, max_jobs=1)
     if tuning:
         b.set_tuning(**tuning)
     acc_b, acc_p = venu.new_accum(W, H), venu.new_accum(W, H)
-    wf = venu.Wavefront(16 << 20)
+    wf = venu.Wavefront(pool)
     if tuning:
         wf.set_tuning(**tuning)
     wf.render(ds, cam, W, H, spp, acc_p, subframe=subframe, max_depth=depth, reset=True)
+    wf.close()
 
     def one():
         b.submit(ds, cam, W, H, spp, acc_b, subframe=subframe, max_depth=depth, reset=True)
@@ -174,7 +175,7 @@ def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, su
     b.close()
     return {"value": segs_step / (ms / 1000.0), "unit": UNIT, "ms": ms, "identical_accumulator": same,
             "method": "the headline render as one job of the batch engine: continuous path regeneration in a "
-                      "16 Mi-path pool, one graph launch (includes its seed-table kernel)"}
+                      f"{pool >> 20} Mi-path pool, one graph launch (includes its seed-table kernel)"}
 
 
 def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
@@ -253,7 +254,7 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
 def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, iters=64):
     """Serving: a Poisson request stream at ~80 % of the server's capacity
     through the render server (continuous batching, resident BVHs, 150 GB HBM
-    budget) in two configurations -- one lane, FIFO, 16 Mi-path pool; and an
+    budget) in two configurations -- one lane, FIFO, 64 Mi-path pool; and an
     express lane for requests of at most 4 Mi paths ahead of a sequential
     8 Mi-path bulk lane -- against the plain method serving the same stream
     one job at a time.  All scenes are resident before each stream starts,
@@ -292,7 +293,7 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
                 self.srv.wait(self.submit(dict(j, W=16, H=16, spp=1)))
 
     # capacity: a burst of requests all at once through the one-lane server
-    srv = venu.Server(budget, pool_paths=16 << 20, max_jobs=256, iterations_per_step=iters)
+    srv = venu.Server(budget, pool_paths=64 << 20, max_jobs=256, iterations_per_step=iters)
     cl = Client(srv)
     calib = workloads.serving_jobs(24, rate_per_s=1.0, seed=2)
     cl.warm(calib)
@@ -338,7 +339,7 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     out = {}
     cl.warm(jobs)
     out["server_fifo"], segs = stream(cl)
-    out["server_fifo"]["config"] = "one lane, FIFO plan order, 16 Mi-path pool"
+    out["server_fifo"]["config"] = "one lane, FIFO plan order, 64 Mi-path pool"
     srv.close()
     srv = venu.Server(budget, pool_paths=8 << 20, max_jobs=256, iterations_per_step=iters, express_paths=4 << 20)
     srv.set_policy("sequential")
@@ -349,8 +350,9 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
                                        "sequential bulk lane with an 8 Mi-path pool")
     srv.close()
 
-    # the plain method: one job at a time, same arrivals, resident BVHs
-    wf = venu.Wavefront(16 << 20)
+    # the plain method: one job at a time, same arrivals, resident BVHs,
+    # waves of up to 128 Mi paths (every path of a request in one wave)
+    wf = venu.Wavefront(128 << 20)
     if tuning:
         wf.set_tuning(**tuning)
     dscenes = {k: venu.DeviceScene(v) for k, v in scenes.items()}
@@ -460,15 +462,17 @@ def main():
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
-    max_paths = args.max_paths
+    # Wave size: every path of the render in flight when it fits, else the
+    # largest wave (128 Mi paths, ~16 GB of queues): fewer waves, fewer tails
+    # (measured on RTIOW 1080p x 256: 16 Mi 8.6, 32 Mi 9.8, 64 Mi 10.3,
+    # 128 Mi 10.7 G segments/s).
+    max_paths = args.max_paths or int(min(128 << 20, W * H * spp))
     if args.tuning:
         tuning = json.loads(args.tuning)
     elif not args.no_autotune:
         from venusaur_gb300 import tune
 
-        tuning, best_mp, tune_log = tune.autotune(
-            ds, cam, W, H, spp, depth, max_paths=(args.max_paths,) if args.max_paths else (4 << 20, 8 << 20, 16 << 20))
-        max_paths = best_mp
+        tuning, _, tune_log = tune.autotune(ds, cam, W, H, spp, depth, max_paths=(max_paths,))
     wf = venu.Wavefront(max_paths)
     if tuning:
         wf.set_tuning(**tuning)
@@ -606,6 +610,7 @@ def main():
     e2e_s = rep.max(t1 - t0)
     e2e = {"value": total_segs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(spheres.nbytes),
            "d2h_bytes_per_step": int(H * W * 4), "ms_per_step": 1000 * e2e_s / args.steps}
+    wf_plain.close()
 
     if rank != 0:
         return
@@ -628,7 +633,7 @@ def main():
     }
     if not args.no_batched and world == 1:
         line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step,
-                                                    args.warmup + args.steps)
+                                                    args.warmup + args.steps, max_paths)
         line["batched"] = run_batched(venu, torch, tuning, max_paths)
         line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True)
         line["served"] = run_served(venu, torch, tuning)

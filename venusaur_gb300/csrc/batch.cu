@@ -405,7 +405,7 @@ extern "C" venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs,
     *out = nullptr;
     venu_status ds = require_device();
     if (ds != VENU_OK) return ds;
-    if (pool_paths == 0) pool_paths = 16u << 20;
+    if (pool_paths == 0) pool_paths = 64u << 20;
     if (max_jobs == 0 || max_jobs > kMaxJobs || pool_paths > (1u << 28)) {
         set_error("venu_batch_create: need 1 <= max_jobs <= 4096 and pool_paths <= 2^28");
         return VENU_ERR_INVALID;

@@ -326,7 +326,8 @@ size_t traverse_smem(int block) { return (size_t)block * kShared * (sizeof(int) 
 using namespace venu;
 
 struct venu_renderer {
-    uint32_t Q = 0;
+    uint32_t Q = 0;     // paths the queues hold now (grown on demand up to Qmax)
+    uint32_t Qmax = 0;  // the wave size asked for at creation
     uint32_t flags = 0;
     Queue q[2] = {};
     int2* hits = nullptr;
@@ -396,16 +397,43 @@ cudaError_t next_events(venu_renderer* r, cudaEvent_t& a, cudaEvent_t& b) {
     return cudaSuccess;
 }
 
-void free_renderer(venu_renderer* r) {
-    for (cudaEvent_t e : r->ev) cudaEventDestroy(e);
-    r->ev.clear();
+void free_queues(venu_renderer* r) {
     for (int i = 0; i < 2; ++i) {
         cudaFree(r->q[i].o);
         cudaFree(r->q[i].d);
         cudaFree(r->q[i].t);
+        r->q[i] = Queue{};
     }
     cudaFree(r->hits);
     cudaFree(r->slots);
+    r->hits = nullptr;
+    r->slots = nullptr;
+    r->Q = 0;
+}
+
+// Path queues for waves of Q paths (96 B + 8 B hit + 16 B slot per path).
+cudaError_t alloc_queues(venu_renderer* r, uint32_t Q) {
+    free_queues(r);
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].o, sizeof(float4) * (size_t)Q);
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].d, sizeof(float4) * (size_t)Q);
+        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].t, sizeof(float4) * (size_t)Q);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&r->hits, sizeof(int2) * (size_t)Q);
+    if (e == cudaSuccess) e = cudaMalloc(&r->slots, sizeof(float4) * (size_t)Q);
+    if (e != cudaSuccess) {
+        free_queues(r);
+        return e;
+    }
+    r->Q = Q;
+    return cudaSuccess;
+}
+
+void free_renderer(venu_renderer* r) {
+    for (cudaEvent_t e : r->ev) cudaEventDestroy(e);
+    r->ev.clear();
+    free_queues(r);
     cudaFree(r->seeds);
     cudaFree(r->cnt);
     cudaFree(r->work);
@@ -422,24 +450,15 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     *out = nullptr;
     venu_status ds = require_device();
     if (ds != VENU_OK) return ds;
-    if (max_paths == 0) max_paths = 16u << 20;
-    if (max_paths > (1u << 27)) {
-        set_error("venu_renderer_create: max_paths above 2^27");
+    if (max_paths == 0) max_paths = 64u << 20;
+    if (max_paths > (1u << 28)) {
+        set_error("venu_renderer_create: max_paths above 2^28");
         return VENU_ERR_TOO_LARGE;
     }
     venu_renderer* r = new venu_renderer();
-    r->Q = max_paths;
+    r->Qmax = max_paths;  // the queues are sized by the first render that needs them
     r->flags = flags;
-    cudaError_t e = cudaSuccess;
-    const size_t Q = max_paths;
-    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
-        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].o, sizeof(float4) * Q);
-        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].d, sizeof(float4) * Q);
-        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].t, sizeof(float4) * Q);
-    }
-    if (e == cudaSuccess) e = cudaMalloc(&r->hits, sizeof(int2) * Q);
-    if (e == cudaSuccess) e = cudaMalloc(&r->slots, sizeof(float4) * Q);
-    if (e == cudaSuccess) e = cudaMalloc(&r->cnt, sizeof(uint32_t) * (kMaxDepth + 1));
+    cudaError_t e = cudaMalloc(&r->cnt, sizeof(uint32_t) * (kMaxDepth + 1));
     if (e == cudaSuccess) e = cudaMalloc(&r->work, sizeof(uint32_t) * (kMaxDepth + 1));
     if (e == cudaSuccess) e = cudaMalloc(&r->err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 4);
@@ -530,6 +549,19 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     const bool count = (r->flags & VENU_RENDERER_COUNT) != 0;
     const bool prof = (r->flags & VENU_RENDERER_PROFILE) != 0;
     r->ev_used = 0;
+    {
+        // queues for waves of min(all paths of this call, Qmax): a small render
+        // holds no more memory than it uses; grown (never shrunk) on demand
+        const uint64_t want = std::min<uint64_t>((uint64_t)npix * spp, r->Qmax);
+        if (want > r->Q) {
+            VENU_CUDA(cudaStreamSynchronize(st));
+            const cudaError_t ae = alloc_queues(r, (uint32_t)want);
+            if (ae != cudaSuccess) {
+                set_error("venu_render: cannot allocate path queues for " + std::to_string(want) + " paths");
+                return VENU_ERR_OOM;
+            }
+        }
+    }
     const venu_tuning& tu = r->tune;
     const size_t tsm = traverse_smem((int)tu.traverse_block);
     const int tb = (int)tu.traverse_block, sb = (int)tu.shade_block;
