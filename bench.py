@@ -561,10 +561,11 @@ def main():
     # per segment from a capture of the same kernel on a smaller case of the
     # same scene (the queue traffic, which grows in proportion to the rays;
     # the node set stays cache-resident), scaled to this launch's segments.
-    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.6 B) and
-    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (87.2 B).
-    # (c1's queues fit in L2: no figure for it.)
-    dram_per_seg = {"c2": 86.6, "c3": 87.2}.get(args.config) if variant == 2 else None
+    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.6 B),
+    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (87.2 B) and, for the
+    # separate traversal kernel, profiles/k_traverse_random1m_1920x1080_2spp.md
+    # (37.1 B).  (c1's queues fit in L2: no figure for it.)
+    dram_per_seg = {("c2", 2): 86.6, ("c3", 2): 87.2, ("c3", 0): 37.1}.get((args.config, variant))
     traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"]) if dram_per_seg else None
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
