@@ -257,3 +257,40 @@ def test_tuning_rejects_bad_values(venu, cuda):
         wf.set_tuning(traverse_block=96)
     with pytest.raises(venu.VenuError):
         wf.set_tuning(refill_min=0)
+
+
+def _edge_scene(oracle, case):
+    sp = oracle.scene_rtiow(0).copy()
+    if case == "hollow_glass":  # RTIOW's hollow bubble: a negative radius inside the glass sphere
+        inner = sp[1:2].copy()
+        inner["radius"] = -0.9
+        sp = np.concatenate([sp, inner])
+    elif case == "zero_radius":
+        sp["radius"][10:40] = 0.0
+    elif case == "duplicates":  # exact copies: equal hits resolved by the smaller slot
+        sp = np.concatenate([sp, sp[4:60]])
+    elif case == "many_huge":  # more huge spheres than are hoisted
+        big = sp[:9].copy()
+        big["center"][:, 0] = np.arange(9) * 3000.0 - 12000.0
+        big["center"][:, 1] = -1000.0
+        big["radius"] = 1000.0
+        sp = np.concatenate([sp, big])
+    elif case == "too_many_huge":  # more than 64 huge spheres: none hoisted
+        big = np.repeat(sp[:1], 70)
+        big["center"][:, 0] = np.arange(70) * 2500.0 - 80000.0
+        sp = np.concatenate([sp, big])
+    return sp
+
+
+@pytest.mark.parametrize("case", ["hollow_glass", "zero_radius", "duplicates", "many_huge", "too_many_huge"])
+def test_edge_scenes_bit_exact(venu, oracle, cuda, case):
+    sp = _edge_scene(oracle, case)
+    ds = _dev_scene(venu, sp)
+    got, want = ds.export_bvh(), oracle.lbvh(sp)
+    assert np.array_equal(got["ids"], want["ids"]) and got["nodes"].tobytes() == want["nodes"].tobytes()
+    W, H, spp = 40, 24, 3
+    cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    acc, _, _, st = _render_gpu(venu, cuda, sp, cam, W, H, spp, 1, 12)
+    ref = oracle.render(sp, cam, W, H, spp, subframe=1, max_depth=12, mode=pyoracle.MODE_GB300)
+    assert np.array_equal(acc.view(np.uint32), ref["accum"].view(np.uint32))
+    assert st["segments"] == ref["segments"]
