@@ -256,7 +256,8 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     through the render server (continuous batching, resident BVHs, 150 GB HBM
     budget) in two configurations -- one lane, FIFO, 64 Mi-path pool; and an
     express lane for requests of at most 4 Mi paths ahead of a sequential
-    8 Mi-path bulk lane -- against the plain method serving the same stream
+    64 Mi-path bulk lane that yields every 4 Mi rays -- against the plain
+    method serving the same stream
     one job at a time.  All scenes are resident before each stream starts,
     for every method."""
     import threading
@@ -341,13 +342,13 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     out["server_fifo"], segs = stream(cl)
     out["server_fifo"]["config"] = "one lane, FIFO plan order, 64 Mi-path pool"
     srv.close()
-    srv = venu.Server(budget, pool_paths=8 << 20, max_jobs=256, iterations_per_step=iters, express_paths=4 << 20)
+    srv = venu.Server(budget, pool_paths=64 << 20, max_jobs=256, iterations_per_step=iters, express_paths=4 << 20)
     srv.set_policy("sequential")
     cl = Client(srv)
     cl.warm(jobs)
     out["server_express"], segs = stream(cl)
     out["server_express"]["config"] = ("express lane (2 Mi-path pool) for requests of <= 4 Mi paths, "
-                                       "sequential bulk lane with an 8 Mi-path pool")
+                                       "sequential bulk lane with a 64 Mi-path pool yielding every 4 Mi rays")
     srv.close()
 
     # the plain method: one job at a time, same arrivals, resident BVHs,

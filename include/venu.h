@@ -304,10 +304,12 @@ VENU_API uint64_t venu_batch_job_bytes(uint32_t width, uint32_t height, uint32_t
  * seeds on `stream`.  The scene and output buffers must stay valid until the
  * job is collected.  VENU_ERR_TOO_LARGE when max_jobs are admitted. */
 VENU_API venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id);
-/* Runs the shared path loop for at most max_iterations iterations (0 = until
- * every admitted job has finished) as one graph launch on `stream`; with
- * VENU_RUN_STOP_ON_FINISH the loop also ends after the iteration in which a
- * job's last path finished, so a server can hand results out at once. */
+/* Runs the shared path loop for at most max_iterations steps (0 = until
+ * every admitted job has finished) as one graph launch on `stream`; a step
+ * is one iteration (every queued ray traced once) unless venu_batch_set_chunk
+ * splits iterations.  With VENU_RUN_STOP_ON_FINISH the loop also ends after
+ * the step in which a job's last path finished, so a server can hand results
+ * out at once. */
 #define VENU_RUN_STOP_ON_FINISH 1u
 VENU_API venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, uint32_t flags, void* stream);
 /* Waits for `stream`, then accumulates, resolves and releases every finished
@@ -333,6 +335,13 @@ VENU_API venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy);
  * a host with new jobs can admit them without waiting for the run.  The only
  * batch call that may be made from another host thread. */
 VENU_API venu_status venu_batch_interrupt(venu_batch* b, uint32_t on);
+/* Rays traced per loop step (0, the default: a whole iteration, every queued
+ * ray, per step).  With a chunk, an iteration over a large pool is split into
+ * steps of at most `rays` rays, and the iteration cap, stop-on-finish and the
+ * interrupt take effect at step boundaries: a host can admit or run other
+ * work after at most one chunk instead of one whole-pool iteration.  Results
+ * do not depend on it. */
+VENU_API venu_status venu_batch_set_chunk(venu_batch* b, uint32_t rays);
 VENU_API venu_status venu_batch_stats_get(venu_batch* b, venu_batch_stats* out);
 VENU_API venu_status venu_batch_destroy(venu_batch* b);
 
@@ -404,9 +413,10 @@ VENU_API venu_status venu_server_submit(venu_server* s, const venu_request* req,
 VENU_API venu_status venu_server_set_policy(venu_server* s, uint32_t policy);
 /* Express lane: requests of at most max_paths paths (width x height x spp)
  * admitted from now on run in a second, small pool (2 Mi paths) that the
- * server advances ahead of the bulk pool at every step; 0 (the default)
- * turns it off.  A small request then waits for at most one iteration of
- * the bulk pool instead of sharing every bounce with the large jobs. */
+ * server advances ahead of the bulk pool at every step, and the bulk pool
+ * yields every 4 Mi traced rays; 0 (the default) turns it off.  A small
+ * request then waits for at most one bulk chunk instead of sharing every
+ * bounce with the large jobs. */
 VENU_API venu_status venu_server_set_express(venu_server* s, uint64_t max_paths);
 /* Frees a progressive session's accumulator (after its admitted request, if
  * any, completes); a later request with the same id starts a new session. */

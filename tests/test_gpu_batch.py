@@ -192,3 +192,30 @@ def test_batch_interrupt(venu, oracle, cuda):
     assert b.collect() == [j["id"]]
     torch.cuda.synchronize()
     assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))
+
+
+@pytest.mark.parametrize("chunk", [1, 100, 7777])
+def test_batch_chunked_steps(venu, oracle, cuda, chunk):
+    """Iterations split into steps of `chunk` rays: the same accumulators;
+    stop-on-finish, step caps and interrupts act at step boundaries."""
+    torch = cuda
+    b = venu.Batch(pool_paths=3000, max_jobs=8)
+    b.set_chunk(chunk)
+    sub = _submit_all(venu, torch, b, oracle, _jobs(oracle))
+    got = []
+    b.interrupt(True)
+    b.run()
+    assert b.stats()["iterations"] == 1  # one step, then the interrupt
+    b.interrupt(False)
+    for _ in range(100000):
+        b.run(max_iterations=37, stop_on_finish=True)
+        got += b.collect()
+        if len(got) == len(sub):
+            break
+    assert sorted(got) == sorted(s["id"] for s in sub)
+    torch.cuda.synchronize()
+    total = 0
+    for s in sub:
+        assert np.array_equal(s["acc"].cpu().numpy().view(np.uint32), s["want"]["accum"].view(np.uint32))
+        total += s["want"]["segments"]
+    assert b.stats()["segments"] == total

@@ -170,6 +170,7 @@ def lib() -> C.CDLL:
     L.venu_batch_destroy.argtypes = [vp]
     L.venu_batch_set_policy.argtypes = [vp, u32]
     L.venu_batch_interrupt.argtypes = [vp, u32]
+    L.venu_batch_set_chunk.argtypes = [vp, u32]
     L.venu_server_set_policy.argtypes = [vp, u32]
     L.venu_server_set_express.argtypes = [vp, C.c_uint64]
     L.venu_server_end_session.argtypes = [vp, C.c_uint64]
@@ -182,7 +183,7 @@ def lib() -> C.CDLL:
                  "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
                  "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit",
                  "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy",
-                 "venu_batch_set_policy", "venu_batch_interrupt", "venu_server_set_policy", "venu_server_set_express", "venu_server_end_session",
+                 "venu_batch_set_policy", "venu_batch_interrupt", "venu_batch_set_chunk", "venu_server_set_policy", "venu_server_set_express", "venu_server_end_session",
                  "venu_server_create", "venu_server_submit", "venu_server_wait", "venu_server_cancel",
                  "venu_server_release", "venu_server_inject", "venu_server_stats_get", "venu_server_destroy"):
         getattr(L, name).restype = C.c_int

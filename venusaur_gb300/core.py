@@ -566,6 +566,10 @@ class Batch:
         shortest_first / fifo)."""
         check(lib().venu_batch_set_policy(self.handle, _policy(policy)))
 
+    def set_chunk(self, rays: int) -> None:
+        """Rays traced per loop step (0: whole iterations)."""
+        check(lib().venu_batch_set_chunk(self.handle, int(rays)))
+
     def interrupt(self, on: bool = True) -> None:
         """Ends a running run() at its next iteration boundary while set."""
         check(lib().venu_batch_interrupt(self.handle, 1 if on else 0))

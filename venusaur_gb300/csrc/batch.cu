@@ -45,12 +45,13 @@ struct LoopCtl {  // device-owned loop state
     uint32_t iter, running, more_gen, take_total, out_base, plan_n, err;
     uint32_t job_finished;  // set when a job's last path finishes (reset per run)
     uint32_t parity;        // the queue traced in this iteration; flipped by k_plan
-    uint32_t pad;
+    uint32_t chunk_end;     // this step traces input rays [work start, chunk_end)
     unsigned long long segments, paths_done, iterations;
 };
 
 struct RunCtl {  // host-written before each run
     uint32_t max_iter, nactive, stop_on_finish, sequential;
+    uint32_t chunk, pad[3];  // rays traced per step (0: the whole input queue)
 };
 
 struct CollectEntry {
@@ -77,21 +78,16 @@ __global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t s
     }
 }
 
-// Plans the next iteration and decides whether there is one.  sequential:
-// a job gets slots only once every job before it in the order has finished
-// all its paths (one job at a time, as rendering them in turn).  The loop
-// condition: more rays or paths to generate, and none of the iteration cap,
-// "a job just finished" (stop-on-finish) or the host's interrupt word (mapped
-// host memory, read volatile).  Flips the queue parity: the queue filled
-// now is the one the next iteration traces.
-__global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
-                       const unsigned long long* __restrict__ job_done,
-                       const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
-                       uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
-                       uint32_t* __restrict__ plan_off, uint32_t Q, const volatile uint32_t* interrupt,
-                       cudaGraphConditionalHandle handle, int use_handle) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const int in = (int)(ctl->parity & 1u), out = 1 - in;
+// Hands the free pool slots to the jobs (plan order) and flips the parity;
+// returns whether any work is left.  sequential: a job gets slots only once
+// every job before it in the order has finished all its paths (one job at a
+// time, as rendering them in turn).
+__device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
+                                   const unsigned long long* __restrict__ job_done,
+                                   const uint32_t* __restrict__ order, const RunCtl* __restrict__ run,
+                                   LoopCtl* ctl, uint32_t* __restrict__ plan_job,
+                                   unsigned long long* __restrict__ plan_start, uint32_t* __restrict__ plan_off,
+                                   uint32_t Q, int in, int out, uint32_t chunk) {
     const uint32_t survivors = ctl->cnt[out];
     const uint32_t free = survivors < Q ? Q - survivors : 0u;
     const uint32_t na = run->nactive;
@@ -117,19 +113,49 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
     ctl->out_base = survivors;
     ctl->cnt[out] = survivors + off;
     ctl->more_gen = more;
-    ctl->cnt[in] = 0;   // the next trace writes into the other queue
-    ctl->work[out] = 0; // and fetches from this one
+    ctl->cnt[in] = 0;    // the next trace writes into the other queue
+    ctl->work[out] = 0;  // and fetches from this one, chunk by chunk
+    ctl->chunk_end = min(chunk, survivors + off);
     ctl->parity = (uint32_t)out;
+    return (survivors + off > 0u || more) ? 1u : 0u;
+}
+
+// Decides the next step and whether there is one.  The loop condition: more rays or paths to generate, and none of the step cap, "a job
+// just finished" (stop-on-finish) or the host's interrupt word (mapped host
+// memory, read volatile).  A step traces a chunk of the input queue
+// (RunCtl::chunk rays, all of them when 0); while input rays are left the
+// next step takes the next chunk, else this plans the next iteration and
+// flips the queue parity: the queue filled now is the one traced next.
+__global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
+                       const unsigned long long* __restrict__ job_done,
+                       const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
+                       uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
+                       uint32_t* __restrict__ plan_off, uint32_t Q, const volatile uint32_t* interrupt,
+                       cudaGraphConditionalHandle handle, int use_handle) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const int in = (int)(ctl->parity & 1u), out = 1 - in;
+    const uint32_t chunk = run->chunk ? run->chunk : 0xffffffffu;
     const uint32_t it = ctl->iter + 1u;
     ctl->iter = it;
     ctl->iterations += 1u;
-    uint32_t go = (survivors + off > 0u || more) ? 1u : 0u;
+    uint32_t go;
+    const uint32_t n_in = ctl->cnt[in], done_to = ctl->chunk_end;
+    if (done_to < n_in) {  // input rays left: the next chunk of this queue
+        ctl->work[in] = done_to;
+        ctl->chunk_end = done_to + min(chunk, n_in - done_to);
+        ctl->take_total = 0u;  // no regeneration this step
+        go = 1u;
+    } else {
+        go = plan_iteration(jobs, job_next, job_done, order, run, ctl, plan_job, plan_start, plan_off, Q, in, out,
+                            chunk);
+    }
     if (run->max_iter && it >= run->max_iter) go = 0u;
     if (run->stop_on_finish && ctl->job_finished) go = 0u;  // hand finished jobs to the host now
     if (*interrupt) go = 0u;                                 // the host has new work to admit
     ctl->running = go;
     if (use_handle) cudaGraphSetConditional(handle, go);
 }
+
 
 __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restrict__ ctl,
                         const uint32_t* __restrict__ plan_job, const unsigned long long* __restrict__ plan_start,
@@ -166,12 +192,11 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
     sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
     const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const Queue qin = in ? q1 : q0, qout = in ? q0 : q1;
-    const uint32_t n = ctl->cnt[in];
+    const uint32_t n = ctl->chunk_end;  // this step: input rays [work[in] at launch, chunk_end)
     const uint32_t lane = threadIdx.x & 31;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctl->segments, (unsigned long long)n);
     TraceCounters K{0, 0};
     bool overflow = false;
-    uint32_t finished = 0;
+    uint32_t finished = 0, traced = 0;
     for (;;) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&ctl->work[in], 32u);
@@ -179,6 +204,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
         if (base >= n) break;
         const uint32_t i = base + lane;
         const bool valid = i < n;
+        traced += (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
         uint32_t job = 0xFFFFFFFFu;
         ShadeOut r;
         r.cont = false;
@@ -209,6 +235,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
         finished += __popc(__ballot_sync(0xffffffffu, fin));
     }
     if (lane == 0 && finished) atomicAdd(&ctl->paths_done, (unsigned long long)finished);
+    if (lane == 0 && traced) atomicAdd(&ctl->segments, (unsigned long long)traced);
     if (overflow) atomicOr(&ctl->err, 1u);
 }
 
@@ -273,6 +300,7 @@ struct venu_batch {
     std::vector<JobHost> jobs;
     std::vector<uint32_t> order;  // active job slots in plan order (policy)
     uint32_t policy = VENU_POLICY_FIFO;
+    uint32_t chunk = 0;  // rays traced per step (0: a whole iteration per step)
     uint64_t next_seq = 0;
     uint32_t* h_interrupt = nullptr;  // mapped host word
     uint32_t* d_interrupt = nullptr;  // its device address
@@ -549,6 +577,8 @@ extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, ui
     rc.nactive = (uint32_t)b->order.size();
     rc.stop_on_finish = (flags & VENU_RUN_STOP_ON_FINISH) ? 1u : 0u;
     rc.sequential = b->policy == VENU_POLICY_SEQUENTIAL ? 1u : 0u;
+    rc.chunk = b->chunk;
+    rc.pad[0] = rc.pad[1] = rc.pad[2] = 0u;
     VENU_CUDA(cudaMemcpyAsync(b->d_run, &rc, sizeof(rc), cudaMemcpyHostToDevice, st));
     VENU_CUDA(cudaMemsetAsync(&b->d_ctl->iter, 0, sizeof(uint32_t), st));
     VENU_CUDA(cudaMemsetAsync(&b->d_ctl->job_finished, 0, sizeof(uint32_t), st));
@@ -644,6 +674,15 @@ extern "C" venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy) {
     }
     b->policy = policy;
     return upload_order(b, nullptr);
+}
+
+extern "C" venu_status venu_batch_set_chunk(venu_batch* b, uint32_t rays) {
+    if (!b) {
+        set_error("venu_batch_set_chunk: NULL batch");
+        return VENU_ERR_INVALID;
+    }
+    b->chunk = rays;
+    return VENU_OK;
 }
 
 extern "C" venu_status venu_batch_interrupt(venu_batch* b, uint32_t on) {

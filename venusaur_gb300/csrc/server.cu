@@ -75,6 +75,7 @@ struct SceneEntry {
 
 constexpr uint64_t kPrivateKey = 1ull << 63;  // scenes of requests without a key
 constexpr uint32_t kExpressPool = 2u << 20;    // paths in flight in the express lane
+constexpr uint32_t kBulkChunk = 4u << 20;      // bulk rays per step while the express lane is on
 
 uint64_t scene_estimate(uint32_t n) { return (uint64_t)n * 72u + 256u; }
 uint64_t image_bytes(const venu_render_opts& o) {
@@ -105,6 +106,7 @@ struct venu_server {
     std::string fatal_msg;
     std::atomic<uint32_t> policy{VENU_POLICY_FIFO};  // plan order, applied by the server thread
     uint32_t applied_policy = VENU_POLICY_FIFO;
+    uint64_t applied_express = 0;
 
     std::atomic<uint64_t> express_paths{0};  // 0: one lane
     // owned by the server thread
@@ -371,6 +373,12 @@ void server_loop(venu_server* s) {
                 venu_batch_set_policy(s->batch, pol);  // the express lane stays FIFO
                 s->applied_policy = pol;
             }
+            // with the express lane on, the bulk pool yields every kBulkChunk
+            // rays, so small requests wait at most one chunk, not one whole
+            // bulk iteration
+            const uint64_t xp = s->express_paths.load();
+            if ((xp != 0) != (s->applied_express != 0)) venu_batch_set_chunk(s->batch, xp ? kBulkChunk : 0u);
+            s->applied_express = xp;
         }
         // admission, first come first served
         for (;;) {
