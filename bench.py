@@ -547,6 +547,9 @@ def main():
     if fused:
         kernel = "k_trace_shade"
         kbytes = trav_bytes + segs_c * 112
+    elif variant == 3:  # fused primary bounce, separate traversal after it
+        kernel = "k_trace_shade (primary) + k_traverse"
+        kbytes = trav_bytes + paths_c * 112 + (segs_c - paths_c) * 40
     else:
         kernel = "k_traverse"
         kbytes = trav_bytes + segs_c * 40

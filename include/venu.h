@@ -253,7 +253,8 @@ typedef struct venu_tuning {
     uint32_t traverse_variant;       /* 0: each warp takes 32 rays and runs them to the end;
                                         1: idle lanes take new rays;
                                         2: as 0, then the warp shades its 32 hits in the same
-                                           kernel (no separate shade launch; default) */
+                                           kernel (no separate shade launch; default);
+                                        3: 2 for the primary rays, 0 for later bounces */
     uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */

@@ -232,6 +232,8 @@ def test_empty_and_tiny_scenes(venu, oracle, cuda):
     dict(traverse_variant=1, refill_min=16, traverse_block=128, shade_block=512, traverse_blocks_per_sm=2),
     dict(traverse_variant=2, refill_min=8, traverse_block=128, shade_block=256),
     dict(traverse_variant=2, refill_min=8, traverse_block=256, shade_block=256, traverse_blocks_per_sm=1),
+    dict(traverse_variant=3, refill_min=8, traverse_block=128, shade_block=256),
+    dict(traverse_variant=3, refill_min=32, traverse_block=256, shade_block=128, traverse_blocks_per_sm=2),
 ])
 def test_render_tunings_bit_exact(venu, oracle, cuda, tuning):
     """Launch shapes and traversal variants change speed, never bits."""

@@ -339,7 +339,7 @@ struct venu_renderer {
     uint32_t* err = nullptr;
     unsigned long long* stats = nullptr;  // segments, nodes, spheres
     venu_tuning tune = {2u, 32u, 128u, 0u, 128u, 0u};
-    int trav_blocks = 0, shade_blocks = 0;
+    int trav_blocks = 0, shade_blocks = 0, fused_blocks = 0;
     venu_render_stats last = {};
     // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
     std::vector<cudaEvent_t> ev;
@@ -367,13 +367,20 @@ cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
     const size_t sm = traverse_smem((int)t.traverse_block);
     cudaError_t e;
-    if (t.traverse_variant == 0) {
+    if (t.traverse_variant == 3) {  // fused primary bounce, then variant 0
+        e = occupancy_grid(k_trace_shade<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->fused_blocks);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+    }
+    if (t.traverse_variant == 0 || t.traverse_variant == 3) {
         e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     } else if (t.traverse_variant == 2) {
         e = occupancy_grid(k_trace_shade<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_trace_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        r->fused_blocks = r->trav_blocks;
     } else {
         e = occupancy_grid(k_traverse_dyn<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess)
@@ -480,7 +487,7 @@ extern "C" venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tun
         set_error("venu_renderer_set_tuning: NULL argument");
         return VENU_ERR_INVALID;
     }
-    const bool ok = t->traverse_variant <= 2u && t->refill_min >= 1u && t->refill_min <= 32u &&
+    const bool ok = t->traverse_variant <= 3u && t->refill_min >= 1u && t->refill_min <= 32u &&
                     (t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) &&
                     t->shade_block >= 64u && t->shade_block <= 512u && (t->shade_block % 32u) == 0u &&
                     t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u;
@@ -593,13 +600,16 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                     VENU_CUDA(next_events(r, e2, e3));
                     VENU_CUDA(cudaEventRecord(e0, st));
                 }
-                if (tu.traverse_variant == 2) {
+                // variant 3: the coherent primary rays fused, the divergent
+                // later bounces with the separate traversal kernel
+                const uint32_t v = tu.traverse_variant <= 2u ? tu.traverse_variant : (b == 0 ? 2u : 0u);
+                if (v == 2) {
                     if (count)
-                        k_trace_shade<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
-                                                                            r->cnt + b + 1, r->slots, r->err, r->stats);
-                    else
-                        k_trace_shade<false><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
+                        k_trace_shade<true><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
                                                                              r->cnt + b + 1, r->slots, r->err, r->stats);
+                    else
+                        k_trace_shade<false><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
+                                                                              r->cnt + b + 1, r->slots, r->err, r->stats);
                     if (prof) {
                         VENU_CUDA(cudaEventRecord(e1, st));
                         VENU_CUDA(cudaEventRecord(e2, st));
@@ -608,7 +618,7 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                     launches += 1;
                     continue;
                 }
-                if (tu.traverse_variant == 0) {
+                if (v == 0) {
                     if (count)
                         k_traverse<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
                                                                          r->err, r->stats);

@@ -13,7 +13,7 @@ import itertools
 from .core import DeviceScene, Wavefront, new_accum
 
 DEFAULT_SPACE = {
-    "traverse_variant": (0, 1, 2),
+    "traverse_variant": (0, 1, 2, 3),
     "refill_min": (4, 8, 16),
     "traverse_block": (64, 128, 256),
     "shade_block": (128, 256),
@@ -27,7 +27,7 @@ def candidates(space=None):
                                           space["traverse_block"], space["shade_block"]):
         # the refill threshold matters to the dynamic-fetch variant only, the
         # shade block to the variants with a separate shade kernel only
-        key = (v, r if v == 1 else 32, tb, sb if v in (0, 1) else 256)
+        key = (v, r if v == 1 else 32, tb, sb if v != 2 else 256)
         if key in seen:
             continue
         seen.add(key)
