@@ -127,12 +127,20 @@ __device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned lon
 // next step takes the next chunk, else this plans the next iteration and
 // flips the queue parity: the queue filled now is the one traced next.
 __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
-                       const unsigned long long* __restrict__ job_done,
+                       const unsigned long long* __restrict__ job_done, uint32_t* __restrict__ job_seen,
                        const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
                        uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
                        uint32_t* __restrict__ plan_off, uint32_t Q, const volatile uint32_t* interrupt,
                        cudaGraphConditionalHandle handle, int use_handle) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    // jobs whose last path finished in this step
+    for (uint32_t i = 0; i < run->nactive; ++i) {
+        const uint32_t j = order[i];
+        if (!job_seen[j] && job_done[j] >= jobs[j].total) {
+            job_seen[j] = 1u;
+            ctl->job_finished = 1u;
+        }
+    }
     const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const uint32_t chunk = run->chunk ? run->chunk : 0xffffffffu;
     const uint32_t it = ctl->iter + 1u;
@@ -183,7 +191,7 @@ __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restri
 }
 
 template <bool COUNT>
-__global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
+__global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
                                                            unsigned long long* __restrict__ job_done, LoopCtl* ctl,
                                                            Queue q0, Queue q1) {
     extern __shared__ unsigned char smem[];
@@ -228,10 +236,9 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade_multi(const DevJob* __restrict__
         const bool fin = valid && !r.cont;
         const uint32_t key = fin ? job : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(0xffffffffu, key);
-        if (fin && lane == (uint32_t)(__ffs(peers) - 1)) {
-            const unsigned long long add = (unsigned long long)__popc(peers);
-            if (atomicAdd(&job_done[job], add) + add == jobs[job].total) atomicExch(&ctl->job_finished, 1u);
-        }
+        // (the result is not read: a fire-and-forget reduction; k_plan
+        // notices finished jobs)
+        if (fin && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&job_done[job], (unsigned long long)__popc(peers));
         finished += __popc(__ballot_sync(0xffffffffu, fin));
     }
     if (lane == 0 && finished) atomicAdd(&ctl->paths_done, (unsigned long long)finished);
@@ -293,6 +300,7 @@ struct venu_batch {
     Queue q[2] = {};
     DevJob* d_jobs = nullptr;
     unsigned long long *d_next = nullptr, *d_done = nullptr, *d_plan_start = nullptr;
+    uint32_t* d_seen = nullptr;  // per job: finish already reported by k_plan
     uint32_t *d_order = nullptr, *d_plan_job = nullptr, *d_plan_off = nullptr;
     LoopCtl* d_ctl = nullptr;
     RunCtl* d_run = nullptr;
@@ -337,7 +345,7 @@ cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
     const size_t sm = traverse_smem((int)b->tune.traverse_block);
     k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
                                                                                   b->q[0], b->q[1]);
-    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
+    k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_seen, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
                              b->d_plan_start, b->d_plan_off, b->Q, b->d_interrupt, b->handle, use_handle ? 1 : 0);
     k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
                                              b->q[0], b->q[1]);
@@ -389,6 +397,7 @@ void free_batch(venu_batch* b) {
     cudaFree(b->d_jobs);
     cudaFree(b->d_next);
     cudaFree(b->d_done);
+    cudaFree(b->d_seen);
     cudaFree(b->d_plan_start);
     cudaFree(b->d_order);
     cudaFree(b->d_plan_job);
@@ -453,6 +462,7 @@ extern "C" venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs,
     if (e == cudaSuccess) e = cudaMalloc(&b->d_jobs, sizeof(DevJob) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned long long) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_done, sizeof(unsigned long long) * max_jobs);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_seen, sizeof(uint32_t) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_plan_start, sizeof(unsigned long long) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_order, sizeof(uint32_t) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_plan_job, sizeof(uint32_t) * max_jobs);
@@ -555,6 +565,7 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     VENU_CUDA(cudaMemcpyAsync(b->d_jobs + slot, &dj, sizeof(dj), cudaMemcpyHostToDevice, st));
     VENU_CUDA(cudaMemsetAsync(b->d_next + slot, 0, sizeof(unsigned long long), st));
     VENU_CUDA(cudaMemsetAsync(b->d_done + slot, 0, sizeof(unsigned long long), st));
+    VENU_CUDA(cudaMemsetAsync(b->d_seen + slot, 0, sizeof(uint32_t), st));
     k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(job->camera, o.width, o.height, o.samples_per_pixel,
                                                                  o.subframe_index, J.seeds);
     VENU_CUDA(cudaGetLastError());

@@ -25,6 +25,11 @@
 #define VENU_TRACE_MAXREG 64
 #endif
 #define VENU_TRACE_BOUNDS __maxnreg__(VENU_TRACE_MAXREG)
+// The multi-job kernel of the batch engine keeps a per-ray scene view.
+#ifndef VENU_TRACE_MULTI_MAXREG
+#define VENU_TRACE_MULTI_MAXREG 64
+#endif
+#define VENU_TRACE_MULTI_BOUNDS __maxnreg__(VENU_TRACE_MULTI_MAXREG)
 
 namespace venu {
 
