@@ -190,6 +190,13 @@ __global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restri
     }
 }
 
+// A pointer read that the compiler may not merge with an earlier read of the
+// same field (so the value is not kept live in a register meanwhile).
+template <typename T>
+__device__ __forceinline__ T ld_volatile_ptr(const T* p) {
+    return *reinterpret_cast<const volatile T*>(p);
+}
+
 template <bool COUNT>
 __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
                                                            unsigned long long* __restrict__ job_done, LoopCtl* ctl,
@@ -219,11 +226,21 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
         if (valid) {
             const float4 o4 = qin.o[i], d4 = qin.d[i];
             job = __float_as_uint(d4.w) >> 8;
-            const SceneView S = jobs[job].scene;
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
             float t;
-            const int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
-            r = shade_one(S, o4, d4, qin.t[i], make_int2(__float_as_int(t), k));
+            int32_t k;
+            {
+                const SceneView S = jobs[job].scene;
+                k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            }
+            // the shading pointers are read again here instead of being kept in
+            // registers through the traversal (the job table is L1/L2-resident)
+            SceneView S2;
+            const SceneView* G = &jobs[job].scene;
+            S2.sph = ld_volatile_ptr(&G->sph);
+            S2.mat = ld_volatile_ptr(&G->mat);
+            S2.meta = ld_volatile_ptr(&G->meta);
+            r = shade_one(S2, o4, d4, qin.t[i], make_int2(__float_as_int(t), k));
             if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(o4.w)] = r.result;
         }
         const uint32_t pos = warp_append(r.cont, &ctl->cnt[out]);
