@@ -178,6 +178,29 @@ def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, su
                       f"{pool >> 20} Mi-path pool, one graph launch (includes its seed-table kernel)"}
 
 
+def profile_mixed(venu, torch, args):
+    """A few steps of the mixed workload for a profiler: its first 12 jobs
+    (2.3 GB of seed tables and sample slots) admitted to a 16 Mi-path pool,
+    the host-driven loop, the given launch shapes."""
+    from venusaur_gb300 import workloads
+
+    jobs = workloads.mixed_jobs(64)[:12]
+    b = venu.Batch(pool_paths=16 << 20, max_jobs=len(jobs), graph=False)
+    b.set_tuning(**(json.loads(args.tuning) if args.tuning else dict(traverse_variant=2, traverse_block=256)))
+    scenes, keep = {}, []
+    for j in jobs:
+        key = (j["n"], j["scene_seed"])
+        if key not in scenes:
+            scenes[key] = venu.DeviceScene(venu.generate_random(j["n"], j["scene_seed"]))
+        cam = venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
+        acc = venu.new_accum(j["W"], j["H"])
+        keep.append(acc)
+        b.submit(scenes[key], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"], max_depth=j["depth"])
+    b.run(max_iterations=args.profile_mixed)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_mixed": b.stats()}))
+
+
 def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
     """The plain method (one venu_render per job, in sequence) against the
     batched engine (all jobs in one shared pool, one graph launch) on the
@@ -425,6 +448,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
     ap.add_argument("--tuning", default="", help="JSON launch shapes to use instead of the autotuner's")
+    ap.add_argument("--profile-mixed", type=int, default=0, metavar="STEPS",
+                    help="only run STEPS loop steps of the first 12 jobs of the mixed workload (~4 GB on the "
+                         "device) through the batch engine's host-driven loop (ncu cannot profile kernels "
+                         "inside conditional graphs) and exit")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
@@ -446,6 +473,9 @@ def main():
     from venusaur_gb300 import build as vb
 
     vb.build()
+    if args.profile_mixed:
+        profile_mixed(venu, torch, args)
+        return
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     spheres = make_scene(venu, cfg["scene"])
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
