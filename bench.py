@@ -144,6 +144,36 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     return rate, dt, sample, res["segments"]
 
 
+def rmse_vs_reference(venu, torch, O, ds, spheres, cam, W, H, depth, spp=16):
+    """Per-pixel RMSE of the GPU image against the reference's arithmetic
+    (the oracle's REF mode: the reference's own RayTracer.cu semantics --
+    double-precision dielectric, pow() Schlick, half-b quadratic,
+    brute-force closest hit -- pinned bit-exactly to the reference's code
+    compiled for the host) at the same seeds on the middle row, beside the
+    seed-to-seed noise of the same estimate."""
+    from oracle import pyoracle
+
+    row = H // 2
+    acc = venu.new_accum(W, H)
+    wf = venu.Wavefront(0)
+    wf.render(ds, cam, W, H, spp, acc, subframe=0, max_depth=depth, reset=True)
+    a = acc.cpu().numpy()[row * W:(row + 1) * W]
+    gpu = a[:, :3] / a[:, 3:4]
+    wf.render(ds, cam, W, H, spp, acc, subframe=7, max_depth=depth, reset=True)
+    b = acc.cpu().numpy()[row * W:(row + 1) * W]
+    other_seeds = b[:, :3] / b[:, 3:4]
+    wf.close()
+    ref = O.render(spheres, cam, W, H, spp, subframe=0, max_depth=depth, mode=pyoracle.MODE_REF,
+                   rows=(row, row + 1))["accum"][row * W:(row + 1) * W, :3]
+    rmse = float(np.sqrt(((gpu - ref) ** 2).mean()))
+    noise = float(np.sqrt(((other_seeds - ref) ** 2).mean()))
+    return {"value": rmse, "seed_noise": noise,
+            "sample": f"row {row}, {W} px x {spp} spp, depth {depth}, subframe 0 (same seeds); seed_noise: "
+                      "the same against subframe 7",
+            "against": "the reference's arithmetic (oracle REF mode, bit-exact with the reference's own "
+                       "RayTracer.cu built for the host)"}
+
+
 def run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step, subframe, pool):
     """The same render as one job of the batch engine: one pool of paths
     regenerated continuously (no waves, no tails), one graph launch.  The
@@ -674,6 +704,7 @@ def main():
         line["served"] = run_served(venu, torch, tuning)
     if cpu_baseline is not None:
         line["cpu_baseline"] = cpu_baseline
+        line["rmse_vs_reference"] = rmse_vs_reference(venu, torch, O, ds, spheres, cam, W, H, depth)
     print(json.dumps(line), flush=True)
 
 
