@@ -325,7 +325,8 @@ VENU_API venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t* f
  * submission order, and a job gets slots only once every earlier job has
  * finished all its paths (no overlap: a job's last bounces are not slowed
  * by the next job's rays; the pool runs part-empty meanwhile).  Results do
- * not depend on the order. */
+ * not depend on the order.  Call between runs, not while a venu_batch_run
+ * is in flight. */
 #define VENU_POLICY_FIFO 0u
 #define VENU_POLICY_SHORTEST_FIRST 1u
 #define VENU_POLICY_SEQUENTIAL 2u
