@@ -231,7 +231,7 @@ def profile_mixed(venu, torch, args):
     print(json.dumps({"profile_mixed": b.stats()}))
 
 
-def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
+def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune=True):
     """The plain method (one venu_render per job, in sequence) against the
     batched engine (all jobs in one shared pool, one graph launch) on the
     mixed-scene workload (or, small=True, on many small RTIOW renders).
@@ -247,16 +247,27 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
             sp = venu.generate_rtiow(j["rtiow_seed"]) if small else venu.generate_random(j["n"], j["scene_seed"])
             scenes[key] = venu.DeviceScene(sp)
     cams = [venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0) for j in jobs]
+    # launch shapes for both methods, and the batch pool size, from the
+    # autotuner on a reduced copy of this job set (every 4th job, at most
+    # 16 spp: ~80 Mi paths of the mixed set, more than the largest pool):
+    # each method gets its own best settings
+    if autotune:
+        from venusaur_gb300 import tune
+
+        red = [dict(scene=scenes[j["key"]], camera=c, W=j["W"], H=j["H"], spp=min(j["spp"], 16), depth=j["depth"],
+                    subframe=j["subframe"]) for j, c in list(zip(jobs, cams))[::4]]
+        tuning, batch_tuning, _ = tune.autotune_jobs(red, pools=(16 << 20, 32 << 20, 64 << 20, 128 << 20))
+    else:
+        batch_tuning = {"pool_paths": max_paths, "traverse_block": 256}
     acc_plain = [venu.new_accum(j["W"], j["H"]) for j in jobs]
     acc_batch = [venu.new_accum(j["W"], j["H"]) for j in jobs]
     img_plain = [torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda") for j in jobs]
     img_batch = [torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda") for j in jobs]
-    wf = venu.Wavefront(max_paths)
+    wf = venu.Wavefront(128 << 20)
     if tuning:
         wf.set_tuning(**tuning)
-    b = venu.Batch(pool_paths=max_paths, max_jobs=len(jobs))
-    if tuning:
-        b.set_tuning(**tuning)
+    b = venu.Batch(pool_paths=batch_tuning["pool_paths"], max_jobs=len(jobs))
+    b.set_tuning(traverse_variant=2, traverse_block=batch_tuning["traverse_block"])
 
     def plain(rep):
         segs = 0
@@ -296,9 +307,10 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False):
         "workload": desc,
         "paths": workloads.paths(jobs), "segments": int(segs),
         "plain": {"value": segs / (p_ms / 1000), "ms": p_ms, "wall_ms": p_wall,
-                  "method": "venu_render per job, in sequence"},
+                  "method": "venu_render per job, in sequence (waves of up to 128 Mi paths)",
+                  "tuning": tuning},
         "batched": {"value": segs / (b_ms / 1000), "ms": b_ms, "wall_ms": b_wall,
-                    "method": "one shared path pool, one graph launch", "pool_paths": max_paths},
+                    "method": "one shared path pool, one graph launch", "tuning": batch_tuning},
         "speedup": p_ms / b_ms,
         "identical_accumulators": bool(same_all),
     }
@@ -699,8 +711,9 @@ def main():
     if not args.no_batched and world == 1:
         line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step,
                                                     args.warmup + args.steps, max_paths)
-        line["batched"] = run_batched(venu, torch, tuning, max_paths)
-        line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True)
+        retune = not (args.tuning or args.no_autotune)
+        line["batched"] = run_batched(venu, torch, tuning, max_paths, autotune=retune)
+        line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True, autotune=retune)
         line["served"] = run_served(venu, torch, tuning)
     if cpu_baseline is not None:
         line["cpu_baseline"] = cpu_baseline

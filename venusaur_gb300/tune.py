@@ -69,3 +69,72 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
                 best = (rate, dict(cand), mp)
         wf.close()
     return best[1], best[2], results
+
+
+def _time(fn) -> float:
+    import torch
+
+    fn()  # warm
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    fn()
+    ev1.record()
+    torch.cuda.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def autotune_jobs(jobs, pools=(16 << 20, 32 << 20, 64 << 20), blocks=(64, 128, 256), space=None, log=None):
+    """Tunes both ways of rendering a set of jobs on (a reduced copy of) it.
+
+    jobs: list of dicts {scene: DeviceScene, camera, W, H, spp, depth,
+    subframe}.  Returns (plain_tuning, batch_tuning, results):
+    plain_tuning -- the venu_tuning fields that render the jobs fastest one
+    by one; batch_tuning -- the batch engine's pool size and block shape
+    that render them fastest together in one pool (the batch always traces
+    and shades in one kernel).  Results never change any image.
+    """
+    from .core import Batch
+
+    results = []
+    accs = [new_accum(j["W"], j["H"]) for j in jobs]
+    cands = list(candidates(space))
+    wf = Wavefront(max(min(128 << 20, max(j["W"] * j["H"] * j["spp"] for j in jobs)), 1 << 20))
+
+    def plain():
+        for j, a in zip(jobs, accs):
+            wf.render(j["scene"], j["camera"], j["W"], j["H"], j["spp"], a, subframe=j["subframe"],
+                      max_depth=j["depth"], reset=True)
+
+    best_plain = None
+    for cand in cands:
+        wf.set_tuning(**cand)
+        ms = _time(plain)
+        results.append(dict(cand, method="plain", ms=ms))
+        if log:
+            log(results[-1])
+        if best_plain is None or ms < best_plain[0]:
+            best_plain = (ms, dict(cand))
+    wf.close()
+
+    best_batch = None
+    for pool in pools:
+        b = Batch(pool_paths=pool, max_jobs=len(jobs))
+        for tb in blocks:
+            b.set_tuning(traverse_variant=2, traverse_block=tb)
+
+            def batched():
+                for j, a in zip(jobs, accs):
+                    b.submit(j["scene"], j["camera"], j["W"], j["H"], j["spp"], a, subframe=j["subframe"],
+                             max_depth=j["depth"], reset=True)
+                b.run()
+                b.collect()
+
+            ms = _time(batched)
+            results.append(dict(method="batched", pool_paths=pool, traverse_block=tb, ms=ms))
+            if log:
+                log(results[-1])
+            if best_batch is None or ms < best_batch[0]:
+                best_batch = (ms, dict(pool_paths=pool, traverse_block=tb))
+        b.close()
+    return best_plain[1], best_batch[1], results
