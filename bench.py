@@ -129,16 +129,21 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
     res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
                    rows=(r0, r0 + rows))
     dt = max(time.perf_counter() - t0, 1e-3)
-    seg_per_path = res["segments"] / (rows * W * spp_s)
-    want_paths = (res["segments"] / dt) * target_s / max(seg_per_path, 1e-9)
-    spp_s = min(spp, 4)
-    rows = int(max(2, min(H - r0, want_paths / (W * spp_s))))
-    if rows == H - r0:
-        spp_s = int(max(spp_s, min(spp, want_paths / (W * rows))))
-    t0 = time.perf_counter()
-    res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
-                   rows=(r0, r0 + rows))
-    dt = time.perf_counter() - t0
+    # a small probe underestimates a many-core rate (thread start-up), so
+    # re-size from each run until a run lasts at least half the target
+    for _ in range(3):
+        seg_per_path = res["segments"] / (rows * W * spp_s)
+        want_paths = (res["segments"] / dt) * target_s / max(seg_per_path, 1e-9)
+        spp_s = min(spp, 4)
+        rows = int(max(2, min(H - r0, want_paths / (W * spp_s))))
+        if rows == H - r0:
+            spp_s = int(max(spp_s, min(spp, want_paths / (W * rows))))
+        t0 = time.perf_counter()
+        res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
+                       rows=(r0, r0 + rows))
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * target_s or (rows == H - r0 and spp_s == spp):
+            break
     rate = res["segments"] / dt
     sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
     return rate, dt, sample, res["segments"]
