@@ -5,13 +5,15 @@
 // scene.  Instead of one wavefront per job, all jobs feed one pool of paths
 // in flight:
 //
-//   trace+shade  every queued ray against its own job's LBVH, shaded, the
-//                survivors compacted into the other queue (the job index
-//                rides in the upper bits of the depth word);
-//   plan         one thread hands the free queue slots to the admitted jobs
+//   trace+shade  every ray of the iteration against its own job's LBVH,
+//                shaded, the survivors compacted into the other queue (the
+//                job index rides in the upper bits of the depth word).  The
+//                iteration's rays are the queued survivors followed by the
+//                new paths the last plan handed out: those camera rays are
+//                made in the kernel, from each job's precomputed raygen
+//                seed table, and never pass through memory;
+//   plan         one thread hands the free pool slots to the admitted jobs
 //                in plan order (submission order, or shortest first);
-//   regen        new camera rays for the planned (job, sample, pixel)
-//                triples, from each job's precomputed raygen seed table;
 //
 // repeated under a device-side while condition, so the whole loop is one
 // CUDA graph launch.  Which of the two queues is the input alternates each
@@ -42,7 +44,10 @@ struct DevJob {
 
 struct LoopCtl {  // device-owned loop state
     uint32_t cnt[2], work[2];
-    uint32_t iter, running, more_gen, take_total, out_base, plan_n, err;
+    uint32_t iter, running, more_gen;
+    uint32_t gen_n;     // new paths of this iteration (made by the trace kernel) ...
+    uint32_t gen_base;  // ... at input indices [gen_base, gen_base + gen_n), after the survivors
+    uint32_t plan_n, err;
     uint32_t job_finished;  // set when a job's last path finishes (reset per run)
     uint32_t parity;        // the queue traced in this iteration; flipped by k_plan
     uint32_t chunk_end;     // this step traces input rays [work start, chunk_end)
@@ -109,8 +114,8 @@ __device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned lon
     }
     plan_off[na] = off;
     ctl->plan_n = na;
-    ctl->take_total = off;
-    ctl->out_base = survivors;
+    ctl->gen_n = off;
+    ctl->gen_base = survivors;
     ctl->cnt[out] = survivors + off;
     ctl->more_gen = more;
     ctl->cnt[in] = 0;    // the next trace writes into the other queue
@@ -151,7 +156,6 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
     if (done_to < n_in) {  // input rays left: the next chunk of this queue
         ctl->work[in] = done_to;
         ctl->chunk_end = done_to + min(chunk, n_in - done_to);
-        ctl->take_total = 0u;  // no regeneration this step
         go = 1u;
     } else {
         go = plan_iteration(jobs, job_next, job_done, order, run, ctl, plan_job, plan_start, plan_off, Q, in, out,
@@ -165,29 +169,31 @@ __global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __re
 }
 
 
-__global__ void k_regen(const DevJob* __restrict__ jobs, const LoopCtl* __restrict__ ctl,
-                        const uint32_t* __restrict__ plan_job, const unsigned long long* __restrict__ plan_start,
-                        const uint32_t* __restrict__ plan_off, Queue q0, Queue q1) {
-    const uint32_t total = ctl->take_total, base = ctl->out_base, np = ctl->plan_n;
-    const Queue q = (ctl->parity & 1u) ? q1 : q0;  // filled now, traced next (k_plan flipped the parity)
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
-        // last plan entry i with plan_off[i] <= t (entries may be empty)
-        uint32_t lo = 0, hi = np;  // invariant: plan_off[lo] <= t < plan_off[hi]
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (plan_off[mid] <= t) lo = mid; else hi = mid;
-        }
-        const uint32_t j = plan_job[lo];
-        const DevJob& J = jobs[j];
-        const unsigned long long l = plan_start[lo] + (t - plan_off[lo]);
-        const uint32_t s = (uint32_t)(l / J.npix);
-        const uint32_t pix = (uint32_t)(l - (unsigned long long)s * J.npix);
-        uint32_t seed = J.seeds[l];
-        const DevCamera C = load_camera(J.cam);
-        f3 o, d;
-        camera_ray(C, pix % J.W, pix / J.W, J.W, J.H, seed, o, d);
-        write_primary(q, base + t, o, d, (uint32_t)l, (int)J.max_depth - 1, seed, j);
+// The camera ray of new path t of the iteration (t < gen_n): its plan entry
+// (the last entry i with plan_off[i] <= t; entries may be empty), job, sample
+// and pixel, from the job's seed table -- what k_raygen writes to the queue
+// for venu_render.  Path numbers within a job fit 31 bits (venu_batch_submit).
+__device__ __forceinline__ void gen_primary(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ plan_job,
+                                            const unsigned long long* __restrict__ plan_start,
+                                            const uint32_t* __restrict__ plan_off, uint32_t np, uint32_t t,
+                                            float4& o4, float4& d4, uint32_t& seed) {
+    uint32_t lo = 0, hi = np;  // invariant: plan_off[lo] <= t < plan_off[hi]
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (plan_off[mid] <= t) lo = mid; else hi = mid;
     }
+    const uint32_t j = plan_job[lo];
+    const DevJob& J = jobs[j];
+    const uint32_t l = (uint32_t)(plan_start[lo] + (t - plan_off[lo]));
+    const uint32_t npix = J.npix, W = J.W;
+    const uint32_t s = l / npix;
+    const uint32_t pix = l - s * npix;
+    seed = J.seeds[l];
+    const DevCamera C = load_camera(J.cam);
+    f3 o, d;
+    camera_ray(C, pix % W, pix / W, W, J.H, seed, o, d);
+    o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)l));
+    d4 = make_float4(d.x, d.y, d.z, __uint_as_float((j << 8) | ((uint32_t)((int)J.max_depth - 1) & kDepthMask)));
 }
 
 // A pointer read that the compiler may not merge with an earlier read of the
@@ -200,6 +206,9 @@ __device__ __forceinline__ T ld_volatile_ptr(const T* p) {
 template <bool COUNT>
 __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
                                                            unsigned long long* __restrict__ job_done, LoopCtl* ctl,
+                                                           const uint32_t* __restrict__ plan_job,
+                                                           const unsigned long long* __restrict__ plan_start,
+                                                           const uint32_t* __restrict__ plan_off,
                                                            Queue q0, Queue q1) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
@@ -208,6 +217,7 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
     const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const Queue qin = in ? q1 : q0, qout = in ? q0 : q1;
     const uint32_t n = ctl->chunk_end;  // this step: input rays [work[in] at launch, chunk_end)
+    const uint32_t gen_base = ctl->gen_base, np = ctl->plan_n;  // new paths from gen_base on
     const uint32_t lane = threadIdx.x & 31;
     TraceCounters K{0, 0};
     bool overflow = false;
@@ -224,7 +234,15 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
         ShadeOut r;
         r.cont = false;
         if (valid) {
-            const float4 o4 = qin.o[i], d4 = qin.d[i];
+            const bool fresh = i >= gen_base;
+            float4 o4, d4;
+            uint32_t seed = 0;
+            if (fresh) {
+                gen_primary(jobs, plan_job, plan_start, plan_off, np, i - gen_base, o4, d4, seed);
+            } else {
+                o4 = qin.o[i];
+                d4 = qin.d[i];
+            }
             job = __float_as_uint(d4.w) >> 8;
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
             float t;
@@ -240,7 +258,8 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
             S2.sph = ld_volatile_ptr(&G->sph);
             S2.mat = ld_volatile_ptr(&G->mat);
             S2.meta = ld_volatile_ptr(&G->meta);
-            r = shade_one(S2, o4, d4, qin.t[i], make_int2(__float_as_int(t), k));
+            const float4 t4 = fresh ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
+            r = shade_one(S2, o4, d4, t4, make_int2(__float_as_int(t), k));
             if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(o4.w)] = r.result;
         }
         const uint32_t pos = warp_append(r.cont, &ctl->cnt[out]);
@@ -330,7 +349,7 @@ struct venu_batch {
     uint32_t* h_interrupt = nullptr;  // mapped host word
     uint32_t* d_interrupt = nullptr;  // its device address
     venu_tuning tune = {2u, 8u, 256u, 0u, 256u, 0u};
-    int trav_blocks = 0, regen_blocks = 0;
+    int trav_blocks = 0;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -351,21 +370,17 @@ cudaError_t batch_configure(venu_batch* b) {
     per_sm = std::max(1, per_sm);
     if (b->tune.traverse_blocks_per_sm) per_sm = std::min(per_sm, (int)b->tune.traverse_blocks_per_sm);
     b->trav_blocks = per_sm * sm_count();
-    b->regen_blocks = 4 * sm_count();
     return cudaSuccess;
 }
 
-// One iteration of the path loop: trace the parity queue, plan (which also
-// sets the loop condition and flips the parity), regenerate into the queue
-// the next iteration traces.
+// One iteration of the path loop: trace the parity queue and the planned new
+// paths, then plan (which also sets the loop condition and flips the parity).
 cudaError_t launch_body(venu_batch* b, cudaStream_t st, bool use_handle) {
     const size_t sm = traverse_smem((int)b->tune.traverse_block);
-    k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(b->d_jobs, b->d_done, b->d_ctl,
-                                                                                  b->q[0], b->q[1]);
+    k_trace_shade_multi<false><<<b->trav_blocks, b->tune.traverse_block, sm, st>>>(
+        b->d_jobs, b->d_done, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off, b->q[0], b->q[1]);
     k_plan<<<1, 32, 0, st>>>(b->d_jobs, b->d_next, b->d_done, b->d_seen, b->d_order, b->d_run, b->d_ctl, b->d_plan_job,
                              b->d_plan_start, b->d_plan_off, b->Q, b->d_interrupt, b->handle, use_handle ? 1 : 0);
-    k_regen<<<b->regen_blocks, 256, 0, st>>>(b->d_jobs, b->d_ctl, b->d_plan_job, b->d_plan_start, b->d_plan_off,
-                                             b->q[0], b->q[1]);
     return cudaGetLastError();
 }
 

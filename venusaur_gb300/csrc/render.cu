@@ -20,9 +20,15 @@
 
 namespace venu {
 
+// Camera rays of one wave (P pixels from p0, k samples from s0): path
+// pos = s * P + pl.  With path_seeds, only each path's raygen seed is written
+// (4 bytes instead of a 48-byte queue entry) and the fused kernel makes the
+// camera ray itself (PrimaryGen); the pixel's seed still advances through
+// every sample's draws, which is what fixes the next sample's seed.
 __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, uint32_t P, uint32_t s0,
                          uint32_t k, uint32_t subframe, int max_depth, uint32_t* __restrict__ seeds,
-                         Queue q, uint32_t* __restrict__ cnt, uint32_t* __restrict__ work, int nbounce) {
+                         Queue q, uint32_t* __restrict__ path_seeds, uint32_t* __restrict__ cnt,
+                         uint32_t* __restrict__ work, int nbounce) {
     const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
     if (pl == 0) {
         cnt[0] = P * k;
@@ -35,10 +41,11 @@ __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, u
     const uint32_t x = pix % W, y = pix / W;
     uint32_t seed = (s0 == 0) ? tea4(pix, subframe) : seeds[pix];
     for (uint32_t s = 0; s < k; ++s) {
+        const uint32_t pos = s * P + pl;
+        if (path_seeds) path_seeds[pos] = seed;
         f3 o, d;
         camera_ray(C, x, y, W, H, seed, o, d);
-        const uint32_t pos = s * P + pl;
-        write_primary(q, pos, o, d, pos, max_depth - 1, seed);
+        if (!path_seeds) write_primary(q, pos, o, d, pos, max_depth - 1, seed);
     }
     seeds[pix] = seed;
 }
@@ -166,7 +173,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
                                                      uint32_t* __restrict__ work, Queue qout,
                                                      uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                      uint32_t* __restrict__ err,
-                                                     unsigned long long* __restrict__ stats) {
+                                                     unsigned long long* __restrict__ stats, PrimaryGen gen) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
@@ -184,10 +191,15 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
         const uint32_t i = base + lane;
         const bool valid = i < n;
         float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4;
+        uint32_t seed = 0;
         int2 hit = make_int2(0, -1);
         if (valid) {
-            o4 = qin.o[i];
-            d4 = qin.d[i];
+            if (gen.path_seeds) {
+                gen_primary(gen, i, o4, d4, seed);
+            } else {
+                o4 = qin.o[i];
+                d4 = qin.d[i];
+            }
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
             float t;
             const int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
@@ -198,7 +210,8 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
         uint32_t slot = 0;
         if (valid) {
             slot = (uint32_t)__float_as_int(o4.w);
-            r = shade_one(S, o4, d4, qin.t[i], hit);
+            const float4 t4 = gen.path_seeds ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
+            r = shade_one(S, o4, d4, t4, hit);
         }
         const uint32_t pos = warp_append(r.cont, cnt_out);
         if (r.cont) {
@@ -584,12 +597,25 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
         k = 1;
     }
     const int nb = (int)maxd;
+    // the fused first bounce (variants 2 and 3) makes its camera rays from
+    // per-path seeds, kept in the first queue's throughput array (bounce 0
+    // reads no queue and writes the other one)
+    const bool gen0 = tu.traverse_variant >= 2u;
+    uint32_t* const path_seeds = gen0 ? reinterpret_cast<uint32_t*>(r->q[0].t) : nullptr;
     for (uint32_t s0 = 0; s0 < spp; s0 += k) {
         const uint32_t kk = std::min(k, spp - s0);
         for (uint32_t p0 = 0; p0 < npix; p0 += P) {
             const uint32_t PP = std::min(P, npix - p0);
             k_raygen<<<(PP + 255) / 256, 256, 0, st>>>(*camera, W, H, p0, PP, s0, kk, opts->subframe_index,
-                                                       (int)maxd, r->seeds, r->q[0], r->cnt, r->work, nb);
+                                                       (int)maxd, r->seeds, r->q[0], path_seeds, r->cnt, r->work,
+                                                       nb);
+            PrimaryGen pg{};
+            pg.cam = *camera;
+            pg.W = W;
+            pg.H = H;
+            pg.p0 = p0;
+            pg.P = PP;
+            pg.depth = (int)maxd - 1;
             ++launches;
             for (int b = 0; b < nb; ++b) {
                 const Queue& qi = r->q[b & 1];
@@ -604,12 +630,15 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                 // later bounces with the separate traversal kernel
                 const uint32_t v = tu.traverse_variant <= 2u ? tu.traverse_variant : (b == 0 ? 2u : 0u);
                 if (v == 2) {
+                    pg.path_seeds = (b == 0) ? path_seeds : nullptr;
                     if (count)
                         k_trace_shade<true><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
-                                                                             r->cnt + b + 1, r->slots, r->err, r->stats);
+                                                                             r->cnt + b + 1, r->slots, r->err, r->stats,
+                                                                             pg);
                     else
                         k_trace_shade<false><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
-                                                                              r->cnt + b + 1, r->slots, r->err, r->stats);
+                                                                              r->cnt + b + 1, r->slots, r->err,
+                                                                              r->stats, pg);
                     if (prof) {
                         VENU_CUDA(cudaEventRecord(e1, st));
                         VENU_CUDA(cudaEventRecord(e2, st));

@@ -32,6 +32,29 @@ __device__ __forceinline__ DevCamera load_camera(const venu_camera& c) {
     return k;
 }
 
+// The primary rays of one wave of the single-scene renderer, made inside the
+// fused kernel from each path's raygen seed (k_raygen writes only the seeds):
+// the same queue entry as write_primary, without the round trip through
+// memory.  path_seeds == nullptr: rays come from the queue.
+struct PrimaryGen {
+    venu_camera cam;
+    const uint32_t* path_seeds;  // [k * P], path pos = s * P + pl
+    uint32_t W, H, p0, P;
+    int depth;                   // max_depth - 1
+};
+
+__device__ __forceinline__ void gen_primary(const PrimaryGen& g, uint32_t pos, float4& o4, float4& d4,
+                                            uint32_t& seed) {
+    const uint32_t s = pos / g.P;
+    const uint32_t pix = g.p0 + (pos - s * g.P);
+    seed = g.path_seeds[pos];
+    const DevCamera C = load_camera(g.cam);
+    f3 o, d;
+    camera_ray(C, pix % g.W, pix / g.W, g.W, g.H, seed, o, d);
+    o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)pos));
+    d4 = make_float4(d.x, d.y, d.z, __uint_as_float((uint32_t)g.depth & kDepthMask));
+}
+
 struct ShadeOut {
     bool cont;
     float4 o, d, t;   // next queue entry when cont
