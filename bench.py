@@ -619,14 +619,17 @@ def main():
     # state queue traffic: 112 B per segment for the fused traverse+shade
     # kernel (28 B ray write + read, 12 B hit write + read, 16 B
     # throughput/seed/pixel read + write), 40 B for the separate traversal
-    # kernel (28 B ray read, 12 B hit write).
+    # kernel (28 B ray read, 12 B hit write).  The fused kernel makes the
+    # primary rays itself from a 4-byte seed per path: 32 B for those
+    # segments (4 B seed write + read, 12 B hit, 16 B throughput/seed/pixel
+    # write after the bounce).
     trav_bytes = nodes * 32 + sph * 16
     if fused:
         kernel = "k_trace_shade"
-        kbytes = trav_bytes + segs_c * 112
+        kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 112
     elif variant == 3:  # fused primary bounce, separate traversal after it
         kernel = "k_trace_shade (primary) + k_traverse"
-        kbytes = trav_bytes + paths_c * 112 + (segs_c - paths_c) * 40
+        kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 40
     else:
         kernel = "k_traverse"
         kbytes = trav_bytes + segs_c * 40
@@ -639,14 +642,15 @@ def main():
     kflops = nodes * 20 + sph * 25 + (segs_c * 60 if fused else 0)
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     # DRAM traffic per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum
-    # per segment from a capture of the same kernel on a smaller case of the
-    # same scene (the queue traffic, which grows in proportion to the rays;
-    # the node set stays cache-resident), scaled to this launch's segments.
-    # Captures: profiles/k_trace_shade_rtiow_1920x1080_4spp.md (86.6 B),
-    # profiles/k_trace_shade_random1m_1920x1080_2spp.md (87.2 B) and, for the
-    # separate traversal kernel, profiles/k_traverse_random1m_1920x1080_2spp.md
-    # (37.1 B).  (c1's queues fit in L2: no figure for it.)
-    dram_per_seg = {("c2", 2): 86.6, ("c3", 2): 87.2, ("c3", 0): 37.1}.get((args.config, variant))
+    # per segment, summed over every launch of the kernel in one render of a
+    # smaller case of the same scene (the queue traffic grows in proportion to
+    # the rays), scaled to this launch's segments.  Captures:
+    # profiles/k_trace_shade_rtiow_1920x1080_4spp.md (62.0 B over all 50
+    # bounces), profiles/k_trace_shade_random1m_1920x1080_2spp.md (116.1 B)
+    # and, for the separate traversal kernel, on primary rays only,
+    # profiles/k_traverse_random1m_1920x1080_2spp.md (37.1 B).  (c1's queues
+    # fit in L2: no figure for it.)
+    dram_per_seg = {("c2", 2): 62.0, ("c3", 2): 116.1, ("c3", 0): 37.1}.get((args.config, variant))
     traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"]) if dram_per_seg else None
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -36,6 +36,7 @@ namespace venu {
 struct DevJob {
     SceneView scene;
     venu_camera cam;
+    DevCamera dcam;  // load_camera(cam), written by k_seed_table
     uint32_t W, H, npix, spp, max_depth, subframe;
     const uint32_t* seeds;  // [spp * npix], sample-major
     float4* slots;          // [spp * npix], sample-major
@@ -69,11 +70,12 @@ struct CollectEntry {
 
 // Raygen RNG state at the start of every sample of every pixel.
 __global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t spp, uint32_t subframe,
-                             uint32_t* __restrict__ seeds) {
+                             uint32_t* __restrict__ seeds, DevCamera* __restrict__ dcam) {
     const uint32_t npix = W * H;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
     const DevCamera C = load_camera(cam);
+    if (pix == 0) *dcam = C;
     const uint32_t x = pix % W, y = pix / W;
     uint32_t seed = tea4(pix, subframe);
     for (uint32_t s = 0; s < spp; ++s) {
@@ -189,9 +191,8 @@ __device__ __forceinline__ void gen_primary(const DevJob* __restrict__ jobs, con
     const uint32_t s = l / npix;
     const uint32_t pix = l - s * npix;
     seed = J.seeds[l];
-    const DevCamera C = load_camera(J.cam);
     f3 o, d;
-    camera_ray(C, pix % W, pix / W, W, J.H, seed, o, d);
+    camera_ray(J.dcam, pix % W, pix / W, W, J.H, seed, o, d);
     o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)l));
     d4 = make_float4(d.x, d.y, d.z, __uint_as_float((j << 8) | ((uint32_t)((int)J.max_depth - 1) & kDepthMask)));
 }
@@ -599,7 +600,7 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     VENU_CUDA(cudaMemsetAsync(b->d_done + slot, 0, sizeof(unsigned long long), st));
     VENU_CUDA(cudaMemsetAsync(b->d_seen + slot, 0, sizeof(uint32_t), st));
     k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(job->camera, o.width, o.height, o.samples_per_pixel,
-                                                                 o.subframe_index, J.seeds);
+                                                                 o.subframe_index, J.seeds, &b->d_jobs[slot].dcam);
     VENU_CUDA(cudaGetLastError());
     b->order.push_back(slot);
     b->resident += J.bytes;

@@ -178,6 +178,11 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
     sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
+    __shared__ DevCamera cam;  // the primary rays' camera basis, once per block
+    if (gen.path_seeds) {      // a kernel parameter: the same in every thread
+        if (threadIdx.x == 0) cam = load_camera(gen.cam);
+        __syncthreads();
+    }
     const uint32_t n = *cnt_in;
     const uint32_t lane = threadIdx.x & 31;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
@@ -195,7 +200,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
         int2 hit = make_int2(0, -1);
         if (valid) {
             if (gen.path_seeds) {
-                gen_primary(gen, i, o4, d4, seed);
+                gen_primary(gen, cam, i, o4, d4, seed);
             } else {
                 o4 = qin.o[i];
                 d4 = qin.d[i];

@@ -43,12 +43,12 @@ struct PrimaryGen {
     int depth;                   // max_depth - 1
 };
 
-__device__ __forceinline__ void gen_primary(const PrimaryGen& g, uint32_t pos, float4& o4, float4& d4,
-                                            uint32_t& seed) {
+// C: load_camera(g.cam), made once per block
+__device__ __forceinline__ void gen_primary(const PrimaryGen& g, const DevCamera& C, uint32_t pos, float4& o4,
+                                            float4& d4, uint32_t& seed) {
     const uint32_t s = pos / g.P;
     const uint32_t pix = g.p0 + (pos - s * g.P);
     seed = g.path_seeds[pos];
-    const DevCamera C = load_camera(g.cam);
     f3 o, d;
     camera_ray(C, pix % g.W, pix / g.W, g.W, g.H, seed, o, d);
     o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)pos));
