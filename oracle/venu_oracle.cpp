@@ -570,41 +570,61 @@ void build_bvh(const vo_sphere* s, uint32_t n, Bvh& B) {
 // GB300-mode ray/box and ray/sphere tests (the CUDA traversal kernel's
 // arithmetic).  Explicit fmaf where the kernel uses one.
 // ---------------------------------------------------------------------------
+// Slab offsets.  The offset -(o inv) of each axis is rounded; a margin of
+// |o inv| 2^-21 per axis covers it.  Shared margin (almost every ray): the
+// offsets unchanged and the largest margin of the three added to the exit
+// parameter.  When that margin exceeds 1 (a near-zero direction component,
+// whose margin would switch off the culling on the other axes) each axis
+// carries its own margin, moved outwards: nlo for the lo plane, nhi for the
+// hi plane (the entry plane is lo when inv >= 0).
+constexpr float kSharedMarginMax = 1.0f;
 struct RayPre {
-    f3 o, d, inv, noi;  // noi = -(o * inv)
-    float a, inv_a, slack;
+    f3 o, d, inv, nlo, nhi;
+    float a, inv_a, slack;  // slack: the shared margin (0 with per-axis margins)
+    bool axis;
 };
 inline RayPre prep(f3 o, f3 d) {
     RayPre R;
     R.o = o;
     R.d = d;
-    float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z}, inv[3], noi[3];
-    float m = 0.0f;
+    float dd[3] = {d.x, d.y, d.z}, oo[3] = {o.x, o.y, o.z}, inv[3], p[3], m[3], nlo[3], nhi[3];
     for (int a = 0; a < 3; ++a) {
         float di = dd[a];
         if (std::fabs(di) < 1e-20f) di = std::copysign(1e-20f, di);
         inv[a] = 1.0f / di;
-        float oi = oo[a] * inv[a];
-        noi[a] = -oi;
-        m = std::fmax(m, std::fabs(oi));
+        p[a] = oo[a] * inv[a];
+        m[a] = std::fabs(p[a]) * 4.76837158203125e-07f;  // 2^-21
     }
+    const float mm = std::fmax(std::fmax(m[0], m[1]), m[2]);
+    R.axis = mm > kSharedMarginMax;
+    for (int a = 0; a < 3; ++a) {
+        if (!R.axis) {
+            nlo[a] = nhi[a] = -p[a];
+        } else {
+            const float lo = -p[a] - m[a], hi = -p[a] + m[a];
+            nlo[a] = inv[a] >= 0.0f ? lo : hi;
+            nhi[a] = inv[a] >= 0.0f ? hi : lo;
+        }
+    }
+    R.slack = R.axis ? 0.0f : mm;
     R.inv = mk(inv[0], inv[1], inv[2]);
-    R.noi = mk(noi[0], noi[1], noi[2]);
-    R.slack = m * 4.76837158203125e-07f;  // 2^-21
+    R.nlo = mk(nlo[0], nlo[1], nlo[2]);
+    R.nhi = mk(nhi[0], nhi[1], nhi[2]);
     R.a = std::fma(d.x, d.x, std::fma(d.y, d.y, d.z * d.z));
     R.inv_a = 1.0f / R.a;
     return R;
 }
 inline bool box_test(const RayPre& R, const vo_node& nd, float tmin, float tfar_cap, float& tnear) {
-    float t0x = std::fma(nd.lo[0], R.inv.x, R.noi.x), t1x = std::fma(nd.hi[0], R.inv.x, R.noi.x);
-    float t0y = std::fma(nd.lo[1], R.inv.y, R.noi.y), t1y = std::fma(nd.hi[1], R.inv.y, R.noi.y);
-    float t0z = std::fma(nd.lo[2], R.inv.z, R.noi.z), t1z = std::fma(nd.hi[2], R.inv.z, R.noi.z);
+    float t0x = std::fma(nd.lo[0], R.inv.x, R.nlo.x), t1x = std::fma(nd.hi[0], R.inv.x, R.nhi.x);
+    float t0y = std::fma(nd.lo[1], R.inv.y, R.nlo.y), t1y = std::fma(nd.hi[1], R.inv.y, R.nhi.y);
+    float t0z = std::fma(nd.lo[2], R.inv.z, R.nlo.z), t1z = std::fma(nd.hi[2], R.inv.z, R.nhi.z);
     float tn = std::fmax(std::fmax(std::fmin(t0x, t1x), std::fmin(t0y, t1y)),
                          std::fmax(std::fmin(t0z, t1z), tmin));
     float tf = std::fmin(std::fmin(std::fmax(t0x, t1x), std::fmax(t0y, t1y)),
                          std::fmin(std::fmax(t0z, t1z), tfar_cap));
     tnear = tn;
-    return tn <= std::fma(tf, 1.00000095367431640625f, R.slack);  // tf * (1 + 2^-20) + slack
+    if (R.axis) return tn <= tf * 1.00000095367431640625f;  // tf * (1 + 2^-20)
+    return tn <= std::fma(tf, 1.00000095367431640625f, R.slack);  // tf * (1 + 2^-20) + shared margin
 }
 // GB300 ray/sphere: perpendicular-distance discriminant (Ray Tracing Gems
 // ch. 7), q-form roots, and an exactly refined c and h when the origin is

@@ -131,6 +131,45 @@ def test_bvh_traversal_matches_brute_force(oracle):
     assert ((idb == -1) == (id64 == -1)).mean() > 0.999
 
 
+def _axis_rays(n, seed):
+    """Rays inside a random-sphere field whose directions have one or two
+    components exactly zero or tiny (down to 1e-30): the near-axis-parallel
+    rays the slab test must cull as well as any other."""
+    rng = np.random.default_rng(seed)
+    o = np.stack([rng.uniform(-90, 90, n), rng.uniform(0.5, 19.5, n), rng.uniform(-90, 90, n)], 1)
+    d = rng.normal(size=(n, 3))
+    tiny = np.array([0.0, -0.0, 1e-30, -1e-12, 1e-9, 3e-7, -2e-6])
+    for i in range(n):
+        for a in rng.choice(3, size=1 + i % 2, replace=False):
+            d[i, a] = tiny[(i // 2) % len(tiny)]
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+def test_near_axis_parallel_rays(oracle):
+    """A direction component at or near zero gives 1/d up to 1e20; its slab
+    rounding margin must not switch off the culling on the other two axes
+    (with one margin shared by all axes such a ray visited every node its
+    slab met: tens of thousands in a 50k-sphere field)."""
+    sp = oracle.scene_random(50_000, 6)
+    rays = _axis_rays(4000, 3)
+    idb, tb, front, nv, ns = oracle.trace_bvh(sp, rays)
+    ok = oracle.trace_bvh(sp, _random_rays_like(rays, 4))[3]
+    assert nv.max() < 8 * max(ok.max(), 1), (nv.max(), ok.max())
+    assert nv.mean() < 3 * ok.mean()
+    id64, t64, disc, t2 = oracle.trace_fp64(sp, rays)
+    well = (id64 >= 0) & (disc > 1e-4) & (t2 > t64 * (1 + 1e-4))
+    assert well.sum() > 1000
+    assert (idb == id64)[well].all()
+    rel = np.abs(tb[well].astype(np.float64) - t64[well]) / t64[well]
+    assert rel.max() < 1e-5, rel.max()
+    assert ((idb == -1) == (id64 == -1)).mean() > 0.999
+
+
+def _random_rays_like(rays, seed):
+    d = np.random.default_rng(seed).normal(size=(len(rays), 3)).astype(np.float32)
+    return np.concatenate([rays[:, :3], d], 1).astype(np.float32)
+
+
 def test_gb300_vs_ref_same_paths(oracle):
     """The GB300 arithmetic and the reference arithmetic trace the same paths:
     at the same seeds > 99% of samples agree within 1e-3, and the

@@ -129,7 +129,16 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                 if (my < n) {
                     ray = my;
                     const float4 o4 = q.o[my], d4 = q.d[my];
-                    if (T.begin(S, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), 0.001f, 1e16f, K)) {
+                    const RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+                    if (R.axis) {
+                        // a near-axis-parallel ray (rare): traced to the end now with
+                        // the per-axis loop, on this lane's free stack; the lane
+                        // stays idle
+                        float t;
+                        const int32_t kk = trace_closest_as<COUNT, true>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x,
+                                                                         blockDim.x, overflow, K);
+                        hits[my] = make_int2(__float_as_int(t), kk);
+                    } else if (T.begin(S, R, 0.001f, 1e16f, K)) {
                         active = true;
                     } else {
                         float t;

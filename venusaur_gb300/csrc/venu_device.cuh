@@ -175,10 +175,27 @@ struct SceneView {
     int32_t hoist[kMaxHoisted];        // their slots (ascending)
 };
 
+// Slab test: a box's entry / exit parameter on axis k is
+// fma(lo_k or hi_k, inv_k, offset).  The offset -(o_k inv_k) is rounded, which
+// a margin of |o_k inv_k| 2^-21 covers (several times that rounding).
+//   Shared margin (almost every ray): one offset n0_k = -(o_k inv_k) per axis
+//   and the largest margin of the three axes added once to the exit
+//   parameter (n1.x), which keeps four floats live during traversal.
+//   Per-axis margins (axis = true): a near-zero direction component (1/d up
+//   to 1e20) makes its own margin huge, and shared by all axes it would
+//   switch off the culling on the other two (such a ray then visits every
+//   node its slab meets).  When the shared margin exceeds 1 (in units of t)
+//   the offsets carry each axis's own margin instead, moved outwards: n0_k
+//   for the lo plane, n1_k for the hi plane (the entry plane is lo when
+//   inv_k >= 0).  Such rays are rare (a direction component below ~1e-5 of
+//   the others) and traverse with their own instantiation of the loop.
 struct RayPre {
-    f3 o, d, inv, noi;  // noi = -(o * inv)
-    float a, inv_a, slack;
+    f3 o, d, inv, n0, n1;
+    float a, inv_a;
+    bool axis;
 };
+
+constexpr float kSharedMarginMax = 1.0f;
 
 __device__ __forceinline__ RayPre prep(f3 o, f3 d) {
     RayPre R;
@@ -188,10 +205,22 @@ __device__ __forceinline__ RayPre prep(f3 o, f3 d) {
     float dy = fabsf(d.y) < 1e-20f ? copysignf(1e-20f, d.y) : d.y;
     float dz = fabsf(d.z) < 1e-20f ? copysignf(1e-20f, d.z) : d.z;
     R.inv = mk(1.0f / dx, 1.0f / dy, 1.0f / dz);
-    float ox = o.x * R.inv.x, oy = o.y * R.inv.y, oz = o.z * R.inv.z;
-    R.noi = mk(-ox, -oy, -oz);
-    float m = fmaxf(fmaxf(fmaxf(0.0f, fabsf(ox)), fabsf(oy)), fabsf(oz));
-    R.slack = m * 4.76837158203125e-07f;  // 2^-21
+    const float px = o.x * R.inv.x, py = o.y * R.inv.y, pz = o.z * R.inv.z;
+    const float mx = fabsf(px) * 4.76837158203125e-07f;  // 2^-21
+    const float my = fabsf(py) * 4.76837158203125e-07f;
+    const float mz = fabsf(pz) * 4.76837158203125e-07f;
+    const float m = fmaxf(fmaxf(mx, my), mz);
+    R.axis = m > kSharedMarginMax;
+    if (!R.axis) {
+        R.n0 = mk(-px, -py, -pz);
+        R.n1 = mk(m, 0.0f, 0.0f);
+    } else {
+        const float lx = -px - mx, hx = -px + mx;
+        const float ly = -py - my, hy = -py + my;
+        const float lz = -pz - mz, hz = -pz + mz;
+        R.n0 = mk(R.inv.x >= 0.0f ? lx : hx, R.inv.y >= 0.0f ? ly : hy, R.inv.z >= 0.0f ? lz : hz);
+        R.n1 = mk(R.inv.x >= 0.0f ? hx : lx, R.inv.y >= 0.0f ? hy : ly, R.inv.z >= 0.0f ? hz : lz);
+    }
     R.a = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
     R.inv_a = 1.0f / R.a;
     return R;
@@ -221,15 +250,19 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 
 // Robust slab test: conservative by a relative 2^-20 plus an absolute slack
 // proportional to |o / d|, so rounding never drops a box the ray touches.
+template <bool AXIS>
 __device__ __forceinline__ bool box_test(const RayPre& R, float4 lo, float4 hi, float tmin,
                                          float tcap, float& tnear) {
-    float t0x = fmaf(lo.x, R.inv.x, R.noi.x), t1x = fmaf(hi.x, R.inv.x, R.noi.x);
-    float t0y = fmaf(lo.y, R.inv.y, R.noi.y), t1y = fmaf(hi.y, R.inv.y, R.noi.y);
-    float t0z = fmaf(lo.z, R.inv.z, R.noi.z), t1z = fmaf(hi.z, R.inv.z, R.noi.z);
+    const f3 nh = AXIS ? R.n1 : R.n0;
+    float t0x = fmaf(lo.x, R.inv.x, R.n0.x), t1x = fmaf(hi.x, R.inv.x, nh.x);
+    float t0y = fmaf(lo.y, R.inv.y, R.n0.y), t1y = fmaf(hi.y, R.inv.y, nh.y);
+    float t0z = fmaf(lo.z, R.inv.z, R.n0.z), t1z = fmaf(hi.z, R.inv.z, nh.z);
     float tn = fmax3(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), tmin));
     float tf = fmin3(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fminf(fmaxf(t0z, t1z), tcap));
     tnear = tn;
-    return tn <= fmaf(tf, 1.00000095367431640625f, R.slack);
+    // tf (1 + 2^-20) covers the roundings of the two fmas; the shared margin
+    // is added here
+    return AXIS ? tn <= tf * 1.00000095367431640625f : tn <= fmaf(tf, 1.00000095367431640625f, R.n1.x);
 }
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -358,7 +391,7 @@ struct TraceCounters {
 // inline) and descends or pops; both return whether more work remains.  The
 // same state machine serves the one-ray-per-thread kernels (trace_closest)
 // and the persistent kernels that refill idle lanes.
-template <bool COUNT>
+template <bool COUNT, bool AXIS = false>
 struct Tracer {
     RayPre R;
     float tmin, tmax, best_t;
@@ -375,9 +408,10 @@ struct Tracer {
         }
     }
 
-    __device__ __forceinline__ bool begin(const SceneView& S, f3 o, f3 d, float tmin_, float tmax_,
+    // R_ from prep(); its axis flag must equal AXIS.
+    __device__ __forceinline__ bool begin(const SceneView& S, const RayPre& R_, float tmin_, float tmax_,
                                           TraceCounters& K) {
-        R = prep(o, d);
+        R = R_;
         tmin = tmin_;
         tmax = tmax_;
         best_t = tmax_;
@@ -396,7 +430,7 @@ struct Tracer {
         float tn;
         float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
         if (COUNT) ++K.nodes;
-        if (!box_test(R, rlo, rhi, tmin, best_t, tn)) return false;
+        if (!box_test<AXIS>(R, rlo, rhi, tmin, best_t, tn)) return false;
         cur = 0;
         // A tree has n-1 internal nodes and each step expands a different one;
         // the guard turns a cyclic (corrupt) tree into an error flag instead
@@ -424,13 +458,13 @@ struct Tracer {
             if (!(w0 & kHoisted)) leaf(w0 & kSlotMask, make_float4(a0.x, a0.y, a0.z, b0.x), K);
         } else {
             if (COUNT) ++K.nodes;
-            h0 = box_test(R, a0, b0, tmin, best_t, tn0);
+            h0 = box_test<AXIS>(R, a0, b0, tmin, best_t, tn0);
         }
         if (w1 & kLeaf) {
             if (!(w1 & kHoisted)) leaf(w1 & kSlotMask, make_float4(a1.x, a1.y, a1.z, b1.x), K);
         } else {
             if (COUNT) ++K.nodes;
-            h1 = box_test(R, a1, b1, tmin, best_t, tn1);
+            h1 = box_test<AXIS>(R, a1, b1, tmin, best_t, tn1);
         }
         if (h0 && h1) {
             int32_t far;
@@ -494,18 +528,29 @@ struct Tracer {
     }
 };
 
+template <bool COUNT, bool AXIS>
+__device__ __forceinline__ int32_t trace_closest_as(const SceneView& S, const RayPre& R, float tmin,
+                                                    float tmax, float& t_out, StackSmem sm,
+                                                    uint32_t tid, uint32_t bdim, bool& overflow,
+                                                    TraceCounters& K) {
+    Tracer<COUNT, AXIS> T;
+    int spill[kSpill];
+    float spill_tn[kSpill];
+    if (T.begin(S, R, tmin, tmax, K))
+        while (T.step(S, sm, tid, bdim, spill, spill_tn, overflow, K)) {
+        }
+    return T.result(t_out);
+}
+
+// Closest hit of one ray (R from prep): the shared-margin loop, or the
+// per-axis one for the rare near-axis-parallel ray.
 template <bool COUNT>
 __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPre& R, float tmin,
                                                  float tmax, float& t_out, StackSmem sm,
                                                  uint32_t tid, uint32_t bdim, bool& overflow,
                                                  TraceCounters& K) {
-    Tracer<COUNT> T;
-    int spill[kSpill];
-    float spill_tn[kSpill];
-    if (T.begin(S, R.o, R.d, tmin, tmax, K))
-        while (T.step(S, sm, tid, bdim, spill, spill_tn, overflow, K)) {
-        }
-    return T.result(t_out);
+    if (R.axis) return trace_closest_as<COUNT, true>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
+    return trace_closest_as<COUNT, false>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
 }
 
 // ---------------------------------------------------------------------------
