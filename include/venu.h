@@ -269,8 +269,9 @@ VENU_API venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tunin
  * optixLaunch); each job is one Renderer::Draw of its own scene, camera and
  * image.  All admitted jobs share one pool of paths in flight: every ray
  * carries its job, finished paths are replaced by new camera rays of the
- * jobs in submission order, and the whole path loop -- traverse+shade,
- * regenerate, repeat -- is one CUDA graph launch driven by a device-side
+ * jobs in plan order (their camera rays made inside the trace kernel), and
+ * the whole path loop -- trace+shade, plan, repeat -- is one CUDA graph
+ * launch driven by a device-side
  * while condition.  Results are bit-identical to venu_render of each job
  * alone (same seeds, same per-pixel sample order). */
 typedef struct venu_batch venu_batch;

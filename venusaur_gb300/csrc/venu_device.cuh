@@ -248,8 +248,9 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
 #endif
 }
 
-// Robust slab test: conservative by a relative 2^-20 plus an absolute slack
-// proportional to |o / d|, so rounding never drops a box the ray touches.
+// Robust slab test: conservative by a relative 2^-20 plus the rounding
+// margins of the slab offsets (shared or per axis, see RayPre), so rounding
+// never drops a box the ray touches.
 template <bool AXIS>
 __device__ __forceinline__ bool box_test(const RayPre& R, float4 lo, float4 hi, float tmin,
                                          float tcap, float& tnear) {
