@@ -116,13 +116,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
-    """Times the CPU port on a bounded row sample sized to ~target_s seconds."""
+def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None, size=None):
+    """Times the CPU port on a bounded row sample sized to ~target_s seconds
+    (or of the given size: (rows, spp) from an earlier call)."""
     from oracle import pyoracle
 
     mode = pyoracle.MODE_GB300 if mode is None else mode
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     r0 = H // 2
+    if size is not None:
+        rows, spp_s = size
+        t0 = time.perf_counter()
+        res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
+                       rows=(r0, r0 + rows))
+        dt = time.perf_counter() - t0
+        sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
+        return res["segments"] / dt, dt, sample, res["segments"], (rows, spp_s)
     # probe: rate and segments per path, then size rows (and samples) to the target
     rows, spp_s = 4, min(spp, 2)
     t0 = time.perf_counter()
@@ -146,7 +155,7 @@ def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None):
             break
     rate = res["segments"] / dt
     sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
-    return rate, dt, sample, res["segments"]
+    return rate, dt, sample, res["segments"], (rows, spp_s)
 
 
 def rmse_vs_reference(venu, torch, O, ds, spheres, cam, W, H, depth, spp=16):
@@ -465,9 +474,11 @@ def run_reference(args, cfg, world, rank):
     spheres = make_scene(venu, cfg["scene"])
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, cfg["W"] / cfg["H"], 0.1, 10.0)
     nt = os.cpu_count() or 1
-    times, segs = [], 0
+    times, segs, size = [], 0, None
     for i in range(args.warmup + args.steps):
-        rate, dt, sample, s = cpu_sample(O, spheres, cam, cfg, nt, target_s=max(2.0, 20.0 / max(1, args.steps)))
+        # the first call sizes the sample (each step ~20 s / steps); the rest reuse it
+        rate, dt, sample, s, size = cpu_sample(O, spheres, cam, cfg, nt,
+                                               target_s=max(2.0, 20.0 / max(1, args.steps)), size=size)
         if i >= args.warmup:
             times.append(dt)
             segs += s
@@ -535,7 +546,7 @@ def main():
         pyoracle.build()
         O = pyoracle.Oracle()
         nt = os.cpu_count() or 1
-        rate, dt, sample, _ = cpu_sample(O, spheres, cam, cfg, nt)
+        rate, dt, sample, _, _ = cpu_sample(O, spheres, cam, cfg, nt)
         cpu_baseline = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample, "seconds": dt}
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
