@@ -649,8 +649,9 @@ def main():
     achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
     peak, peak_kind = load_peaks()
     # FP32 view (per-segment estimate): 20 flop per box, 25 per sphere, 60
-    # per shade; peak = 152 SMs x 128 lanes x 2 x max SM clock
-    kflops = nodes * 20 + sph * 25 + (segs_c * 60 if fused else 0)
+    # per shade, 30 per camera ray (made in the fused kernel); peak = 152 SMs
+    # x 128 lanes x 2 x max SM clock
+    kflops = nodes * 20 + sph * 25 + (segs_c * 60 + paths_c * 30 if fused else 0)
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
     # DRAM traffic per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum
     # per segment, summed over every launch of the kernel in one render of a
