@@ -51,12 +51,15 @@ def time_render(wf: Wavefront, scene: DeviceScene, cam, W, H, spp, depth, accum,
 
 
 def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8 << 20,), tune_spp=None,
-             reps=2, log=None):
-    """Returns (best_tuning: dict, best_max_paths: int, results: list)."""
+             reps=2, log=None, finalists=3, final_reps=6):
+    """Returns (best_tuning: dict, best_max_paths: int, results: list).
+
+    Every candidate is timed once (reps renders); the `finalists` fastest are
+    timed again with final_reps renders each and the fastest of those wins,
+    so that run-to-run noise between close candidates decides less."""
     tune_spp = tune_spp or max(1, min(spp, 8))
     accum = new_accum(W, H)
     results = []
-    best = None
     for mp in max_paths:
         wf = Wavefront(mp)
         for cand in candidates(space):
@@ -65,9 +68,18 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
             results.append(dict(cand, max_paths=mp, segments_per_s=rate, ms=ms))
             if log:
                 log(results[-1])
-            if best is None or rate > best[0]:
-                best = (rate, dict(cand), mp)
         wf.close()
+    ranked = sorted(results, key=lambda r: -r["segments_per_s"])[:max(1, finalists)]
+    best = None
+    for r in ranked:
+        cand = {k: r[k] for k in r if k not in ("max_paths", "segments_per_s", "ms")}
+        wf = Wavefront(r["max_paths"])
+        wf.set_tuning(**cand)
+        rate, ms = time_render(wf, scene, cam, W, H, tune_spp, depth, accum, final_reps)
+        wf.close()
+        r["final_segments_per_s"] = rate
+        if best is None or rate > best[0]:
+            best = (rate, cand, r["max_paths"])
     return best[1], best[2], results
 
 
