@@ -374,7 +374,7 @@ __device__ __forceinline__ bool sphere_test(const RayPre& R, float4 S, float tmi
 // banks) and whose older entries spill to local memory.  Ties on t go to the
 // smaller slot, so the result does not depend on traversal order.
 // ---------------------------------------------------------------------------
-constexpr int kShared = 16;  // shared-memory entries per thread (power of two)
+constexpr int kShared = 8;   // shared-memory entries per thread (power of two)
 constexpr int kSpill = 64;   // local-memory entries beyond those
 
 struct StackSmem {
