@@ -175,6 +175,34 @@ def test_batch_policy(venu, oracle, cuda, policy):
         assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))
 
 
+@pytest.mark.parametrize("policy", ["fifo", "shortest_first", "sequential"])
+def test_batch_many_jobs_policy(venu, oracle, cuda, policy):
+    """70 jobs (more than one warp of the plan kernel, which hands out the
+    free slots 32 jobs at a time) in a pool that holds a few of them: every
+    result exact; under the sequential policy the jobs finish strictly in
+    submission order."""
+    torch = cuda
+    b = venu.Batch(pool_paths=512, max_jobs=80)
+    b.set_policy(policy)
+    scenes = [oracle.scene_rtiow(k) for k in range(4)]
+    jobs = []
+    for k in range(70):
+        W, H, spp = 8 + (k % 3) * 4, 6, 1 + (k * 7) % 3
+        jobs.append(_one(venu, torch, oracle, b, scenes[k % 4], (13, 2, 3), W, H, spp, 4, sub=1 + k % 5))
+    order = []
+    for _ in range(400):
+        b.run(stop_on_finish=True)
+        order += b.collect()
+        if len(order) == len(jobs):
+            break
+    torch.cuda.synchronize()
+    assert sorted(order) == sorted(j["id"] for j in jobs)
+    if policy == "sequential":
+        assert order == [j["id"] for j in jobs]
+    for j in jobs:
+        assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))
+
+
 def test_batch_interrupt(venu, oracle, cuda):
     """While the interrupt flag is set a run ends after one iteration;
     cleared, the run goes to the end.  Results are exact."""

@@ -25,14 +25,20 @@ def _torch():
     return torch
 
 
+_cuda_available = None
+
+
 def _stream_handle(stream=None):
     """cudaStream_t of `stream` (default: torch's current stream).  Without a
     CUDA device this is NULL and the library itself reports the missing
     device (VENU_ERR_NO_DEVICE)."""
+    global _cuda_available
     if stream is not None:
         return C.c_void_p(stream.cuda_stream)
     torch = _torch()
-    if not torch.cuda.is_available():
+    if _cuda_available is None:
+        _cuda_available = torch.cuda.is_available()
+    if not _cuda_available:
         return None
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -508,12 +514,9 @@ class Renderer:
 # Batched / served rendering: many jobs in one shared path pool
 # ---------------------------------------------------------------------------
 def _camera_c(camera: np.ndarray) -> "_lib.CameraC":
-    c = np.ascontiguousarray(camera, CAMERA_DTYPE)[0]
-    cc = _lib.CameraC()
-    for f in ("origin", "u", "v", "w"):
-        getattr(cc, f)[:] = [float(x) for x in c[f]]
-    cc.lens_radius = float(c["lens_radius"])
-    return cc
+    # CAMERA_DTYPE and venu_camera have the same 52-byte layout
+    c = np.ascontiguousarray(camera, CAMERA_DTYPE).reshape(-1)[:1]
+    return _lib.CameraC.from_buffer_copy(c.tobytes())
 
 
 def _policy(policy) -> int:

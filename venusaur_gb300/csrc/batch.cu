@@ -68,108 +68,160 @@ struct CollectEntry {
     uint32_t npix, spp, reset, pix_off;
 };
 
-// Raygen RNG state at the start of every sample of every pixel.
-__global__ void k_seed_table(venu_camera cam, uint32_t W, uint32_t H, uint32_t spp, uint32_t subframe,
-                             uint32_t* __restrict__ seeds, DevCamera* __restrict__ dcam) {
-    const uint32_t npix = W * H;
+// Admits job dj into table slot `slot`: its raygen RNG state at the start of
+// every sample of every pixel (the seed table), and -- from its first thread
+// -- its table entry with the camera basis and zeroed counters, so a submit
+// is one allocation and this one launch.
+__global__ void k_seed_table(DevJob dj, uint32_t slot, DevJob* __restrict__ jobs,
+                             unsigned long long* __restrict__ job_next, unsigned long long* __restrict__ job_done,
+                             uint32_t* __restrict__ job_seen) {
+    const uint32_t W = dj.W, npix = dj.npix;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     if (pix >= npix) return;
-    const DevCamera C = load_camera(cam);
-    if (pix == 0) *dcam = C;
+    const DevCamera C = load_camera(dj.cam);
+    if (pix == 0) {
+        dj.dcam = C;
+        jobs[slot] = dj;
+        job_next[slot] = 0ull;
+        job_done[slot] = 0ull;
+        job_seen[slot] = 0u;
+    }
+    uint32_t* __restrict__ seeds = const_cast<uint32_t*>(dj.seeds);
     const uint32_t x = pix % W, y = pix / W;
-    uint32_t seed = tea4(pix, subframe);
-    for (uint32_t s = 0; s < spp; ++s) {
+    uint32_t seed = tea4(pix, dj.subframe);
+    for (uint32_t s = 0; s < dj.spp; ++s) {
         seeds[(size_t)s * npix + pix] = seed;
         f3 o, d;
-        camera_ray(C, x, y, W, H, seed, o, d);  // advances the seed past the sample's draws
+        camera_ray(C, x, y, W, dj.H, seed, o, d);  // advances the seed past the sample's draws
     }
 }
 
 // Hands the free pool slots to the jobs (plan order) and flips the parity;
 // returns whether any work is left.  sequential: a job gets slots only once
 // every job before it in the order has finished all its paths (one job at a
-// time, as rendering them in turn).
+// time, as rendering them in turn).  One warp: jobs go 32 at a time, one per
+// lane.  The greedy hand-out -- each job in order takes min(its remaining
+// paths, the slots still free) -- has a closed form: the slots taken by jobs
+// 0..k together are min(free, the sum of their remaining paths), so a warp
+// prefix sum gives every job's share and offset at once.
 __device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
                                    const unsigned long long* __restrict__ job_done,
                                    const uint32_t* __restrict__ order, const RunCtl* __restrict__ run,
                                    LoopCtl* ctl, uint32_t* __restrict__ plan_job,
                                    unsigned long long* __restrict__ plan_start, uint32_t* __restrict__ plan_off,
                                    uint32_t Q, int in, int out, uint32_t chunk) {
+    const uint32_t lane = threadIdx.x;  // a single 32-thread block
     const uint32_t survivors = ctl->cnt[out];
-    const uint32_t free = survivors < Q ? Q - survivors : 0u;
+    const unsigned long long free = survivors < Q ? Q - survivors : 0u;
     const uint32_t na = run->nactive;
     const bool sequential = run->sequential != 0u;
-    uint32_t off = 0, more = 0;
-    bool blocked = false;
-    for (uint32_t i = 0; i < na; ++i) {
-        const uint32_t j = order[i];
-        const unsigned long long total = jobs[j].total, nx = job_next[j];
-        const unsigned long long rem = total - nx;
-        const uint32_t take = blocked ? 0u : (uint32_t)min(rem, (unsigned long long)(free - off));
-        if (sequential && job_done[j] < total) blocked = true;
-        plan_job[i] = j;
-        plan_start[i] = nx;
-        plan_off[i] = off;
-        off += take;
-        job_next[j] = nx + take;
-        if (nx + take < total) more = 1;
+    unsigned long long carry = 0;  // remaining paths of the unblocked jobs before this chunk
+    bool blocked_before = false, more = false;
+    for (uint32_t base = 0; base < na; base += 32u) {
+        const uint32_t i = base + lane;
+        const bool valid = i < na;
+        uint32_t j = 0;
+        unsigned long long total = 0, nx = 0;
+        if (valid) {
+            j = order[i];
+            total = jobs[j].total;
+            nx = job_next[j];
+        }
+        const bool unfinished = valid && sequential && job_done[j] < total;
+        const uint32_t um = __ballot_sync(0xffffffffu, unfinished);
+        // blocked: an earlier job of the order has not finished (the job that
+        // has not finished itself still takes slots)
+        const bool blocked = blocked_before || (um & ((1u << lane) - 1u)) != 0u;
+        const unsigned long long rem = (valid && !blocked) ? total - nx : 0ull;
+        unsigned long long incl = rem;  // inclusive prefix sum over the lanes
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long v = __shfl_up_sync(0xffffffffu, incl, d);
+            if ((int)lane >= d) incl += v;
+        }
+        const unsigned long long before = min(free, carry + incl - rem);
+        const unsigned long long upto = min(free, carry + incl);
+        const unsigned long long take = upto - before;
+        if (valid) {
+            plan_job[i] = j;
+            plan_start[i] = nx;
+            plan_off[i] = (uint32_t)before;
+            job_next[j] = nx + take;
+        }
+        more = more || __any_sync(0xffffffffu, valid && nx + take < total);
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+        blocked_before = blocked_before || um != 0u;
     }
-    plan_off[na] = off;
-    ctl->plan_n = na;
-    ctl->gen_n = off;
-    ctl->gen_base = survivors;
-    ctl->cnt[out] = survivors + off;
-    ctl->more_gen = more;
-    ctl->cnt[in] = 0;    // the next trace writes into the other queue
-    ctl->work[out] = 0;  // and fetches from this one, chunk by chunk
-    ctl->chunk_end = min(chunk, survivors + off);
-    ctl->parity = (uint32_t)out;
+    const uint32_t off = (uint32_t)min(free, carry);
+    __syncwarp();  // every lane has read the loop state before lane 0 rewrites it
+    if (lane == 0) {
+        plan_off[na] = off;
+        ctl->plan_n = na;
+        ctl->gen_n = off;
+        ctl->gen_base = survivors;
+        ctl->cnt[out] = survivors + off;
+        ctl->more_gen = more ? 1u : 0u;
+        ctl->cnt[in] = 0;    // the next trace writes into the other queue
+        ctl->work[out] = 0;  // and fetches from this one, chunk by chunk
+        ctl->chunk_end = min(chunk, survivors + off);
+        ctl->parity = (uint32_t)out;
+    }
     return (survivors + off > 0u || more) ? 1u : 0u;
 }
 
-// Decides the next step and whether there is one.  The loop condition: more rays or paths to generate, and none of the step cap, "a job
-// just finished" (stop-on-finish) or the host's interrupt word (mapped host
-// memory, read volatile).  A step traces a chunk of the input queue
+// Decides the next step and whether there is one (one warp).  The loop
+// condition: more rays or paths to generate, and none of the step cap, "a
+// job just finished" (stop-on-finish) or the host's interrupt word (mapped
+// host memory, read volatile).  A step traces a chunk of the input queue
 // (RunCtl::chunk rays, all of them when 0); while input rays are left the
 // next step takes the next chunk, else this plans the next iteration and
 // flips the queue parity: the queue filled now is the one traced next.
-__global__ void k_plan(const DevJob* __restrict__ jobs, unsigned long long* __restrict__ job_next,
-                       const unsigned long long* __restrict__ job_done, uint32_t* __restrict__ job_seen,
-                       const uint32_t* __restrict__ order, const RunCtl* __restrict__ run, LoopCtl* ctl,
-                       uint32_t* __restrict__ plan_job, unsigned long long* __restrict__ plan_start,
-                       uint32_t* __restrict__ plan_off, uint32_t Q, const volatile uint32_t* interrupt,
-                       cudaGraphConditionalHandle handle, int use_handle) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(32) k_plan(const DevJob* __restrict__ jobs,
+                                             unsigned long long* __restrict__ job_next,
+                                             const unsigned long long* __restrict__ job_done,
+                                             uint32_t* __restrict__ job_seen, const uint32_t* __restrict__ order,
+                                             const RunCtl* __restrict__ run, LoopCtl* ctl,
+                                             uint32_t* __restrict__ plan_job,
+                                             unsigned long long* __restrict__ plan_start,
+                                             uint32_t* __restrict__ plan_off, uint32_t Q,
+                                             const volatile uint32_t* interrupt,
+                                             cudaGraphConditionalHandle handle, int use_handle) {
+    const uint32_t lane = threadIdx.x;
     // jobs whose last path finished in this step
-    for (uint32_t i = 0; i < run->nactive; ++i) {
+    bool fin = false;
+    const uint32_t na = run->nactive;
+    for (uint32_t i = lane; i < na; i += 32u) {
         const uint32_t j = order[i];
         if (!job_seen[j] && job_done[j] >= jobs[j].total) {
             job_seen[j] = 1u;
-            ctl->job_finished = 1u;
+            fin = true;
         }
     }
+    if (__any_sync(0xffffffffu, fin) && lane == 0) ctl->job_finished = 1u;
     const int in = (int)(ctl->parity & 1u), out = 1 - in;
     const uint32_t chunk = run->chunk ? run->chunk : 0xffffffffu;
     const uint32_t it = ctl->iter + 1u;
-    ctl->iter = it;
-    ctl->iterations += 1u;
-    uint32_t go;
     const uint32_t n_in = ctl->cnt[in], done_to = ctl->chunk_end;
+    __syncwarp();
+    uint32_t go;
     if (done_to < n_in) {  // input rays left: the next chunk of this queue
-        ctl->work[in] = done_to;
-        ctl->chunk_end = done_to + min(chunk, n_in - done_to);
+        if (lane == 0) {
+            ctl->work[in] = done_to;
+            ctl->chunk_end = done_to + min(chunk, n_in - done_to);
+        }
         go = 1u;
     } else {
         go = plan_iteration(jobs, job_next, job_done, order, run, ctl, plan_job, plan_start, plan_off, Q, in, out,
                             chunk);
     }
+    if (lane != 0) return;
+    ctl->iter = it;
+    ctl->iterations += 1u;
     if (run->max_iter && it >= run->max_iter) go = 0u;
     if (run->stop_on_finish && ctl->job_finished) go = 0u;  // hand finished jobs to the host now
     if (*interrupt) go = 0u;                                 // the host has new work to admit
     ctl->running = go;
     if (use_handle) cudaGraphSetConditional(handle, go);
 }
-
 
 // The camera ray of new path t of the iteration (t < gen_n): its plan entry
 // (the last entry i with plan_off[i] <= t; entries may be empty), job, sample
@@ -345,6 +397,7 @@ struct venu_batch {
     std::vector<JobHost> jobs;
     std::vector<uint32_t> order;  // active job slots in plan order (policy)
     uint32_t policy = VENU_POLICY_FIFO;
+    bool order_dirty = false;     // b->order changed since it was last uploaded (at the next run)
     uint32_t chunk = 0;  // rays traced per step (0: a whole iteration per step)
     uint64_t next_seq = 0;
     uint32_t* h_interrupt = nullptr;  // mapped host word
@@ -418,10 +471,7 @@ venu_status build_graph(venu_batch* b) {
 
 void free_batch(venu_batch* b) {
     destroy_graph(b);
-    for (auto& j : b->jobs) {
-        cudaFree(j.seeds);
-        cudaFree(j.slots);
-    }
+    for (auto& j : b->jobs) cudaFree(j.slots);  // seeds share the allocation
     for (int i = 0; i < 2; ++i) {
         cudaFree(b->q[i].o);
         cudaFree(b->q[i].d);
@@ -569,13 +619,15 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     JobHost& J = b->jobs[slot];
     J = JobHost{};
-    cudaError_t e = cudaMallocAsync(&J.seeds, sizeof(uint32_t) * total, st);
-    if (e == cudaSuccess) e = cudaMallocAsync(&J.slots, sizeof(float4) * total, st);
+    // one allocation: the sample slots, then the seed table
+    void* buf = nullptr;
+    cudaError_t e = cudaMallocAsync(&buf, (sizeof(float4) + sizeof(uint32_t)) * total, st);
     if (e != cudaSuccess) {
-        if (J.seeds) cudaFreeAsync(J.seeds, st);
         J = JobHost{};
         return cuda_fail(e, "venu_batch_submit: job buffers");
     }
+    J.slots = static_cast<float4*>(buf);
+    J.seeds = reinterpret_cast<uint32_t*>(J.slots + total);
     J.active = true;
     J.desc = *job;
     J.total = total;
@@ -595,17 +647,12 @@ extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job
     dj.seeds = J.seeds;
     dj.slots = J.slots;
     dj.total = total;
-    VENU_CUDA(cudaMemcpyAsync(b->d_jobs + slot, &dj, sizeof(dj), cudaMemcpyHostToDevice, st));
-    VENU_CUDA(cudaMemsetAsync(b->d_next + slot, 0, sizeof(unsigned long long), st));
-    VENU_CUDA(cudaMemsetAsync(b->d_done + slot, 0, sizeof(unsigned long long), st));
-    VENU_CUDA(cudaMemsetAsync(b->d_seen + slot, 0, sizeof(uint32_t), st));
-    k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(job->camera, o.width, o.height, o.samples_per_pixel,
-                                                                 o.subframe_index, J.seeds, &b->d_jobs[slot].dcam);
+    k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(dj, slot, b->d_jobs, b->d_next, b->d_done,
+                                                                 b->d_seen);
     VENU_CUDA(cudaGetLastError());
     b->order.push_back(slot);
+    b->order_dirty = true;  // uploaded by the next run
     b->resident += J.bytes;
-    venu_status us = upload_order(b, st);
-    if (us != VENU_OK) return us;
     if (job_id) *job_id = slot;
     return VENU_OK;
 }
@@ -616,6 +663,11 @@ extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, ui
         return VENU_ERR_INVALID;
     }
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (b->order_dirty) {
+        venu_status us = upload_order(b, st);
+        if (us != VENU_OK) return us;
+        b->order_dirty = false;
+    }
     RunCtl rc;
     rc.max_iter = max_iterations;
     rc.nactive = (uint32_t)b->order.size();
@@ -686,8 +738,7 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
         VENU_CUDA(cudaGetLastError());
         for (uint32_t slot : fin) {
             JobHost& J = b->jobs[slot];
-            VENU_CUDA(cudaFreeAsync(J.seeds, st));
-            VENU_CUDA(cudaFreeAsync(J.slots, st));
+            VENU_CUDA(cudaFreeAsync(J.slots, st));  // seeds share the allocation
             b->resident -= J.bytes;
             J = JobHost{};
         }
@@ -696,10 +747,7 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
             if (b->jobs[slot].active) keep.push_back(slot);
         b->order.swap(keep);
     }
-    if (!ent.empty() || b->policy == VENU_POLICY_SHORTEST_FIRST) {
-        venu_status us = upload_order(b, st);
-        if (us != VENU_OK) return us;
-    }
+    if (!ent.empty() || b->policy == VENU_POLICY_SHORTEST_FIRST) b->order_dirty = true;
     const uint32_t n = (uint32_t)fin.size();
     if (finished_ids)
         for (uint32_t i = 0; i < n && i < cap; ++i) finished_ids[i] = fin[i];
@@ -717,7 +765,8 @@ extern "C" venu_status venu_batch_set_policy(venu_batch* b, uint32_t policy) {
         return VENU_ERR_INVALID;
     }
     b->policy = policy;
-    return upload_order(b, nullptr);
+    b->order_dirty = true;  // re-sorted and uploaded by the next run
+    return VENU_OK;
 }
 
 extern "C" venu_status venu_batch_set_chunk(venu_batch* b, uint32_t rays) {
