@@ -291,9 +291,9 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
         return segs
 
     def batched(rep):
-        for j, cam, acc, img in zip(jobs, cams, acc_batch, img_batch):
-            b.submit(scenes[j["key"]], cam, j["W"], j["H"], j["spp"], acc, subframe=j["subframe"],
-                     max_depth=j["depth"], reset=True, image8=img)
+        b.submit_many([dict(scene=scenes[j["key"]], camera=cam, width=j["W"], height=j["H"], spp=j["spp"],
+                            accum=acc, subframe=j["subframe"], max_depth=j["depth"], image8=img)
+                       for j, cam, acc, img in zip(jobs, cams, acc_batch, img_batch)])
         b.run()
         done = b.collect()
         assert len(done) == len(jobs)

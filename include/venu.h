@@ -306,6 +306,11 @@ VENU_API uint64_t venu_batch_job_bytes(uint32_t width, uint32_t height, uint32_t
  * seeds on `stream`.  The scene and output buffers must stay valid until the
  * job is collected.  VENU_ERR_TOO_LARGE when max_jobs are admitted. */
 VENU_API venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id);
+/* n jobs at once (one call, one seed-table launch per 32 jobs): job_ids[k]
+ * gets job k's id.  All or nothing: on an error no job of the call is
+ * admitted.  venu_batch_submit is this with n = 1. */
+VENU_API venu_status venu_batch_submit_many(venu_batch* b, const venu_job_desc* jobs, uint32_t n, void* stream,
+                                            uint32_t* job_ids);
 /* Runs the shared path loop for at most max_iterations steps (0 = until
  * every admitted job has finished) as one graph launch on `stream`; a step
  * is one iteration (every queued ray traced once) unless venu_batch_set_chunk

@@ -203,6 +203,37 @@ def test_batch_many_jobs_policy(venu, oracle, cuda, policy):
         assert np.array_equal(j["acc"].cpu().numpy().view(np.uint32), j["want"]["accum"].view(np.uint32))
 
 
+def test_batch_submit_many(venu, oracle, cuda):
+    """One call admits 44 jobs (two seed-table groups of at most 32): every
+    result exact.  All or nothing: a call with one invalid job, or with more
+    jobs than free slots, admits none."""
+    torch = cuda
+    b = venu.Batch(pool_paths=2048, max_jobs=48)
+    scenes = [oracle.scene_rtiow(k) for k in range(3)]
+    dev = [venu.DeviceScene(sp) for sp in scenes]
+    specs, wants = [], []
+    for k in range(44):
+        W, H, spp, depth, sub = 6 + (k % 4) * 3, 5, 1 + k % 3, 4, 1 + k % 4
+        cam, want = _want(oracle, dict(scene=scenes[k % 3], eye=(13, 2, 3), W=W, H=H, spp=spp, depth=depth, sub=sub))
+        specs.append(dict(scene=dev[k % 3], camera=cam, width=W, height=H, spp=spp, subframe=sub, max_depth=depth,
+                          accum=venu.new_accum(W, H)))
+        wants.append(want)
+    bad = dict(specs[0], width=1)
+    with pytest.raises(venu.VenuError):
+        b.submit_many(specs[:3] + [bad])
+    assert b.stats()["active_jobs"] == 0
+    with pytest.raises(venu.VenuError):
+        b.submit_many(specs + specs[:5])  # 49 jobs, 48 slots
+    assert b.stats()["active_jobs"] == 0
+    ids = b.submit_many(specs)
+    assert len(set(ids)) == 44 and b.stats()["active_jobs"] == 44
+    b.run()
+    assert sorted(b.collect()) == sorted(ids)
+    torch.cuda.synchronize()
+    for spec, want in zip(specs, wants):
+        assert np.array_equal(spec["accum"].cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
+
+
 def test_batch_interrupt(venu, oracle, cuda):
     """While the interrupt flag is set a run ends after one iteration;
     cleared, the run goes to the end.  Results are exact."""

@@ -164,6 +164,7 @@ def lib() -> C.CDLL:
     L.venu_batch_job_bytes.restype = C.c_uint64
     L.venu_batch_job_bytes.argtypes = [u32, u32, u32]
     L.venu_batch_submit.argtypes = [vp, C.POINTER(JobDesc), vp, C.POINTER(u32)]
+    L.venu_batch_submit_many.argtypes = [vp, C.POINTER(JobDesc), u32, vp, C.POINTER(u32)]
     L.venu_batch_run.argtypes = [vp, u32, u32, vp]
     L.venu_batch_collect.argtypes = [vp, vp, vp, u32, C.POINTER(u32)]
     L.venu_batch_stats_get.argtypes = [vp, C.POINTER(BatchStats)]
@@ -181,7 +182,7 @@ def lib() -> C.CDLL:
                  "venu_scene_info_get", "venu_scene_export_bvh",
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",
                  "venu_renderer_stats", "venu_renderer_destroy", "venu_renderer_set_tuning",
-                 "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit",
+                 "venu_renderer_get_tuning", "venu_batch_create", "venu_batch_set_tuning", "venu_batch_submit", "venu_batch_submit_many",
                  "venu_batch_run", "venu_batch_collect", "venu_batch_stats_get", "venu_batch_destroy",
                  "venu_batch_set_policy", "venu_batch_interrupt", "venu_batch_set_chunk", "venu_server_set_policy", "venu_server_set_express", "venu_server_end_session",
                  "venu_server_create", "venu_server_submit", "venu_server_wait", "venu_server_cancel",

@@ -560,6 +560,25 @@ class Batch:
         check(lib().venu_batch_submit(self.handle, C.byref(d), _stream_handle(stream), C.byref(jid)))
         return int(jid.value)
 
+    def submit_many(self, jobs, stream=None) -> list:
+        """Admits several jobs with one call (venu_batch_submit_many): each a
+        dict of submit()'s arguments (scene, camera, width, height, spp,
+        accum, and optionally subframe, max_depth, reset, image_f, image8).
+        All or nothing; returns the job ids in order."""
+        n = len(jobs)
+        arr = (_lib.JobDesc * max(1, n))()
+        for d, j in zip(arr, jobs):
+            d.scene = j["scene"].handle.value
+            d.camera = _camera_c(j["camera"])
+            d.opts = RenderOpts(j["width"], j["height"], j["spp"], j.get("subframe", 1), j.get("max_depth", 50),
+                                _lib.FLAG_RESET_ACCUM if j.get("reset", True) else 0)
+            d.accum = ptr(j["accum"]).value
+            d.image_f = ptr(j["image_f"]).value if j.get("image_f") is not None else None
+            d.image8 = ptr(j["image8"]).value if j.get("image8") is not None else None
+        ids = (C.c_uint32 * max(1, n))()
+        check(lib().venu_batch_submit_many(self.handle, arr, n, _stream_handle(stream), ids))
+        return [int(ids[k]) for k in range(n)]
+
     def run(self, max_iterations: int = 0, stop_on_finish: bool = False, stream=None) -> None:
         flags = _lib.RUN_STOP_ON_FINISH if stop_on_finish else 0
         check(lib().venu_batch_run(self.handle, max_iterations, flags, _stream_handle(stream)))

@@ -29,6 +29,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <string>
 #include <vector>
 
 namespace venu {
@@ -68,20 +69,40 @@ struct CollectEntry {
     uint32_t npix, spp, reset, pix_off;
 };
 
-// Admits job dj into table slot `slot`: its raygen RNG state at the start of
-// every sample of every pixel (the seed table), and -- from its first thread
-// -- its table entry with the camera basis and zeroed counters, so a submit
-// is one allocation and this one launch.
-__global__ void k_seed_table(DevJob dj, uint32_t slot, DevJob* __restrict__ jobs,
-                             unsigned long long* __restrict__ job_next, unsigned long long* __restrict__ job_done,
-                             uint32_t* __restrict__ job_seen) {
+// Up to kSeedGroup jobs admitted by one launch, passed by value (no staging
+// copy): their table entries, table slots and pixel offsets.
+constexpr uint32_t kSeedGroup = 32;
+struct SeedGroup {
+    DevJob job[kSeedGroup];
+    uint32_t slot[kSeedGroup];
+    uint32_t pix_off[kSeedGroup + 1];  // pix_off[k]: first thread of job k; pix_off[n]: all pixels
+    uint32_t n;
+};
+
+// Admits a group of jobs: each job's raygen RNG state at the start of every
+// sample of every pixel (the seed table, one thread per pixel), and -- from
+// each job's first thread -- its table entry with the camera basis and
+// zeroed counters.  A submit is one allocation per job and one launch per
+// group.
+__global__ void k_seed_tables(const __grid_constant__ SeedGroup g, DevJob* __restrict__ jobs,
+                              unsigned long long* __restrict__ job_next, unsigned long long* __restrict__ job_done,
+                              uint32_t* __restrict__ job_seen) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.pix_off[g.n]) return;
+    uint32_t lo = 0, hi = g.n;  // last job k with pix_off[k] <= t
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (g.pix_off[mid] <= t) lo = mid; else hi = mid;
+    }
+    const DevJob& dj = g.job[lo];
+    const uint32_t pix = t - g.pix_off[lo];
     const uint32_t W = dj.W, npix = dj.npix;
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
     const DevCamera C = load_camera(dj.cam);
     if (pix == 0) {
-        dj.dcam = C;
-        jobs[slot] = dj;
+        const uint32_t slot = g.slot[lo];
+        DevJob w = dj;
+        w.dcam = C;
+        jobs[slot] = w;
         job_next[slot] = 0ull;
         job_done[slot] = 0ull;
         job_seen[slot] = 0u;
@@ -591,70 +612,124 @@ extern "C" venu_status venu_batch_set_tuning(venu_batch* b, const venu_tuning* t
     return VENU_OK;
 }
 
-extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id) {
-    if (!b || !job || !job->scene || !job->accum) {
-        set_error("venu_batch_submit: NULL argument");
+namespace {
+
+venu_status check_job(const venu_job_desc* job, uint32_t k) {
+    const std::string at = "venu_batch_submit: job " + std::to_string(k) + ": ";
+    if (!job->scene || !job->accum) {
+        set_error(at + "NULL scene or accumulator");
         return VENU_ERR_INVALID;
     }
     const venu_render_opts& o = job->opts;
     if (o.width < 2 || o.height < 2 || o.samples_per_pixel == 0 || o.max_depth == 0 || o.max_depth > 64) {
-        set_error("venu_batch_submit: need width,height >= 2, spp >= 1, 1 <= max_depth <= 64");
+        set_error(at + "need width,height >= 2, spp >= 1, 1 <= max_depth <= 64");
         return VENU_ERR_INVALID;
     }
     const uint64_t npix = (uint64_t)o.width * o.height, total = npix * o.samples_per_pixel;
     if (npix > (1u << 30) || total > 0x7fffffffull) {
-        set_error("venu_batch_submit: a job may have at most 2^31 - 1 paths");
+        set_error(at + "a job may have at most 2^31 - 1 paths");
         return VENU_ERR_TOO_LARGE;
     }
-    uint32_t slot = b->max_jobs;
-    for (uint32_t i = 0; i < b->max_jobs; ++i)
-        if (!b->jobs[i].active) {
-            slot = i;
-            break;
-        }
-    if (slot == b->max_jobs) {
+    return VENU_OK;
+}
+
+cudaError_t launch_seed_group(venu_batch* b, SeedGroup& g, cudaStream_t st) {
+    if (g.n == 0) return cudaSuccess;
+    const uint32_t threads = g.pix_off[g.n];
+    k_seed_tables<<<(threads + 255) / 256, 256, 0, st>>>(g, b->d_jobs, b->d_next, b->d_done, b->d_seen);
+    g.n = 0;
+    g.pix_off[0] = 0;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" venu_status venu_batch_submit_many(venu_batch* b, const venu_job_desc* jobs, uint32_t n, void* stream,
+                                              uint32_t* job_ids) {
+    if (!b || (n && !jobs)) {
+        set_error("venu_batch_submit: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        const venu_status v = check_job(jobs + k, k);
+        if (v != VENU_OK) return v;
+    }
+    std::vector<uint32_t> slots;
+    for (uint32_t i = 0; i < b->max_jobs && slots.size() < n; ++i)
+        if (!b->jobs[i].active) slots.push_back(i);
+    if (slots.size() < n) {
         set_error("venu_batch_submit: max_jobs jobs are already admitted");
         return VENU_ERR_TOO_LARGE;
     }
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    JobHost& J = b->jobs[slot];
-    J = JobHost{};
-    // one allocation: the sample slots, then the seed table
-    void* buf = nullptr;
-    cudaError_t e = cudaMallocAsync(&buf, (sizeof(float4) + sizeof(uint32_t)) * total, st);
-    if (e != cudaSuccess) {
+    SeedGroup g;
+    std::memset(&g, 0, sizeof(g));
+    for (uint32_t k = 0; k < n; ++k) {
+        const venu_job_desc* job = jobs + k;
+        const venu_render_opts& o = job->opts;
+        const uint64_t npix = (uint64_t)o.width * o.height, total = npix * o.samples_per_pixel;
+        const uint32_t slot = slots[k];
+        JobHost& J = b->jobs[slot];
         J = JobHost{};
-        return cuda_fail(e, "venu_batch_submit: job buffers");
+        // one allocation: the sample slots, then the seed table
+        void* buf = nullptr;
+        cudaError_t e = cudaMallocAsync(&buf, (sizeof(float4) + sizeof(uint32_t)) * total, st);
+        // a group holds kSeedGroup jobs and at most 2^31 pixels (one job has at most 2^30)
+        if (e == cudaSuccess && (g.n == kSeedGroup || (uint64_t)g.pix_off[g.n] + npix > (1ull << 31)))
+            e = launch_seed_group(b, g, st);
+        if (e != cudaSuccess) {
+            // nothing of this call is admitted: free what it allocated
+            if (buf) cudaFreeAsync(buf, st);
+            for (uint32_t m = 0; m < k; ++m) {
+                JobHost& P = b->jobs[slots[m]];
+                cudaFreeAsync(P.slots, st);
+                P = JobHost{};
+            }
+            b->jobs[slot] = JobHost{};
+            return cuda_fail(e, "venu_batch_submit: job buffers");
+        }
+        J.slots = static_cast<float4*>(buf);
+        J.seeds = reinterpret_cast<uint32_t*>(J.slots + total);
+        J.active = true;
+        J.desc = *job;
+        J.total = total;
+        J.remaining = total;
+        J.bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel);
+        DevJob& dj = g.job[g.n];
+        dj.scene = view_of(job->scene);
+        dj.cam = job->camera;
+        dj.W = o.width;
+        dj.H = o.height;
+        dj.npix = (uint32_t)npix;
+        dj.spp = o.samples_per_pixel;
+        dj.max_depth = o.max_depth;
+        dj.subframe = o.subframe_index;
+        dj.seeds = J.seeds;
+        dj.slots = J.slots;
+        dj.total = total;
+        g.slot[g.n] = slot;
+        g.pix_off[g.n + 1] = g.pix_off[g.n] + (uint32_t)npix;
+        ++g.n;
     }
-    J.slots = static_cast<float4*>(buf);
-    J.seeds = reinterpret_cast<uint32_t*>(J.slots + total);
-    J.active = true;
-    J.desc = *job;
-    J.total = total;
-    J.remaining = total;
-    J.seq = b->next_seq++;
-    J.bytes = venu_batch_job_bytes(o.width, o.height, o.samples_per_pixel);
-    DevJob dj;
-    std::memset(&dj, 0, sizeof(dj));
-    dj.scene = view_of(job->scene);
-    dj.cam = job->camera;
-    dj.W = o.width;
-    dj.H = o.height;
-    dj.npix = (uint32_t)npix;
-    dj.spp = o.samples_per_pixel;
-    dj.max_depth = o.max_depth;
-    dj.subframe = o.subframe_index;
-    dj.seeds = J.seeds;
-    dj.slots = J.slots;
-    dj.total = total;
-    k_seed_table<<<(uint32_t)((npix + 255) / 256), 256, 0, st>>>(dj, slot, b->d_jobs, b->d_next, b->d_done,
-                                                                 b->d_seen);
-    VENU_CUDA(cudaGetLastError());
-    b->order.push_back(slot);
-    b->order_dirty = true;  // uploaded by the next run
-    b->resident += J.bytes;
-    if (job_id) *job_id = slot;
+    const cudaError_t le = launch_seed_group(b, g, st);
+    if (le != cudaSuccess) return cuda_fail(le, "venu_batch_submit: seed tables");
+    for (uint32_t k = 0; k < n; ++k) {
+        JobHost& J = b->jobs[slots[k]];
+        J.seq = b->next_seq++;
+        b->order.push_back(slots[k]);
+        b->resident += J.bytes;
+        if (job_ids) job_ids[k] = slots[k];
+    }
+    if (n) b->order_dirty = true;  // uploaded by the next run
     return VENU_OK;
+}
+
+extern "C" venu_status venu_batch_submit(venu_batch* b, const venu_job_desc* job, void* stream, uint32_t* job_id) {
+    if (!job) {
+        set_error("venu_batch_submit: NULL argument");
+        return VENU_ERR_INVALID;
+    }
+    return venu_batch_submit_many(b, job, 1, stream, job_id);
 }
 
 extern "C" venu_status venu_batch_run(venu_batch* b, uint32_t max_iterations, uint32_t flags, void* stream) {

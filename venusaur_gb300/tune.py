@@ -136,9 +136,8 @@ def autotune_jobs(jobs, pools=(16 << 20, 32 << 20, 64 << 20), blocks=(64, 128, 2
             b.set_tuning(traverse_variant=2, traverse_block=tb)
 
             def batched():
-                for j, a in zip(jobs, accs):
-                    b.submit(j["scene"], j["camera"], j["W"], j["H"], j["spp"], a, subframe=j["subframe"],
-                             max_depth=j["depth"], reset=True)
+                b.submit_many([dict(scene=j["scene"], camera=j["camera"], width=j["W"], height=j["H"], spp=j["spp"],
+                                    accum=a, subframe=j["subframe"], max_depth=j["depth"]) for j, a in zip(jobs, accs)])
                 b.run()
                 b.collect()
 
