@@ -164,7 +164,9 @@ def test_batch_policy(venu, oracle, cuda, policy):
     if policy == "shortest_first":
         assert first == [small["id"]] and it <= 8
     elif policy == "fifo":
-        assert it >= 18  # 65536 paths through a 4096-path pool (>= 16 iterations) before the small job starts
+        # 65536 paths through a 4096-path pool (>= 16 iterations) before the
+        # small job's paths are generated
+        assert first == [big["id"]] and it >= 16
     else:
         assert first == [big["id"]]  # the small job cannot start before the big one is done
     b.run()

@@ -52,7 +52,8 @@ struct LoopCtl {  // device-owned loop state
     uint32_t plan_n, err;
     uint32_t job_finished;  // set when a job's last path finishes (reset per run)
     uint32_t parity;        // the queue traced in this iteration; flipped by k_plan
-    uint32_t chunk_end;     // this step traces input rays [work start, chunk_end)
+    uint32_t chunk_end;     // this step traces input rays [chunk_start, chunk_end)
+    uint32_t chunk_start;
     unsigned long long segments, paths_done, iterations;
 };
 
@@ -183,6 +184,7 @@ __device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned lon
         ctl->more_gen = more ? 1u : 0u;
         ctl->cnt[in] = 0;    // the next trace writes into the other queue
         ctl->work[out] = 0;  // and fetches from this one, chunk by chunk
+        ctl->chunk_start = 0u;
         ctl->chunk_end = min(chunk, survivors + off);
         ctl->parity = (uint32_t)out;
     }
@@ -227,6 +229,7 @@ __global__ void __launch_bounds__(32) k_plan(const DevJob* __restrict__ jobs,
     if (done_to < n_in) {  // input rays left: the next chunk of this queue
         if (lane == 0) {
             ctl->work[in] = done_to;
+            ctl->chunk_start = done_to;
             ctl->chunk_end = done_to + min(chunk, n_in - done_to);
         }
         go = 1u;
@@ -277,25 +280,25 @@ __device__ __forceinline__ T ld_volatile_ptr(const T* p) {
     return *reinterpret_cast<const volatile T*>(p);
 }
 
-template <bool COUNT>
-__global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
-                                                           unsigned long long* __restrict__ job_done, LoopCtl* ctl,
-                                                           const uint32_t* __restrict__ plan_job,
-                                                           const unsigned long long* __restrict__ plan_start,
-                                                           const uint32_t* __restrict__ plan_off,
-                                                           Queue q0, Queue q1) {
-    extern __shared__ unsigned char smem[];
-    StackSmem sm;
-    sm.node = reinterpret_cast<int*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
-    const int in = (int)(ctl->parity & 1u), out = 1 - in;
-    const Queue qin = in ? q1 : q0, qout = in ? q0 : q1;
-    const uint32_t n = ctl->chunk_end;  // this step: input rays [work[in] at launch, chunk_end)
+// One warp-batch loop of the batch kernel.  IN_PLACE (a step with no more
+// rays than the grid has threads): each path is finished in place, bounce
+// after bounce (the step leaves no survivors); the output queue is unused
+// then, and its throughput slot i carries ray i's state between bounces.
+// (Chunked steps: survivors of earlier chunks of the iteration sit below
+// chunk_start, which no scratch index reaches.)  A separate instantiation,
+// so the ordinary loop keeps its registers.
+template <bool COUNT, bool IN_PLACE>
+__device__ __forceinline__ void trace_shade_multi_loop(const DevJob* __restrict__ jobs,
+                                                       unsigned long long* __restrict__ job_done, LoopCtl* ctl,
+                                                       const uint32_t* __restrict__ plan_job,
+                                                       const unsigned long long* __restrict__ plan_start,
+                                                       const uint32_t* __restrict__ plan_off, const Queue& qin,
+                                                       const Queue& qout, int in, int out, StackSmem sm,
+                                                       bool& overflow, TraceCounters& K, uint32_t& finished,
+                                                       uint32_t& traced) {
+    const uint32_t n = ctl->chunk_end;  // this step: input rays [chunk_start, chunk_end)
     const uint32_t gen_base = ctl->gen_base, np = ctl->plan_n;  // new paths from gen_base on
     const uint32_t lane = threadIdx.x & 31;
-    TraceCounters K{0, 0};
-    bool overflow = false;
-    uint32_t finished = 0, traced = 0;
     for (;;) {
         uint32_t base = 0;
         if (lane == 0) base = atomicAdd(&ctl->work[in], 32u);
@@ -303,7 +306,6 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
         if (base >= n) break;
         const uint32_t i = base + lane;
         const bool valid = i < n;
-        traced += (uint32_t)__popc(__ballot_sync(0xffffffffu, valid));
         uint32_t job = 0xFFFFFFFFu;
         ShadeOut r;
         r.cont = false;
@@ -318,23 +320,33 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
                 d4 = qin.d[i];
             }
             job = __float_as_uint(d4.w) >> 8;
-            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            float t;
-            int32_t k;
-            {
-                const SceneView S = jobs[job].scene;
-                k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            for (bool first = true;; first = false) {
+                RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+                float t;
+                int32_t k;
+                {
+                    const SceneView S = jobs[job].scene;
+                    k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+                }
+                ++traced;  // per lane: one segment
+                // the shading pointers are read again here instead of being kept in
+                // registers through the traversal (the job table is L1/L2-resident)
+                SceneView S2;
+                const SceneView* G = &jobs[job].scene;
+                S2.sph = ld_volatile_ptr(&G->sph);
+                S2.mat = ld_volatile_ptr(&G->mat);
+                S2.meta = ld_volatile_ptr(&G->meta);
+                const float4 t4 = (IN_PLACE && !first) ? qout.t[i]
+                                  : fresh                ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
+                                                         : qin.t[i];
+                const float4 ow = o4;  // .w: the path's slot
+                r = shade_one(S2, o4, d4, t4, make_int2(__float_as_int(t), k));
+                if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(ow.w)] = r.result;
+                if (!IN_PLACE || !r.cont) break;
+                o4 = r.o;
+                d4 = r.d;
+                qout.t[i] = r.t;
             }
-            // the shading pointers are read again here instead of being kept in
-            // registers through the traversal (the job table is L1/L2-resident)
-            SceneView S2;
-            const SceneView* G = &jobs[job].scene;
-            S2.sph = ld_volatile_ptr(&G->sph);
-            S2.mat = ld_volatile_ptr(&G->mat);
-            S2.meta = ld_volatile_ptr(&G->meta);
-            const float4 t4 = fresh ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
-            r = shade_one(S2, o4, d4, t4, make_int2(__float_as_int(t), k));
-            if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(o4.w)] = r.result;
         }
         const uint32_t pos = warp_append(r.cont, &ctl->cnt[out]);
         if (r.cont) {
@@ -351,6 +363,32 @@ __global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __rest
         if (fin && lane == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&job_done[job], (unsigned long long)__popc(peers));
         finished += __popc(__ballot_sync(0xffffffffu, fin));
     }
+}
+
+template <bool COUNT>
+__global__ void VENU_TRACE_MULTI_BOUNDS k_trace_shade_multi(const DevJob* __restrict__ jobs,
+                                                           unsigned long long* __restrict__ job_done, LoopCtl* ctl,
+                                                           const uint32_t* __restrict__ plan_job,
+                                                           const unsigned long long* __restrict__ plan_start,
+                                                           const uint32_t* __restrict__ plan_off,
+                                                           Queue q0, Queue q1) {
+    extern __shared__ unsigned char smem[];
+    StackSmem sm;
+    sm.node = reinterpret_cast<int*>(smem);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
+    const int in = (int)(ctl->parity & 1u), out = 1 - in;
+    const Queue qin = in ? q1 : q0, qout = in ? q0 : q1;
+    const uint32_t lane = threadIdx.x & 31;
+    TraceCounters K{0, 0};
+    bool overflow = false;
+    uint32_t finished = 0, traced = 0;
+    if (ctl->chunk_end - ctl->chunk_start <= gridDim.x * blockDim.x)
+        trace_shade_multi_loop<COUNT, true>(jobs, job_done, ctl, plan_job, plan_start, plan_off, qin, qout, in, out,
+                                            sm, overflow, K, finished, traced);
+    else
+        trace_shade_multi_loop<COUNT, false>(jobs, job_done, ctl, plan_job, plan_start, plan_off, qin, qout, in, out,
+                                             sm, overflow, K, finished, traced);
+    for (int off = 16; off > 0; off >>= 1) traced += __shfl_xor_sync(0xffffffffu, traced, off);
     if (lane == 0 && finished) atomicAdd(&ctl->paths_done, (unsigned long long)finished);
     if (lane == 0 && traced) atomicAdd(&ctl->segments, (unsigned long long)traced);
     if (overflow) atomicOr(&ctl->err, 1u);

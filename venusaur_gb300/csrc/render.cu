@@ -173,6 +173,66 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     }
 }
 
+// One warp-batch loop of the fused kernel.  IN_PLACE (a launch with no more
+// rays than the grid has threads): each path is finished in place, bounce
+// after bounce, instead of going through the next queue (whose launches then
+// find no rays); the output queue is unused then, and its throughput slot i
+// carries ray i's state between bounces.  A separate instantiation, so the
+// ordinary loop keeps its registers.
+template <bool COUNT, bool IN_PLACE>
+__device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue& qin, uint32_t n,
+                                                 uint32_t* __restrict__ work, const Queue& qout,
+                                                 uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
+                                                 const PrimaryGen& gen, const DevCamera& cam, StackSmem sm,
+                                                 bool& overflow, TraceCounters& K, uint32_t& extra) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const uint32_t i = base + lane;
+        const bool valid = i < n;
+        ShadeOut r;
+        r.cont = false;
+        uint32_t slot = 0;
+        if (valid) {
+            float4 o4, d4;
+            uint32_t seed = 0;
+            if (gen.path_seeds) {
+                gen_primary(gen, cam, i, o4, d4, seed);
+            } else {
+                o4 = qin.o[i];
+                d4 = qin.d[i];
+            }
+            slot = (uint32_t)__float_as_int(o4.w);
+            for (bool first = true;; first = false) {
+                RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+                float t;
+                const int32_t k =
+                    trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+                const float4 t4 = (IN_PLACE && !first) ? qout.t[i]
+                                  : gen.path_seeds     ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
+                                                       : qin.t[i];
+                r = shade_one(S, o4, d4, t4, make_int2(__float_as_int(t), k));
+                if (!IN_PLACE || !r.cont) break;
+                o4 = r.o;
+                d4 = r.d;
+                qout.t[i] = r.t;
+                ++extra;
+            }
+        }
+        const uint32_t pos = warp_append(r.cont, cnt_out);
+        if (r.cont) {
+            qout.o[pos] = r.o;
+            qout.d[pos] = r.d;
+            qout.t[pos] = r.t;
+        } else if (valid) {
+            slots[slot] = r.result;
+        }
+    }
+}
+
 // Traverse and shade in one pass: each warp takes 32 rays, traverses them,
 // then shades all 32 together once the warp has reconverged and appends the
 // continuing paths with one ballot and one atomic.  Saves the hit record
@@ -197,44 +257,13 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
     TraceCounters K{0, 0};
     bool overflow = false;
-    for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(work, 32u);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const uint32_t i = base + lane;
-        const bool valid = i < n;
-        float4 o4 = make_float4(0.f, 0.f, 0.f, 0.f), d4 = o4;
-        uint32_t seed = 0;
-        int2 hit = make_int2(0, -1);
-        if (valid) {
-            if (gen.path_seeds) {
-                gen_primary(gen, cam, i, o4, d4, seed);
-            } else {
-                o4 = qin.o[i];
-                d4 = qin.d[i];
-            }
-            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            float t;
-            const int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
-            hit = make_int2(__float_as_int(t), k);
-        }
-        ShadeOut r;
-        r.cont = false;
-        uint32_t slot = 0;
-        if (valid) {
-            slot = (uint32_t)__float_as_int(o4.w);
-            const float4 t4 = gen.path_seeds ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
-            r = shade_one(S, o4, d4, t4, hit);
-        }
-        const uint32_t pos = warp_append(r.cont, cnt_out);
-        if (r.cont) {
-            qout.o[pos] = r.o;
-            qout.d[pos] = r.d;
-            qout.t[pos] = r.t;
-        } else if (valid) {
-            slots[slot] = r.result;
-        }
+    uint32_t extra = 0;  // segments traced in place after a ray's first
+    if (n <= gridDim.x * blockDim.x) {
+        trace_shade_loop<COUNT, true>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
+        for (int off = 16; off > 0; off >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, off);
+        if (lane == 0 && extra) atomicAdd(stats, (unsigned long long)extra);
+    } else {
+        trace_shade_loop<COUNT, false>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
     }
     if (overflow) atomicOr(err, 1u);
     if (COUNT) {
