@@ -688,6 +688,9 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                         VENU_CUDA(cudaEventRecord(e3, st));
                     }
                     launches += 1;
+                    // a first bounce with no more paths than the fused grid has
+                    // threads finishes them all in place: no later bounce has rays
+                    if (b == 0 && (uint64_t)PP * kk <= (uint64_t)r->fused_blocks * (uint64_t)tb) break;
                     continue;
                 }
                 if (v == 0) {
