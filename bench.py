@@ -657,18 +657,18 @@ def main():
     # per segment, summed over every launch of the kernel in one render of a
     # smaller case of the same scene (the queue traffic grows in proportion to
     # the rays), scaled to this launch's segments.  Captures:
-    # profiles/k_trace_shade_rtiow_1920x1080_4spp.md (63.5 B over all 50
-    # bounces), profiles/k_trace_shade_random1m_1920x1080_2spp.md (121.1 B;
-    # 41.4 B on the primary launch) and, for the separate traversal kernel,
+    # profiles/k_trace_shade_rtiow_1920x1080_4spp.md (62.5 B over all 50
+    # bounces), profiles/k_trace_shade_random1m_1920x1080_2spp.md (125.7 B;
+    # 43.4 B on the primary launch) and, for the separate traversal kernel,
     # profiles/k_traverse_random1m_1920x1080_2spp.md (57.4 B over all
     # launches, 59.0 B after the primary one).  Variant 3 on the 1M-sphere
     # scene: the fused kernel's primary figure for the primary rays, the
     # traversal kernel's for the rest.  (c1's queues fit in L2: no figure.)
-    dram_per_seg = {("c2", 2): 63.5, ("c3", 2): 121.1, ("c3", 0): 57.4}.get((args.config, variant))
+    dram_per_seg = {("c2", 2): 62.5, ("c3", 2): 125.7, ("c3", 0): 57.4}.get((args.config, variant))
     if dram_per_seg is not None:
         traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"])
     elif (args.config, variant) == ("c3", 3):
-        traffic = (41.4 * paths_c + 59.0 * (segs_c - paths_c)) / max(1, st["traverse_launches"])
+        traffic = (43.4 * paths_c + 59.0 * (segs_c - paths_c)) / max(1, st["traverse_launches"])
         dram_per_seg = traffic * max(1, st["traverse_launches"]) / max(1, segs_c)
     else:
         traffic = None
