@@ -552,10 +552,11 @@ def main():
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
     # Wave size: every path of the render in flight when it fits, else the
-    # largest wave (128 Mi paths, ~16 GB of queues): fewer waves, fewer tails
-    # (measured on RTIOW 1080p x 256: 16 Mi 8.6, 32 Mi 9.8, 64 Mi 10.3,
-    # 128 Mi 10.7 G segments/s).
-    max_paths = args.max_paths or int(min(128 << 20, W * H * spp))
+    # largest wave the renderer takes (2^28 paths, ~29 GB of queues and
+    # slots): fewer waves, fewer tails (measured on RTIOW 1080p x 256: 16 Mi
+    # 8.6, 32 Mi 9.8, 64 Mi 10.3, 128 Mi 10.7 G segments/s; later, with the
+    # primary rays made in the kernel, 128 Mi 11.07, 256 Mi 11.27).
+    max_paths = args.max_paths or int(min(256 << 20, W * H * spp))
     if args.tuning:
         tuning = json.loads(args.tuning)
     elif not args.no_autotune:
