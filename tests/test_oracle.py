@@ -241,3 +241,25 @@ def test_refit_identity_and_moved(oracle):
     b = oracle.render(mv, cam, 36, 24, 2, subframe=3, max_depth=8)
     assert np.array_equal(a["accum"].view(np.uint32), b["accum"].view(np.uint32))
     assert a["segments"] == b["segments"]
+
+
+def test_invariant_division_magic():
+    """The kernels divide path and pixel indices (< 2^31) by per-wave
+    constants (1..2^30) as a multiply and a shift (Granlund & Montgomery,
+    N = 31): l = ceil(log2 d), m = floor(2^(31+l)/d) + 1 < 2^32,
+    x / d = (x m) >> (31 + l).  Exact for every divisor tried at its
+    boundary dividends."""
+    rng = np.random.default_rng(2)
+    ds = list(range(1, 3000)) + [1 << k for k in range(31)] + [(1 << k) + j for k in range(2, 31) for j in (-1, 1)]
+    ds += [int(x) for x in rng.integers(1, (1 << 30) + 1, 3000)] + [1920, 2073600, 147456, 1 << 30]
+    for d in ds:
+        if not 1 <= d <= 1 << 30:
+            continue
+        l = (d - 1).bit_length()
+        m = (1 << (31 + l)) // d + 1
+        assert m < 1 << 32
+        top = (1 << 31) - 1
+        for x in [0, 1, d - 1, d, d + 1, top, top - 1, top // d * d, top // d * d - 1] + \
+                 [int(v) for v in rng.integers(0, 1 << 31, 8)]:
+            if 0 <= x <= top:
+                assert (x * m) >> (31 + l) == x // d, (x, d)

@@ -37,8 +37,9 @@ namespace venu {
 struct DevJob {
     SceneView scene;
     venu_camera cam;
-    DevCamera dcam;  // load_camera(cam), written by k_seed_table
+    DevCamera dcam;  // load_camera(cam), written by k_seed_tables
     uint32_t W, H, npix, spp, max_depth, subframe;
+    FastDiv div_npix, div_W;  // make_fastdiv(npix), make_fastdiv(W)
     const uint32_t* seeds;  // [spp * npix], sample-major
     float4* slots;          // [spp * npix], sample-major
     unsigned long long total;
@@ -264,11 +265,12 @@ __device__ __forceinline__ void gen_primary(const DevJob* __restrict__ jobs, con
     const DevJob& J = jobs[j];
     const uint32_t l = (uint32_t)(plan_start[lo] + (t - plan_off[lo]));
     const uint32_t npix = J.npix, W = J.W;
-    const uint32_t s = l / npix;
+    const uint32_t s = fast_div(l, J.div_npix);
     const uint32_t pix = l - s * npix;
+    const uint32_t y = fast_div(pix, J.div_W);
     seed = J.seeds[l];
     f3 o, d;
-    camera_ray(J.dcam, pix % W, pix / W, W, J.H, seed, o, d);
+    camera_ray(J.dcam, pix - y * W, y, W, J.H, seed, o, d);
     o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)l));
     d4 = make_float4(d.x, d.y, d.z, __uint_as_float((j << 8) | ((uint32_t)((int)J.max_depth - 1) & kDepthMask)));
 }
@@ -739,6 +741,8 @@ extern "C" venu_status venu_batch_submit_many(venu_batch* b, const venu_job_desc
         dj.W = o.width;
         dj.H = o.height;
         dj.npix = (uint32_t)npix;
+        dj.div_npix = make_fastdiv((uint32_t)npix);
+        dj.div_W = make_fastdiv(o.width);
         dj.spp = o.samples_per_pixel;
         dj.max_depth = o.max_depth;
         dj.subframe = o.subframe_index;

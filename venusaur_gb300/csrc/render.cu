@@ -659,6 +659,8 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
             pg.p0 = p0;
             pg.P = PP;
             pg.depth = (int)maxd - 1;
+            pg.div_P = make_fastdiv(PP);
+            pg.div_W = make_fastdiv(W);
             ++launches;
             for (int b = 0; b < nb; ++b) {
                 const Queue& qi = r->q[b & 1];

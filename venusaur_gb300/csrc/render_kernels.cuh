@@ -32,6 +32,27 @@ __device__ __forceinline__ DevCamera load_camera(const venu_camera& c) {
     return k;
 }
 
+// Division of x < 2^31 by an invariant d (1 <= d <= 2^30) as a multiply and a
+// shift (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994, with N = 31): l = ceil(log2 d),
+// m = floor(2^(31+l) / d) + 1 < 2^32, and x / d = (x m) >> (31 + l) exactly.
+struct FastDiv {
+    uint32_t m, shift;
+};
+
+__host__ __device__ inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while (l < 31u && (1u << l) < d) ++l;
+    FastDiv f;
+    f.m = (uint32_t)((1ull << (31u + l)) / d + 1ull);
+    f.shift = 31u + l;
+    return f;
+}
+
+__device__ __forceinline__ uint32_t fast_div(uint32_t x, FastDiv f) {
+    return (uint32_t)(((unsigned long long)x * f.m) >> f.shift);
+}
+
 // The primary rays of one wave of the single-scene renderer, made inside the
 // fused kernel from each path's raygen seed (k_raygen writes only the seeds):
 // the same queue entry as write_primary, without the round trip through
@@ -41,16 +62,18 @@ struct PrimaryGen {
     const uint32_t* path_seeds;  // [k * P], path pos = s * P + pl
     uint32_t W, H, p0, P;
     int depth;                   // max_depth - 1
+    FastDiv div_P, div_W;        // make_fastdiv(P), make_fastdiv(W)
 };
 
 // C: load_camera(g.cam), made once per block
 __device__ __forceinline__ void gen_primary(const PrimaryGen& g, const DevCamera& C, uint32_t pos, float4& o4,
                                             float4& d4, uint32_t& seed) {
-    const uint32_t s = pos / g.P;
+    const uint32_t s = fast_div(pos, g.div_P);
     const uint32_t pix = g.p0 + (pos - s * g.P);
+    const uint32_t y = fast_div(pix, g.div_W);
     seed = g.path_seeds[pos];
     f3 o, d;
-    camera_ray(C, pix % g.W, pix / g.W, g.W, g.H, seed, o, d);
+    camera_ray(C, pix - y * g.W, y, g.W, g.H, seed, o, d);
     o4 = make_float4(o.x, o.y, o.z, __int_as_float((int)pos));
     d4 = make_float4(d.x, d.y, d.z, __uint_as_float((uint32_t)g.depth & kDepthMask));
 }
