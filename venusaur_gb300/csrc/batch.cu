@@ -47,7 +47,7 @@ struct DevJob {
 
 struct LoopCtl {  // device-owned loop state
     uint32_t cnt[2], work[2];
-    uint32_t iter, running, more_gen;
+    uint32_t iter, running;
     uint32_t gen_n;     // new paths of this iteration (made by the trace kernel) ...
     uint32_t gen_base;  // ... at input indices [gen_base, gen_base + gen_n), after the survivors
     uint32_t plan_n, err;
@@ -182,7 +182,6 @@ __device__ uint32_t plan_iteration(const DevJob* __restrict__ jobs, unsigned lon
         ctl->gen_n = off;
         ctl->gen_base = survivors;
         ctl->cnt[out] = survivors + off;
-        ctl->more_gen = more ? 1u : 0u;
         ctl->cnt[in] = 0;    // the next trace writes into the other queue
         ctl->work[out] = 0;  // and fetches from this one, chunk by chunk
         ctl->chunk_start = 0u;
