@@ -600,7 +600,7 @@ class Batch:
         ids = (C.c_uint32 * self.max_jobs)()
         n = C.c_uint32()
         check(lib().venu_batch_collect(self.handle, _stream_handle(stream), ids, self.max_jobs, C.byref(n)))
-        return [int(ids[i]) for i in range(n.value)]
+        return [int(ids[i]) for i in range(min(n.value, self.max_jobs))]
 
     def stats(self) -> dict:
         s = _lib.BatchStats()

@@ -830,11 +830,24 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
     std::vector<CollectEntry> ent;
     std::vector<uint32_t> fin;
     uint32_t pix_off = 0;
+    // one k_collect per group of finished jobs with at most 2^31 pixels
+    // (a job has at most 2^30), so the thread index stays 32-bit
+    auto flush = [&]() -> cudaError_t {
+        if (ent.empty()) return cudaSuccess;
+        cudaError_t e = cudaMemcpyAsync(b->d_collect, ent.data(), sizeof(CollectEntry) * ent.size(),
+                                        cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return e;
+        k_collect<<<(pix_off + 255) / 256, 256, 0, st>>>(b->d_collect, (uint32_t)ent.size(), pix_off);
+        ent.clear();
+        pix_off = 0;
+        return cudaGetLastError();
+    };
     for (uint32_t slot : b->order) {
         JobHost& J = b->jobs[slot];
         J.remaining = J.total - std::min<uint64_t>(done[slot], J.total);
         if (done[slot] < J.total) continue;
         const venu_render_opts& o = J.desc.opts;
+        if ((uint64_t)pix_off + (uint64_t)o.width * o.height > (1ull << 31)) VENU_CUDA(flush());
         CollectEntry c;
         c.accum = reinterpret_cast<float4*>(J.desc.accum);
         c.image_f = reinterpret_cast<float4*>(J.desc.image_f);
@@ -848,10 +861,8 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
         ent.push_back(c);
         fin.push_back(slot);
     }
-    if (!ent.empty()) {
-        VENU_CUDA(cudaMemcpyAsync(b->d_collect, ent.data(), sizeof(CollectEntry) * ent.size(), cudaMemcpyHostToDevice, st));
-        k_collect<<<(pix_off + 255) / 256, 256, 0, st>>>(b->d_collect, (uint32_t)ent.size(), pix_off);
-        VENU_CUDA(cudaGetLastError());
+    VENU_CUDA(flush());
+    if (!fin.empty()) {
         for (uint32_t slot : fin) {
             JobHost& J = b->jobs[slot];
             VENU_CUDA(cudaFreeAsync(J.slots, st));  // seeds share the allocation
@@ -863,7 +874,7 @@ extern "C" venu_status venu_batch_collect(venu_batch* b, void* stream, uint32_t*
             if (b->jobs[slot].active) keep.push_back(slot);
         b->order.swap(keep);
     }
-    if (!ent.empty() || b->policy == VENU_POLICY_SHORTEST_FIRST) b->order_dirty = true;
+    if (!fin.empty() || b->policy == VENU_POLICY_SHORTEST_FIRST) b->order_dirty = true;
     const uint32_t n = (uint32_t)fin.size();
     if (finished_ids)
         for (uint32_t i = 0; i < n && i < cap; ++i) finished_ids[i] = fin[i];

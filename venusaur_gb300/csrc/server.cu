@@ -333,6 +333,7 @@ venu_status run_lane(venu_server* s, int l, uint32_t max_iter, std::vector<uint3
     if (rs == VENU_OK) rs = venu_batch_collect(b, s->st, fin.data(), (uint32_t)fin.size(), &nfin);
     if (rs != VENU_OK) return rs;
     std::vector<Request*> done;
+    nfin = std::min<uint32_t>(nfin, (uint32_t)fin.size());  // fin holds max_jobs ids, the most a collect returns
     for (uint32_t i = 0; i < nfin; ++i) {
         auto it = s->active[l].find(fin[i]);
         if (it == s->active[l].end()) continue;
