@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
 // find no rays); the output queue is unused then, and its throughput slot i
 // carries ray i's state between bounces.  A separate instantiation, so the
 // ordinary loop keeps its registers.
-template <bool COUNT, bool IN_PLACE>
+template <bool COUNT, bool IN_PLACE, int KS>
 __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue& qin, uint32_t n,
                                                  uint32_t* __restrict__ work, const Queue& qout,
                                                  uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
@@ -210,7 +210,7 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
                 RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
                 float t;
                 const int32_t k =
-                    trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+                    trace_closest<COUNT, KS>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
                 const float4 t4 = (IN_PLACE && !first) ? qout.t[i]
                                   : gen.path_seeds     ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
                                                        : qin.t[i];
@@ -237,7 +237,7 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
 // then shades all 32 together once the warp has reconverged and appends the
 // continuing paths with one ballot and one atomic.  Saves the hit record
 // round trip, the second read of the rays and one launch per bounce.
-template <bool COUNT>
+template <bool COUNT, int KS>
 __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
                                                      uint32_t* __restrict__ work, Queue qout,
                                                      uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
@@ -246,7 +246,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
     extern __shared__ unsigned char smem[];
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
-    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * kShared * blockDim.x);
+    sm.tn = reinterpret_cast<float*>(smem + sizeof(int) * KS * blockDim.x);
     __shared__ DevCamera cam;  // the primary rays' camera basis, once per block
     if (gen.path_seeds) {      // a kernel parameter: the same in every thread
         if (threadIdx.x == 0) cam = load_camera(gen.cam);
@@ -259,11 +259,11 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
     bool overflow = false;
     uint32_t extra = 0;  // segments traced in place after a ray's first
     if (n <= gridDim.x * blockDim.x) {
-        trace_shade_loop<COUNT, true>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
+        trace_shade_loop<COUNT, true, KS>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
         for (int off = 16; off > 0; off >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, off);
         if (lane == 0 && extra) atomicAdd(stats, (unsigned long long)extra);
     } else {
-        trace_shade_loop<COUNT, false>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
+        trace_shade_loop<COUNT, false, KS>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
     }
     if (overflow) atomicOr(err, 1u);
     if (COUNT) {
@@ -375,7 +375,8 @@ SceneView view_of(const venu_scene* s) {
     return v;
 }
 
-size_t traverse_smem(int block) { return (size_t)block * kShared * (sizeof(int) + sizeof(float)); }
+size_t traverse_smem(int block, int entries) { return (size_t)block * entries * (sizeof(int) + sizeof(float)); }
+size_t traverse_smem(int block) { return traverse_smem(block, kShared); }
 
 }  // namespace venu
 
@@ -423,20 +424,25 @@ cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
     const size_t sm = traverse_smem((int)t.traverse_block);
     cudaError_t e;
-    if (t.traverse_variant == 3) {  // fused primary bounce, then variant 0
-        e = occupancy_grid(k_trace_shade<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->fused_blocks);
+    if (t.traverse_variant >= 2) {  // the fused kernel: every bounce (2), the primary one (3)
+        e = occupancy_grid(k_trace_shade<false, kShared>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm,
+                           r->fused_blocks);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_trace_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            e = cudaFuncSetAttribute(k_trace_shade<true, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        // the shallow-tree instantiation needs less shared memory; same grid
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade<false, kSharedShallow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade<true, kSharedShallow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm);
         if (e != cudaSuccess) return e;
     }
     if (t.traverse_variant == 0 || t.traverse_variant == 3) {
         e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     } else if (t.traverse_variant == 2) {
-        e = occupancy_grid(k_trace_shade<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_trace_shade<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        r->fused_blocks = r->trav_blocks;
+        r->trav_blocks = r->fused_blocks;
     } else {
         e = occupancy_grid(k_traverse_dyn<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess)
@@ -644,6 +650,9 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     // per-path seeds, kept in the first queue's throughput array (bounce 0
     // reads no queue and writes the other one)
     const bool gen0 = tu.traverse_variant >= 2u;
+    // small scenes have shallow trees: a 4-entry shared stack leaves more of
+    // the SM's memory to L1 (measured: RTIOW +0.5 %; 1M spheres -4.5 %)
+    const bool shallow = scene->n <= 4096u;
     uint32_t* const path_seeds = gen0 ? reinterpret_cast<uint32_t*>(r->q[0].t) : nullptr;
     for (uint32_t s0 = 0; s0 < spp; s0 += k) {
         const uint32_t kk = std::min(k, spp - s0);
@@ -676,14 +685,21 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                 const uint32_t v = tu.traverse_variant <= 2u ? tu.traverse_variant : (b == 0 ? 2u : 0u);
                 if (v == 2) {
                     pg.path_seeds = (b == 0) ? path_seeds : nullptr;
-                    if (count)
-                        k_trace_shade<true><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
-                                                                             r->cnt + b + 1, r->slots, r->err, r->stats,
-                                                                             pg);
-                    else
-                        k_trace_shade<false><<<r->fused_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,
-                                                                              r->cnt + b + 1, r->slots, r->err,
-                                                                              r->stats, pg);
+                    if (shallow) {
+                        const size_t fsm = traverse_smem(tb, kSharedShallow);
+                        if (count)
+                            k_trace_shade<true, kSharedShallow><<<r->fused_blocks, tb, fsm, st>>>(
+                                S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                        else
+                            k_trace_shade<false, kSharedShallow><<<r->fused_blocks, tb, fsm, st>>>(
+                                S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                    } else if (count) {
+                        k_trace_shade<true, kShared><<<r->fused_blocks, tb, tsm, st>>>(
+                            S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                    } else {
+                        k_trace_shade<false, kShared><<<r->fused_blocks, tb, tsm, st>>>(
+                            S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                    }
                     if (prof) {
                         VENU_CUDA(cudaEventRecord(e1, st));
                         VENU_CUDA(cudaEventRecord(e2, st));

@@ -375,6 +375,7 @@ __device__ __forceinline__ bool sphere_test(const RayPre& R, float4 S, float tmi
 // smaller slot, so the result does not depend on traversal order.
 // ---------------------------------------------------------------------------
 constexpr int kShared = 8;   // shared-memory entries per thread (power of two)
+constexpr int kSharedShallow = 4;  // the fused kernel's choice for shallow trees (small scenes)
 constexpr int kSpill = 64;   // local-memory entries beyond those
 
 struct StackSmem {
@@ -392,7 +393,7 @@ struct TraceCounters {
 // inline) and descends or pops; both return whether more work remains.  The
 // same state machine serves the one-ray-per-thread kernels (trace_closest)
 // and the persistent kernels that refill idle lanes.
-template <bool COUNT, bool AXIS = false>
+template <bool COUNT, bool AXIS = false, int KS = kShared>
 struct Tracer {
     RayPre R;
     float tmin, tmax, best_t;
@@ -479,9 +480,9 @@ struct Tracer {
                 far_tn = tn1;
                 cur = w0;
             }
-            const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
-            if (sp >= kShared) {
-                const int g = sp - kShared;
+            const uint32_t j = (uint32_t)(sp & (KS - 1)) * bdim + tid;
+            if (sp >= KS) {
+                const int g = sp - KS;
                 if (g >= kSpill) {
                     overflow = true;
                     return false;
@@ -504,12 +505,12 @@ struct Tracer {
         }
         while (sp > 0) {
             --sp;
-            const uint32_t j = (uint32_t)(sp & (kShared - 1)) * bdim + tid;
+            const uint32_t j = (uint32_t)(sp & (KS - 1)) * bdim + tid;
             const int32_t e = sm.node[j];
             const float etn = sm.tn[j];
-            if (sp >= kShared) {
-                sm.node[j] = spill[sp - kShared];
-                sm.tn[j] = spill_tn[sp - kShared];
+            if (sp >= KS) {
+                sm.node[j] = spill[sp - KS];
+                sm.tn[j] = spill_tn[sp - KS];
             }
             if (etn <= best_t) {
                 cur = e;
@@ -529,12 +530,12 @@ struct Tracer {
     }
 };
 
-template <bool COUNT, bool AXIS>
+template <bool COUNT, bool AXIS, int KS = kShared>
 __device__ __forceinline__ int32_t trace_closest_as(const SceneView& S, const RayPre& R, float tmin,
                                                     float tmax, float& t_out, StackSmem sm,
                                                     uint32_t tid, uint32_t bdim, bool& overflow,
                                                     TraceCounters& K) {
-    Tracer<COUNT, AXIS> T;
+    Tracer<COUNT, AXIS, KS> T;
     int spill[kSpill];
     float spill_tn[kSpill];
     if (T.begin(S, R, tmin, tmax, K))
@@ -544,14 +545,15 @@ __device__ __forceinline__ int32_t trace_closest_as(const SceneView& S, const Ra
 }
 
 // Closest hit of one ray (R from prep): the shared-margin loop, or the
-// per-axis one for the rare near-axis-parallel ray.
-template <bool COUNT>
+// per-axis one for the rare near-axis-parallel ray.  KS: shared-memory stack
+// entries per thread (the kernel's StackSmem holds KS of them).
+template <bool COUNT, int KS = kShared>
 __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPre& R, float tmin,
                                                  float tmax, float& t_out, StackSmem sm,
                                                  uint32_t tid, uint32_t bdim, bool& overflow,
                                                  TraceCounters& K) {
-    if (R.axis) return trace_closest_as<COUNT, true>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
-    return trace_closest_as<COUNT, false>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
+    if (R.axis) return trace_closest_as<COUNT, true, KS>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
+    return trace_closest_as<COUNT, false, KS>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
 }
 
 // ---------------------------------------------------------------------------
