@@ -1,28 +1,38 @@
 """Benchmark: path segments/s of the RTIOW path tracer on GB300.
 
-Default workload (`--config c2`): the RTIOW final scene (485 spheres, seed 0),
-1920x1080, 256 spp, max depth 50, FP32 Kahan accumulation, rendered by the
-plain single-scene wavefront method.  One step = one full render (Draw) of
-that image.  Inputs are synthetic (the seeded scene generator); the working
-set of the ray queues (>1.5 GB) is far larger than L2, so no explicit L2
-flush is done between steps.
+Headline workload (`--config c2`): the RTIOW final scene (485 spheres, seed
+0), 1920x1080, 256 spp, max depth 50, FP32 Kahan accumulation, rendered by
+the plain single-scene wavefront method.  One step = one full render (Draw)
+of that image.  Inputs are synthetic (the seeded scene generator); the
+working set of the ray queues (>1.5 GB) is far larger than L2, so no explicit
+L2 flush is done between steps.
 
 Reported keys (one JSON line on rank 0):
   value      segments/s with the scene resident (device-timed, CUDA events)
   e2e        the same metric through the public C ABI from host memory:
              scene upload + LBVH build + render + image download per step
-  roofline   the traversal kernel's algorithmic bytes per launch / its
-             event-timed duration, against the measured HBM copy bandwidth
-  cpu_baseline  the CPU port (oracle) on a bounded row sample of the workload
+  roofline   the traversal kernel: algorithmic bytes per launch / its
+             event-timed duration against the measured HBM copy bandwidth,
+             the measured SIMD utilisation of its traversal loop, its FP32
+             rate, and (when the kernel sources match the ones the ncu
+             figures were taken on) DRAM bytes per segment
+  configs    the other single-GPU configurations: c1 (400x225x16) and c3
+             (1M spheres, 1080p x 64, with the LBVH build time and bytes
+             fetched per ray segment)
+  cpu_baseline  the reference's arithmetic (its intersection and shading
+             programs restated on the host, closest hit through the host LBVH)
+             on a fixed sample of the workload, every host thread
+  batched / batched_small_jobs / served   plain vs batched vs served methods
 
-`--impl reference` times the reference's path-tracing algorithm on the host
-cores (the CPU port, all threads) on the same config and prints its line.
-With torchrun (N>1) each rank renders its own replica (no collective on the
-data path); rank 0 prints the aggregate.
+`--impl reference` times the same host restatement of the reference's
+arithmetic on the same fixed sample each step and prints its line; it loads
+nothing of the product library.  With torchrun (N>1) each rank renders its
+own replica (no collective on the data path); rank 0 prints the aggregate.
 """
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import subprocess
@@ -43,8 +53,37 @@ CONFIGS = {
     "c3": dict(workload="1M-sphere scene (200x20x200 box), 1920x1080, 64 spp, depth 50, plain wavefront",
                scene="random1m", W=1920, H=1080, spp=64, depth=50, eye=(60, 15, 60)),
 }
+# The fixed CPU sample of each configuration: rows [r0, r1) of the image at
+# `spp` samples per pixel, subframe 1.  The cpu_baseline leg and every step of
+# the reference arm render exactly this sample.
+CPU_SAMPLE = {
+    "c1": dict(rows=(0, 225), spp=16),
+    "c2": dict(rows=(540, 1080), spp=64),
+    "c3": dict(rows=(540, 548), spp=8),
+}
 METRIC = "path segments/s on 1 GB300 (batched/served vs plain); p50/p99 render latency"
 UNIT = "segments/s"
+
+# Sources of the plain renderer's kernels: the ncu figures below hold only
+# while these files are byte-identical to the ones they were taken on.
+KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/render_kernels.cuh",
+                  "venusaur_gb300/csrc/render.cu")
+# ncu figures of the dominant kernel, per (config, traverse variant), summed
+# over every launch of one render of a reduced case of the same scene (fewer
+# samples per pixel: the per-segment traffic does not depend on the sample
+# count).  dram_b_per_seg = (dram__bytes_read.sum + dram__bytes_write.sum) /
+# segments; lanes_per_inst = smsp__thread_inst_executed_per_inst_executed.ratio
+# (active lanes per issued instruction, all instructions).  `sha` is
+# kernel_sources_sha() of the captured build.
+NCU_FIGURES = {"sha": None, "figures": {}}
+
+
+def kernel_sources_sha() -> str:
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def load_peaks():
@@ -62,6 +101,14 @@ def make_scene(venu, kind):
     if kind == "random1m":
         return venu.generate_random(1_000_000, 1)
     raise ValueError(kind)
+
+
+def oracle_scene(O, cfg):
+    """The same scene and camera from the oracle's own generators (equal to
+    the product's byte for byte), so a CPU leg needs nothing of the product."""
+    sp = O.scene_rtiow(0) if cfg["scene"] == "rtiow" else O.scene_random(1_000_000, 1)
+    cam = O.camera(cfg["eye"], (0, 0, 0), 20.0, cfg["W"] / cfg["H"], 0.1, 10.0)
+    return sp, cam
 
 
 class ClockSampler:
@@ -116,46 +163,31 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_sample(O, spheres, cam, cfg, nthreads, target_s=12.0, mode=None, size=None):
-    """Times the CPU port on a bounded row sample sized to ~target_s seconds
-    (or of the given size: (rows, spp) from an earlier call)."""
+def cpu_run(O, spheres, cam, cfg, name, mode, nthreads, repeats=1):
+    """Renders the fixed CPU sample of configuration `name` `repeats` times
+    on the host; returns (segments/s, seconds, segments, description)."""
     from oracle import pyoracle
 
-    mode = pyoracle.MODE_GB300 if mode is None else mode
-    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
-    r0 = H // 2
-    if size is not None:
-        rows, spp_s = size
+    smp = CPU_SAMPLE[name]
+    (r0, r1), spp = smp["rows"], smp["spp"]
+    W, H, depth = cfg["W"], cfg["H"], cfg["depth"]
+    segs, secs = 0, 0.0
+    for _ in range(repeats):
         t0 = time.perf_counter()
-        res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
-                       rows=(r0, r0 + rows))
-        dt = time.perf_counter() - t0
-        sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
-        return res["segments"] / dt, dt, sample, res["segments"], (rows, spp_s)
-    # probe: rate and segments per path, then size rows (and samples) to the target
-    rows, spp_s = 4, min(spp, 2)
-    t0 = time.perf_counter()
-    res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
-                   rows=(r0, r0 + rows))
-    dt = max(time.perf_counter() - t0, 1e-3)
-    # a small probe underestimates a many-core rate (thread start-up), so
-    # re-size from each run until a run lasts at least half the target
-    for _ in range(3):
-        seg_per_path = res["segments"] / (rows * W * spp_s)
-        want_paths = (res["segments"] / dt) * target_s / max(seg_per_path, 1e-9)
-        spp_s = min(spp, 4)
-        rows = int(max(2, min(H - r0, want_paths / (W * spp_s))))
-        if rows == H - r0:
-            spp_s = int(max(spp_s, min(spp, want_paths / (W * rows))))
-        t0 = time.perf_counter()
-        res = O.render(spheres, cam, W, H, spp_s, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
-                       rows=(r0, r0 + rows))
-        dt = time.perf_counter() - t0
-        if dt >= 0.5 * target_s or (rows == H - r0 and spp_s == spp):
-            break
-    rate = res["segments"] / dt
-    sample = f"rows [{r0},{r0 + rows}) x {W} px x {spp_s} spp (depth {depth}) of the {W}x{H} workload"
-    return rate, dt, sample, res["segments"], (rows, spp_s)
+        res = O.render(spheres, cam, W, H, spp, subframe=1, max_depth=depth, mode=mode, nthreads=nthreads,
+                       rows=(r0, r1))
+        secs += time.perf_counter() - t0
+        segs += res["segments"]
+    arith = {pyoracle.MODE_REF_BVH: "reference", pyoracle.MODE_GB300: "gb300", pyoracle.MODE_REF: "reference"}[mode]
+    desc = (f"rows [{r0},{r1}) x {W} px x {spp} spp (depth {depth}, subframe 1) of the {W}x{H} workload, "
+            f"{arith} arithmetic")
+    return segs / secs, secs, segs, desc
+
+
+REF_ARITH = ("the reference's intersection, closest-hit and miss programs (Core/RayTracer.cu:163-449: half-b "
+             "quadratic, double-precision dielectric, pow() Schlick, recursive attenuation) restated on the host "
+             "and bit-exact with the reference's own RayTracer.cu compiled for the host; closest hit through "
+             "the host LBVH in place of OptiX's traversal")
 
 
 def rmse_vs_reference(venu, torch, O, ds, spheres, cam, W, H, depth, spp=16):
@@ -462,23 +494,22 @@ def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, 
     return out
 
 
-def run_reference(args, cfg, world, rank):
-    if rank != 0:
+def run_reference(args, cfg):
+    """The reference arm: the reference's arithmetic on the host cores (the
+    oracle's REF_BVH mode), the fixed CPU sample of the configuration per
+    step.  It builds its scene and camera with the oracle's own generators and
+    loads nothing of the product library.  Under torchrun only rank 0 works."""
+    if int(os.environ.get("RANK", "0")) != 0:
         return
     from oracle import pyoracle
 
     pyoracle.build()
     O = pyoracle.Oracle()
-    import venusaur_gb300 as venu
-
-    spheres = make_scene(venu, cfg["scene"])
-    cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, cfg["W"] / cfg["H"], 0.1, 10.0)
+    spheres, cam = oracle_scene(O, cfg)
     nt = os.cpu_count() or 1
-    times, segs, size = [], 0, None
+    times, segs = [], 0
     for i in range(args.warmup + args.steps):
-        # the first call sizes the sample (each step ~20 s / steps); the rest reuse it
-        rate, dt, sample, s, size = cpu_sample(O, spheres, cam, cfg, nt,
-                                               target_s=max(2.0, 20.0 / max(1, args.steps)), size=size)
+        rate, dt, s, sample = cpu_run(O, spheres, cam, cfg, args.config, pyoracle.MODE_REF_BVH, nt)
         if i >= args.warmup:
             times.append(dt)
             segs += s
@@ -486,68 +517,24 @@ def run_reference(args, cfg, world, rank):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded RTIOW generator)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": cfg["workload"], "cpu_sample": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "arithmetic": "reference",
+                         "sample": sample, "what": REF_ARITH},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="venu", choices=["venu", "reference"])
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
-    ap.add_argument("--max-paths", type=int, default=0)
-    ap.add_argument("--spp", type=int, default=0, help="override the config's samples per pixel (small profiling cases)")
-    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
-    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
-    ap.add_argument("--tuning", default="", help="JSON launch shapes to use instead of the autotuner's")
-    ap.add_argument("--profile-mixed", type=int, default=0, metavar="STEPS",
-                    help="only run STEPS loop steps of the first 12 jobs of the mixed workload (~4 GB on the "
-                         "device) through the batch engine's host-driven loop (ncu cannot profile kernels "
-                         "inside conditional graphs) and exit")
-    ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
-    args = ap.parse_args()
-    cfg = dict(CONFIGS[args.config])
-    if args.spp:
-        cfg["spp"] = args.spp
-        cfg["workload"] = cfg["workload"].replace(f"{CONFIGS[args.config]['spp']} spp", f"{args.spp} spp")
-    from venusaur_gb300.replicas import Replicas
-
-    rep = Replicas()
-    world, rank, local = rep.world, rep.rank, rep.local
-    if args.impl == "reference":
-        run_reference(args, cfg, world, rank)
-        return
-
-    import torch
-
-    torch.cuda.set_device(local)
-    import venusaur_gb300 as venu
-    from venusaur_gb300 import build as vb
-
-    vb.build()
-    if args.profile_mixed:
-        profile_mixed(venu, torch, args)
-        return
+def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
+    """The plain single-scene method on one configuration: autotuned launch
+    shapes, `warmup` untimed renders, `steps` renders timed with CUDA events,
+    then deterministic replays of the last step for the roofline (events
+    around every traversal launch; a counting build for box and sphere tests
+    and the traversal loop's SIMD utilisation).  Returns (block, state)."""
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     spheres = make_scene(venu, cfg["scene"])
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
-    # CPU baseline first, on an idle host (rank 0, single process only): the
-    # oracle port on a bounded row sample of the same workload, every core.
-    cpu_baseline = None
-    if not args.no_cpu and world == 1:
-        from oracle import pyoracle
-
-        pyoracle.build()
-        O = pyoracle.Oracle()
-        nt = os.cpu_count() or 1
-        rate, dt, sample, _, _ = cpu_sample(O, spheres, cam, cfg, nt)
-        cpu_baseline = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample, "seconds": dt}
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
@@ -572,47 +559,40 @@ def main():
     def step(i):
         wf.render(ds, cam, W, H, spp, accum, subframe=1 + i, max_depth=depth, reset=True, image8=img8)
 
-    for i in range(args.warmup):
+    for i in range(warmup):
         step(i)
     torch.cuda.synchronize()
-
-    barrier = rep.barrier
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    barrier()
+    clocks = ClockSampler(rep.local) if headline else None
+    if clocks:
+        clocks.start()
+    rep.barrier()
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for i in range(args.steps):
-        step(args.warmup + i)
+    for i in range(steps):
+        step(warmup + i)
     e1.record(stream)
     torch.cuda.synchronize()
-    barrier()
-    clk = clocks.stop()
+    rep.barrier()
+    clk = clocks.stop() if clocks else None
     # per-step stats are those of the last render; every step renders the
     # same workload (only the seed differs), so counts are per step
     st = wf.stats()
     segs_step = st["segments"]
     # replicas: segments of every rank over the slowest rank's time
-    total_segs, secs, value = rep.throughput(segs_step * args.steps, e0.elapsed_time(e1) / 1000.0)
+    total_segs, secs, value = rep.throughput(segs_step * steps, e0.elapsed_time(e1) / 1000.0)
     ms = 1000.0 * secs
-    launches = st["kernel_launches"] * args.steps
 
     # --- roofline of the traversal kernel -----------------------------------
-    # The last timed step is rendered again twice: once with CUDA events
-    # around every traverse/shade launch (per-kernel device time), once with
-    # the counting traversal (nodes visited, spheres tested).  Both are
-    # deterministic replays of the same workload as the timed steps.
-    last_sub = 1 + args.warmup + args.steps - 1
+    last_sub = 1 + warmup + steps - 1
     acc2 = venu.new_accum(W, H)
     wfp = venu.Wavefront(max_paths, profile=True)
     if tuning:
         wfp.set_tuning(**tuning)
     wfp.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
     torch.cuda.synchronize()
-    st = wfp.stats()
+    stp = wfp.stats()
     wfp.close()
     wfc = venu.Wavefront(max_paths, count=True)
     if tuning:
@@ -645,59 +625,74 @@ def main():
     else:
         kernel = "k_traverse"
         kbytes = trav_bytes + segs_c * 40
-    per_launch_bytes = kbytes / max(1, st["traverse_launches"])
-    avg_launch_ms = st["traverse_ms"] / max(1, st["traverse_launches"])
-    achieved = per_launch_bytes / (avg_launch_ms / 1000.0) / 1e9
+    nl = max(1, stp["traverse_launches"])
+    per_launch_bytes = kbytes / nl
+    avg_launch_s = stp["traverse_ms"] / nl / 1000.0
+    achieved = per_launch_bytes / avg_launch_s / 1e9
     peak, peak_kind = load_peaks()
     # FP32 view (per-segment estimate): 20 flop per box, 25 per sphere, 60
-    # per shade, 30 per camera ray (made in the fused kernel); peak = 152 SMs
-    # x 128 lanes x 2 x max SM clock
+    # per shade, 30 per camera ray (made in the fused kernel); peak = SMs x
+    # 128 FP32 lanes x 2 (FMA) x the highest SM clock seen (else 2070 MHz)
     kflops = nodes * 20 + sph * 25 + (segs_c * 60 + paths_c * 30 if fused else 0)
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12
-    # DRAM traffic per launch: ncu's dram__bytes_read.sum + dram__bytes_write.sum
-    # per segment, summed over every launch of the kernel in one render of a
-    # smaller case of the same scene (the queue traffic grows in proportion to
-    # the rays), scaled to this launch's segments.  Captures:
-    # profiles/k_trace_shade_rtiow_1920x1080_4spp.md (62.5 B over all 50
-    # bounces), profiles/k_trace_shade_random1m_1920x1080_2spp.md (125.7 B;
-    # 43.4 B on the primary launch) and, for the separate traversal kernel,
-    # profiles/k_traverse_random1m_1920x1080_2spp.md (57.4 B over all
-    # launches, 59.0 B after the primary one).  Variant 3 on the 1M-sphere
-    # scene: the fused kernel's primary figure for the primary rays, the
-    # traversal kernel's for the rest.  (c1's queues fit in L2: no figure.)
-    dram_per_seg = {("c2", 2): 62.5, ("c3", 2): 125.7, ("c3", 0): 57.4}.get((args.config, variant))
-    if dram_per_seg is not None:
-        traffic = dram_per_seg * segs_c / max(1, st["traverse_launches"])
-    elif (args.config, variant) == ("c3", 3):
-        traffic = (43.4 * paths_c + 59.0 * (segs_c - paths_c)) / max(1, st["traverse_launches"])
-        dram_per_seg = traffic * max(1, st["traverse_launches"]) / max(1, segs_c)
-    else:
-        traffic = None
+    sm_mhz = (clk or {}).get("sm_max_mhz") or 2070.0
+    fp32_peak = venu.sm_count() * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fp32_tflops = kflops / (stp["traverse_ms"] / 1000.0) / 1e12
+    simd = sc["lane_steps"] / max(1, 32 * sc["warp_steps"])
+    sha = kernel_sources_sha()
+    fig = NCU_FIGURES["figures"].get(f"{name}/v{variant}") if NCU_FIGURES["sha"] == sha else None
+    traffic = dram_frac = None
+    if fig is not None:
+        traffic = fig["dram_b_per_seg"] * segs_c / nl
+        dram_frac = traffic / avg_launch_s / 1e9 / peak
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
         "peak_kind": peak_kind, "traffic": traffic, "kernel": kernel,
-        "traffic_per_segment": dram_per_seg,
+        "frac_kind": "algorithmic bytes (32 B per box test, 16 B per sphere test, queue traffic) per launch / "
+                     "event time; the node set is served from L1/L2, so this is not DRAM throughput",
         "bytes_per_segment": kbytes / max(1, segs_c),
         "nodes_per_segment": nodes / max(1, segs_c), "spheres_per_segment": sph / max(1, segs_c),
-        "kernel_share": st["traverse_ms"] / max(1e-9, ms / args.steps),
-        "note": "achieved = algorithmic bytes (nodes, spheres, queues) per launch / event time; the node set "
-                "is L1/L2-resident, so DRAM carries only the ray queues (traffic, from ncu) and the kernel "
-                "is issue-bound on the ALU pipe (profiles/)",
-        "fp32_tflops": kflops / (st["traverse_ms"] / 1000.0) / 1e12, "fp32_peak_tflops": fp32_peak,
+        "simd_utilization": simd,
+        "simd_utilization_kind": "traversal steps summed over lanes / (32 x steps issued per warp), counting "
+                                 "build of the same render (live)",
+        "dram_bytes_per_segment": fig["dram_b_per_seg"] if fig else None,
+        "dram_frac": dram_frac,
+        "lanes_per_inst_ncu": fig["lanes_per_inst"] if fig else None,
+        "ncu_kernel_sources_sha": NCU_FIGURES["sha"], "kernel_sources_sha": sha,
+        "ncu_note": None if fig else ("no ncu figures for these kernel sources and this variant: traffic, "
+                                      "dram_frac and lanes_per_inst_ncu are null"),
+        "kernel_share": stp["traverse_ms"] / max(1e-9, ms / steps),
+        "fp32_tflops": fp32_tflops, "fp32_peak_tflops": fp32_peak, "fp32_frac": fp32_tflops / fp32_peak,
     }
+    block = {
+        "workload": cfg["workload"], "value": value, "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+        "warmup": warmup, "segments_per_step": segs_step, "paths_per_step": st["paths"],
+        "spheres": int(len(spheres)), "width": W, "height": H, "spp": spp, "max_depth": depth,
+        "tuning": dict(wf.tuning(), max_paths=max_paths), "autotune_candidates": len(tune_log),
+        "lbvh": {"build_ms": ds.info()["build_ms"], "device_bytes": ds.info()["device_bytes"]},
+        "gpu_launches": st["kernel_launches"] * steps,
+        "roofline": roofline,
+    }
+    state = dict(wf=wf, ds=ds, spheres=spheres, cam=cam, accum=accum, img8=img8, tuning=tuning,
+                 max_paths=max_paths, segs_step=segs_step, total_segs=total_segs, clocks=clk, stream=stream)
+    return block, state
 
-    # --- end-to-end through the C ABI from host memory ----------------------
+
+def measure_e2e(venu, torch, rep, cfg, state, steps):
+    """The headline metric through the C ABI from pinned host memory: scene
+    upload + LBVH build + render + image download every step."""
     import ctypes as C
 
     from venusaur_gb300._lib import RenderOpts, check, lib, ptr
 
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    spheres, cam, accum, img8 = state["spheres"], state["cam"], state["accum"], state["img8"]
     host_sph = torch.from_numpy(spheres.view(np.uint8)).pin_memory()
     host_img = torch.empty((H * W, 4), dtype=torch.uint8).pin_memory()
-    wf_plain = venu.Wavefront(max_paths)
-    if tuning:
-        wf_plain.set_tuning(**tuning)
+    wf_plain = venu.Wavefront(state["max_paths"])
+    if state["tuning"]:
+        wf_plain.set_tuning(**state["tuning"])
     cam_np = np.ascontiguousarray(cam)
-    h = C.c_void_p(stream.cuda_stream)
+    h = C.c_void_p(state["stream"].cuda_stream)
 
     def e2e_step(i):
         sc_h = C.c_void_p()
@@ -709,45 +704,131 @@ def main():
         lib().venu_scene_destroy(sc_h)
 
     e2e_step(0)
-    barrier()
+    rep.barrier()
     t0 = time.perf_counter()
-    for i in range(args.steps):
+    for i in range(steps):
         e2e_step(i + 1)
     t1 = time.perf_counter()
     e2e_s = rep.max(t1 - t0)
-    e2e = {"value": total_segs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(spheres.nbytes),
-           "d2h_bytes_per_step": int(H * W * 4), "ms_per_step": 1000 * e2e_s / args.steps}
     wf_plain.close()
+    return {"value": state["total_segs"] / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(spheres.nbytes),
+            "d2h_bytes_per_step": int(H * W * 4), "ms_per_step": 1000 * e2e_s / steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="venu", choices=["venu", "reference"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--max-paths", type=int, default=0)
+    ap.add_argument("--spp", type=int, default=0, help="override the config's samples per pixel (small profiling cases)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--tuning", default="", help="JSON launch shapes to use instead of the autotuner's")
+    ap.add_argument("--profile-mixed", type=int, default=0, metavar="STEPS",
+                    help="only run STEPS loop steps of the first 12 jobs of the mixed workload (~4 GB on the "
+                         "device) through the batch engine's host-driven loop (ncu cannot profile kernels "
+                         "inside conditional graphs) and exit")
+    ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
+    ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' blocks")
+    args = ap.parse_args()
+    cfg = dict(CONFIGS[args.config])
+    if args.spp:
+        cfg["spp"] = args.spp
+        cfg["workload"] = cfg["workload"].replace(f"{CONFIGS[args.config]['spp']} spp", f"{args.spp} spp")
+    if args.impl == "reference":
+        run_reference(args, cfg)
+        return
+    from venusaur_gb300.replicas import Replicas
+
+    rep = Replicas()
+    world, rank, local = rep.world, rep.rank, rep.local
+
+    import torch
+
+    torch.cuda.set_device(local)
+    import venusaur_gb300 as venu
+    from venusaur_gb300 import build as vb
+
+    vb.build()
+    if args.profile_mixed:
+        profile_mixed(venu, torch, args)
+        return
+    # CPU baseline first, on an idle host (rank 0, single process only): the
+    # reference's arithmetic on the fixed sample of this configuration, every
+    # host thread; the GB300-arithmetic port on the same sample beside it.
+    cpu_baseline = cpu_gb300 = None
+    O = None
+    if not args.no_cpu and world == 1:
+        from oracle import pyoracle
+
+        pyoracle.build()
+        O = pyoracle.Oracle()
+        nt = os.cpu_count() or 1
+        o_sph, o_cam = oracle_scene(O, cfg)
+        cpu_run(O, o_sph, o_cam, CONFIGS["c1"], "c1", pyoracle.MODE_REF_BVH, nt)  # thread start-up, page-in
+        rate, dt, segs, sample = cpu_run(O, o_sph, o_cam, cfg, args.config, pyoracle.MODE_REF_BVH, nt, repeats=3)
+        cpu_baseline = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "arithmetic": "reference",
+                        "sample": sample + " (3 runs)", "seconds": dt, "what": REF_ARITH}
+        rate, dt, segs, sample = cpu_run(O, o_sph, o_cam, cfg, args.config, pyoracle.MODE_GB300, nt)
+        cpu_gb300 = {"value": rate, "unit": UNIT, "cores": nt, "kind": "port", "arithmetic": "gb300",
+                     "sample": sample, "seconds": dt,
+                     "what": "the oracle's restatement of this library's own arithmetic over the same LBVH"}
+
+    steps, warmup = args.steps, args.warmup
+    block, state = measure_plain(venu, torch, rep, args.config, cfg, args, steps, warmup, headline=True)
+    e2e = measure_e2e(venu, torch, rep, cfg, state, steps)
+    others = {}
+    if not args.no_configs and world == 1:
+        for name in ("c1", "c2", "c3"):
+            if name == args.config:
+                continue
+            if name == "c2" and args.config != "c2":
+                continue  # the headline's own config only as headline
+            b, st2 = measure_plain(venu, torch, rep, name, dict(CONFIGS[name]), args, min(steps, 5), 3,
+                                   headline=False)
+            st2["wf"].close()
+            others[name] = b
+            del st2
+            torch.cuda.empty_cache()
 
     if rank != 0:
         return
+    W, H = cfg["W"], cfg["H"]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": block["value"], "unit": UNIT, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": block["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded RTIOW scene generator)",
-        "config": {"workload": cfg["workload"], "width": W, "height": H, "spp": spp, "max_depth": depth,
-                   "spheres": int(len(spheres)), "method": "plain single-scene wavefront",
+        "config": {"workload": cfg["workload"], "width": W, "height": H, "spp": cfg["spp"],
+                   "max_depth": cfg["depth"], "spheres": block["spheres"], "method": "plain single-scene wavefront",
                    "l2": "working set (ray queues > 1.5 GB) larger than L2; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU",
-                   "segments_per_step": segs_step, "paths_per_step": st["paths"],
-                   "tuning": dict(wf.tuning(), max_paths=max_paths),
-                   "autotune_candidates": len(tune_log),
-                   "lbvh": {"build_ms": ds.info()["build_ms"], "device_bytes": ds.info()["device_bytes"]}},
-        "gpu_launches": launches,
-        "clocks": clk,
+                   "segments_per_step": block["segments_per_step"], "paths_per_step": block["paths_per_step"],
+                   "tuning": block["tuning"], "autotune_candidates": block["autotune_candidates"],
+                   "lbvh": block["lbvh"]},
+        "gpu_launches": block["gpu_launches"],
+        "clocks": state["clocks"],
         "e2e": e2e,
-        "roofline": roofline,
+        "roofline": block["roofline"],
     }
+    if others:
+        line["configs"] = others
     if not args.no_batched and world == 1:
-        line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, spp, depth, segs_step,
-                                                    args.warmup + args.steps, max_paths)
+        ds, cam, tuning = state["ds"], state["cam"], state["tuning"]
+        line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, cfg["spp"], cfg["depth"],
+                                                    state["segs_step"], warmup + steps, state["max_paths"])
         retune = not (args.tuning or args.no_autotune)
-        line["batched"] = run_batched(venu, torch, tuning, max_paths, autotune=retune)
-        line["batched_small_jobs"] = run_batched(venu, torch, tuning, max_paths, small=True, autotune=retune)
+        line["batched"] = run_batched(venu, torch, tuning, state["max_paths"], autotune=retune)
+        line["batched_small_jobs"] = run_batched(venu, torch, tuning, state["max_paths"], small=True,
+                                                 autotune=retune)
         line["served"] = run_served(venu, torch, tuning)
     if cpu_baseline is not None:
         line["cpu_baseline"] = cpu_baseline
-        line["rmse_vs_reference"] = rmse_vs_reference(venu, torch, O, ds, spheres, cam, W, H, depth)
+        line["cpu_port_gb300"] = cpu_gb300
+        line["rmse_vs_reference"] = rmse_vs_reference(venu, torch, O, state["ds"], state["spheres"], state["cam"],
+                                                      W, H, cfg["depth"])
     print(json.dumps(line), flush=True)
 
 

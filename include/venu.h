@@ -117,6 +117,9 @@ typedef struct venu_render_stats {
     float shade_ms;          /*   summed CUDA-event times of each kernel's launches */
     uint32_t traverse_launches;
     uint32_t shade_launches;
+    uint64_t lane_steps;     /* counting renders only: traversal steps summed over lanes, */
+    uint64_t warp_steps;     /*   and over warps (one per step the warp issues); */
+                             /*   lane_steps / (32 warp_steps) = SIMD utilisation of traversal */
 } venu_render_stats;
 
 /* ---- errors / device -------------------------------------------------- */
@@ -207,8 +210,22 @@ VENU_API venu_status venu_scene_destroy(venu_scene* scene);
  * it keeps the last call's contents: calls whose work overlaps on the GPU
  * (other streams, other host threads) race and must be serialised.
  *
+ * The device address of that array is looked up once per device ordinal and
+ * kept for the life of the process; it belongs to the CUDA context current at
+ * that first call, so this entry point must not be used after that device's
+ * context is destroyed (cudaDeviceReset) in the same process.
+ *
  * Outputs (device, 16-byte aligned where float4):
- *   nodes_out      (n-1) x 8 floats: {lo.xyz, left} {hi.xyz, right} (n > 1)
+ *   nodes_out      (n-1) x 8 floats: {lo.xyz, left} {hi.xyz, right} (n > 1;
+ *                  may be NULL for n = 1).  Child words as
+ *                  venu_scene_export_bvh writes them: >= 0 an internal node,
+ *                  0x80000000 | slot a leaf, and 0x40000000 also set on the
+ *                  leaf of a hoisted sphere (one of at most four huge spheres,
+ *                  radius above a quarter of the largest centroid extent).  A
+ *                  traversal of these nodes must test the hoisted spheres
+ *                  before the walk and skip their leaves in it, as this
+ *                  library's does; their slots are the leaf words that carry
+ *                  0x40000000
  *   spheres_out    n x 4 floats {center, radius} in Morton slot order
  *   materials_out  n x 4 floats {albedo, fuzz or ir}
  *   meta_out       n uint32: original index | material << 30
@@ -218,6 +235,23 @@ VENU_API venu_status venu_scene_destroy(venu_scene* scene);
 VENU_API venu_status venu_lbvh_build_noalloc(const venu_sphere* spheres_dev, uint32_t n, float* nodes_out,
                                              float* spheres_out, float* materials_out, uint32_t* meta_out,
                                              uint32_t* morton_out, void* stream);
+
+/* ---- device self-tests ------------------------------------------------
+ * The device arithmetic that results depend on bit for bit, exposed so a
+ * caller can compare it word for word with a host restatement.  All pointers
+ * are device memory; asynchronous on `stream`. */
+/* tea_out[i] = tea<4>(a[i], b[i]) for i < n (Core/random.cuh:31-46); then
+ * nsteps steps of the LCG from `seed` (Core/random.cuh:49-67): rnd_out[k] the
+ * k-th draw, states_out[k] the state after it (either may be NULL). */
+VENU_API venu_status venu_selftest_rng(const uint32_t* a_dev, const uint32_t* b_dev, uint32_t n,
+                                       uint32_t* tea_out_dev, uint32_t seed, uint32_t nsteps,
+                                       float* rnd_out_dev, uint32_t* states_out_dev, void* stream);
+/* out[i] = x[i]^(1/2.4) for i < n: which = 0 the library's own power routine,
+ * used by every sRGB encode (Core/RayTracer.cu:16-47 calls powf; this one
+ * is built from IEEE operations only, so a host restatement matches it bit
+ * for bit; x in [2^-126, 1]); which = 1 CUDA's powf(x, 1.0f/2.4f). */
+VENU_API venu_status venu_selftest_srgb_pow(const float* x_dev, uint64_t n, uint32_t which, float* out_dev,
+                                            void* stream);
 
 /* ---- closest hit for arbitrary rays (optixTrace without programs) ----- */
 /* rays_dev: n x 6 floats (origin, direction).  Writes, per ray, the hit

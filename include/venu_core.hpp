@@ -3,9 +3,10 @@
 // in venu.h.  Header-only; link libvenusaur_gb300.so and the CUDA runtime.
 //
 // It replaces Core/material.h, Core/sphere.h, Core/Scene.h, Core/camera.h,
-// Core/CUDAOutputBuffer.h (CUDA_DEVICE mode) and Core/Renderer.h so that a
-// main loop written against the reference (Init / Draw / Cleanup) compiles
-// unchanged apart from the includes; glm is replaced by a small vec3.
+// Core/CUDAOutputBuffer.h (the CUDA_DEVICE and ZERO_COPY buffer types) and
+// Core/Renderer.h so that a main loop written against the reference
+// (Init / Draw / Cleanup) compiles unchanged apart from the includes; glm is
+// replaced by a small vec3.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,6 +26,10 @@ struct vec3 {
     vec3() = default;
     vec3(float a, float b, float c) : x(a), y(b), z(c) {}
 };
+// the glm::vec3 operations the reference's main loop uses (lookat - lookfrom)
+inline vec3 operator+(const vec3& a, const vec3& b) { return vec3(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline vec3 operator-(const vec3& a, const vec3& b) { return vec3(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline vec3 operator*(const vec3& a, float s) { return vec3(a.x * s, a.y * s, a.z * s); }
 
 class Exception : public std::runtime_error {
    public:
@@ -209,42 +214,104 @@ class Camera {
     bool m_changed = true;
 };
 
-// Core/CUDAOutputBuffer.h, CUDA_DEVICE mode: device RGBA8 pixels (+ RGBA32F).
+// Core/CUDAOutputBuffer.h:56-61
+enum class CUDAOutputBufferType {
+    CUDA_DEVICE = 0,  // device memory (supported)
+    GL_INTEROP = 1,   // an OpenGL pixel buffer: no display here, rejected
+    ZERO_COPY = 2,    // mapped pinned host memory the kernels write to (supported)
+    CUDA_P2P = 3      // device memory shared with a GL display: rejected
+};
+
+// Core/CUDAOutputBuffer.h:64-106,108-382 (template, constructor, map / unmap,
+// getHostPointer) for the headless buffer types.  The GL types need the
+// display path, which this library replaces by writePPM / writePFM: their
+// construction throws.  Besides the reference's PIXEL_FORMAT pixels the
+// buffer holds the RGBA32F running mean that venu_render writes (floatPixels,
+// writePFM).
+template <typename PIXEL_FORMAT>
 class CUDAOutputBuffer {
    public:
-    CUDAOutputBuffer(int32_t width, int32_t height) { resize(width, height); }
+    CUDAOutputBuffer(CUDAOutputBufferType type, int32_t width, int32_t height) : m_type(type) {
+        if (type == CUDAOutputBufferType::GL_INTEROP || type == CUDAOutputBufferType::CUDA_P2P)
+            throw Exception(VENU_ERR_INVALID, "CUDAOutputBuffer: GL_INTEROP and CUDA_P2P need an OpenGL display");
+        resize(width, height);
+    }
     ~CUDAOutputBuffer() { release(); }
     CUDAOutputBuffer(const CUDAOutputBuffer&) = delete;
     CUDAOutputBuffer& operator=(const CUDAOutputBuffer&) = delete;
-    void resize(int32_t w, int32_t h) {
-        release();
-        m_width = w < 1 ? 1 : w;
-        m_height = h < 1 ? 1 : h;
-        cuda_check(cudaMalloc(&m_pixels, 4u * m_width * m_height), "CUDAOutputBuffer");
-        cuda_check(cudaMalloc(&m_pixels_f, 16u * m_width * m_height), "CUDAOutputBuffer");
-    }
+
+    void setDevice(int32_t device_idx) { m_device_idx = device_idx; }
     void setStream(cudaStream_t s) { m_stream = s; }
-    uint8_t* map() { return m_pixels; }
-    void unmap() { cuda_check(cudaStreamSynchronize(m_stream), "unmap"); }
+
+    // Core/CUDAOutputBuffer.h:173-234; sizes below 1 become 1 (ensureMinimumSize)
+    void resize(int32_t width, int32_t height) {
+        width = width < 1 ? 1 : width;
+        height = height < 1 ? 1 : height;
+        if (m_pixels && width == m_width && height == m_height) return;
+        release();
+        m_width = width;
+        m_height = height;
+        makeCurrent();
+        const size_t n = (size_t)m_width * m_height;
+        if (m_type == CUDAOutputBufferType::CUDA_DEVICE) {
+            cuda_check(cudaMalloc(reinterpret_cast<void**>(&m_pixels), sizeof(PIXEL_FORMAT) * n), "CUDAOutputBuffer");
+        } else {
+            cuda_check(cudaHostAlloc(reinterpret_cast<void**>(&m_host_zcopy_pixels), sizeof(PIXEL_FORMAT) * n,
+                                     cudaHostAllocPortable | cudaHostAllocMapped),
+                       "CUDAOutputBuffer");
+            cuda_check(cudaHostGetDevicePointer(reinterpret_cast<void**>(&m_pixels), m_host_zcopy_pixels, 0),
+                       "CUDAOutputBuffer");
+        }
+        cuda_check(cudaMalloc(&m_pixels_f, 16u * n), "CUDAOutputBuffer");
+    }
+
+    // Device address of the pixels for the kernels (Core/CUDAOutputBuffer.h:236-262).
+    PIXEL_FORMAT* map() { return m_pixels; }
+    // Waits for the stream (Core/CUDAOutputBuffer.h:264-282).
+    void unmap() {
+        makeCurrent();
+        cuda_check(cudaStreamSynchronize(m_stream), "unmap");
+    }
+
     int32_t width() const { return m_width; }
     int32_t height() const { return m_height; }
-    float* floatPixels() { return m_pixels_f; }
-    std::vector<uint8_t> getHostPointer() {
-        std::vector<uint8_t> h(4u * m_width * m_height);
-        cuda_check(cudaMemcpy(h.data(), m_pixels, h.size(), cudaMemcpyDeviceToHost), "getHostPointer");
-        return h;
+
+    // Core/CUDAOutputBuffer.h:284-339: the GL pixel buffer of the display.
+    unsigned int getPBO() {
+        throw Exception(VENU_ERR_INVALID, "CUDAOutputBuffer::getPBO: no OpenGL display (use writePPM)");
     }
+    void deletePBO() {}
+
+    // Core/CUDAOutputBuffer.h:348-382: a host copy of the pixels.
+    PIXEL_FORMAT* getHostPointer() {
+        if (m_type == CUDAOutputBufferType::ZERO_COPY) {
+            unmap();
+            return m_host_zcopy_pixels;
+        }
+        m_host_pixels.resize((size_t)m_width * m_height);
+        makeCurrent();
+        cuda_check(cudaMemcpy(m_host_pixels.data(), m_pixels, sizeof(PIXEL_FORMAT) * m_host_pixels.size(),
+                              cudaMemcpyDeviceToHost),
+                   "getHostPointer");
+        return m_host_pixels.data();
+    }
+
     cudaStream_t stream() const { return m_stream; }
+    float* floatPixels() { return m_pixels_f; }
     std::vector<float> getHostFloat() {
         std::vector<float> h(4u * m_width * m_height);
+        makeCurrent();
         cuda_check(cudaMemcpy(h.data(), m_pixels_f, h.size() * sizeof(float), cudaMemcpyDeviceToHost),
                    "getHostFloat");
         return h;
     }
     // Headless stand-ins for the GL display (Core/CUDAOutputBuffer.h:284-339).
     void writePPM(const char* path) {
-        std::vector<uint8_t> h = getHostPointer();
-        check(venu_image_write_ppm(path, h.data(), (uint32_t)m_width, (uint32_t)m_height), "writePPM");
+        static_assert(sizeof(PIXEL_FORMAT) == 4, "writePPM needs 4-byte RGBA8 pixels");
+        const PIXEL_FORMAT* h = getHostPointer();
+        check(venu_image_write_ppm(path, reinterpret_cast<const uint8_t*>(h), (uint32_t)m_width,
+                                   (uint32_t)m_height),
+              "writePPM");
     }
     void writePFM(const char* path) {
         std::vector<float> h = getHostFloat();
@@ -252,16 +319,23 @@ class CUDAOutputBuffer {
     }
 
    private:
+    void makeCurrent() { cuda_check(cudaSetDevice(m_device_idx), "cudaSetDevice"); }
     void release() {
-        if (m_pixels) cudaFree(m_pixels);
+        if (m_type == CUDAOutputBufferType::CUDA_DEVICE && m_pixels) cudaFree(m_pixels);
+        if (m_host_zcopy_pixels) cudaFreeHost(m_host_zcopy_pixels);
         if (m_pixels_f) cudaFree(m_pixels_f);
         m_pixels = nullptr;
+        m_host_zcopy_pixels = nullptr;
         m_pixels_f = nullptr;
     }
+    CUDAOutputBufferType m_type;
     int32_t m_width = 0, m_height = 0;
-    uint8_t* m_pixels = nullptr;
+    PIXEL_FORMAT* m_pixels = nullptr;            // device address (mapped, for ZERO_COPY)
+    PIXEL_FORMAT* m_host_zcopy_pixels = nullptr;  // ZERO_COPY host memory
+    std::vector<PIXEL_FORMAT> m_host_pixels;
     float* m_pixels_f = nullptr;
     cudaStream_t m_stream = nullptr;
+    int32_t m_device_idx = 0;
 };
 
 // Core/Renderer.h:22-97 over venu_scene / venu_render.
@@ -283,7 +357,9 @@ class Renderer {
         check(venu_scene_update(m_scene, recs.data(), (uint32_t)recs.size(), nullptr), "venu_scene_update");
         m_scene_changed = true;
     }
-    void Draw(Camera& camera, CUDAOutputBuffer& out) {
+    // Core/Renderer.h:35-78: one progressive subframe of samples_per_pixel
+    // samples (16, the reference's fixed count, by default).
+    void Draw(Camera& camera, CUDAOutputBuffer<uchar4>& out) {
         const uint64_t npix = (uint64_t)out.width() * out.height();
         uint32_t flags = 0;
         const bool scene_changed = m_scene_changed;
@@ -298,7 +374,8 @@ class Renderer {
         ++m_subframe;
         venu_camera cam = camera.frame();
         venu_render_opts o{(uint32_t)out.width(), (uint32_t)out.height(), m_spp, m_subframe, m_max_depth, flags};
-        check(venu_render(m_renderer, m_scene, &cam, &o, m_accum, out.floatPixels(), out.map(), out.stream()),
+        check(venu_render(m_renderer, m_scene, &cam, &o, m_accum, out.floatPixels(),
+                          reinterpret_cast<uint8_t*>(out.map()), out.stream()),
               "venu_render");
         out.unmap();
     }

@@ -33,6 +33,7 @@ NODE_DTYPE = np.dtype([("lo", "<f4", (3,)), ("left", "<i4"), ("hi", "<f4", (3,))
 
 MODE_REF = 0
 MODE_GB300 = 1
+MODE_REF_BVH = 2  # the reference's arithmetic, closest hit through the host LBVH
 
 
 class _Opts(C.Structure):
@@ -42,13 +43,13 @@ class _Opts(C.Structure):
 
 
 def build(ref_root: str | None = None, with_ref: bool = False) -> None:
-    """Compile the oracle (and, if asked and present, the reference build)."""
+    """Compile the oracle and, if asked, the reference build (from ref_root,
+    else the recipe's own REF_ROOT; skipped where no checkout is there)."""
     cmd = ["make", "-s", "-C", HERE, "all"]
     subprocess.run(cmd, check=True)
     if with_ref:
-        root = ref_root or "/root/reference"
-        if os.path.isdir(os.path.join(root, "Core")):
-            subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={root}"], check=True)
+        extra = [f"REF_ROOT={ref_root}"] if ref_root else []
+        subprocess.run(["make", "-s", "-C", HERE, "ref"] + extra, check=True)
 
 
 def _p(a, t=C.c_void_p):
@@ -148,6 +149,14 @@ class Oracle:
                             _p(nv), _p(ns))
         return idv, t, front, nv, ns
 
+    def trace_stack_depth(self, spheres, rays, tmin=0.001, tmax=1e16):
+        """Per ray, the deepest traversal stack of the GB300 LBVH walk."""
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(len(rays), np.uint32)
+        self.L.vo_trace_bvh_stack(_p(spheres), C.c_uint32(len(spheres)), _p(rays), C.c_uint32(len(rays)),
+                                  C.c_float(tmin), C.c_float(tmax), _p(out))
+        return out
+
     def trace_ref(self, spheres, rays, tmin=0.001, tmax=1e16):
         rays = np.ascontiguousarray(rays, np.float32)
         n = len(rays)
@@ -184,6 +193,19 @@ class Oracle:
                                       _p(accum), _p(image_f), _p(image8), _p(samples), _p(nv), _p(ns))
         return dict(accum=accum, image_f=image_f, image8=image8, segments=int(segs),
                     samples=samples, nodes=int(nv[0]), spheres=int(ns[0]))
+
+    def srgb_pow(self, x) -> np.ndarray:
+        """x^(1/2.4) by the GB300 arithmetic's power routine (x in [2^-126, 1])."""
+        x = np.ascontiguousarray(x, np.float32).reshape(-1)
+        out = np.empty_like(x)
+        self.L.vo_srgb_pow(_p(x), C.c_uint64(len(x)), _p(out))
+        return out
+
+    def make_color_gb300(self, rgb) -> np.ndarray:
+        rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+        out = np.zeros((len(rgb), 4), np.uint8)
+        self.L.vo_make_color_gb300(_p(rgb), C.c_uint32(len(rgb)), _p(out))
+        return out
 
     def make_color(self, rgb) -> np.ndarray:
         rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)

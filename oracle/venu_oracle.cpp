@@ -711,16 +711,92 @@ struct Hit {
 
 const int32_t kNone = 0x7fffffff;
 
-// GB300 traversal: test-children-at-parent, near child first, far child's
-// child pair pushed with its entry distance; popped entries culled against
-// the current closest hit.  Ties on t go to the smaller sorted slot.
+// The LBVH walk shared by both arithmetic modes: test-children-at-parent,
+// near child first, far child's child pair pushed with its entry distance;
+// popped entries culled against the current closest hit (best_t, which the
+// leaf callback lowers).  Hoisted huge spheres are tested first.
+// Deepest traversal stack of the walks on this thread since it was last reset
+// (the kernels keep the top entries of the same stack in shared memory).
+thread_local int tl_max_stack = 0;
+
+template <class Leaf>
+void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, uint64_t* nv, Leaf leaf) {
+    for (int32_t k : B.hoist) leaf(k);  // huge spheres first (the ground)
+    if (B.n == 1) {
+        leaf(0);
+        return;
+    }
+    float tn;
+    if (nv) ++*nv;
+    if (!box_test(R, B.nodes[0], tmin, best_t, tn)) return;
+    struct Ent { int32_t l, r; float tn; };
+    Ent stack[128];
+    int sp = 0;
+    int32_t pl = B.nodes[0].left, pr = B.nodes[0].right;
+    for (;;) {
+        bool h0 = false, h1 = false;
+        float tn0 = 0, tn1 = 0;
+        int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
+        if (pl & kLeaf) {
+            if (!(pl & kHoisted)) leaf(pl & kSlotMask);
+        } else {
+            const vo_node& nd = B.nodes[pl];
+            if (nv) ++*nv;
+            h0 = box_test(R, nd, tmin, best_t, tn0);
+            c0l = nd.left;
+            c0r = nd.right;
+        }
+        if (pr & kLeaf) {
+            if (!(pr & kHoisted)) leaf(pr & kSlotMask);
+        } else {
+            const vo_node& nd = B.nodes[pr];
+            if (nv) ++*nv;
+            h1 = box_test(R, nd, tmin, best_t, tn1);
+            c1l = nd.left;
+            c1r = nd.right;
+        }
+        if (h0 && h1) {
+            if (tn1 < tn0) {
+                stack[sp++] = Ent{c0l, c0r, tn0};
+                pl = c1l;
+                pr = c1r;
+            } else {
+                stack[sp++] = Ent{c1l, c1r, tn1};
+                pl = c0l;
+                pr = c0r;
+            }
+            if (sp > tl_max_stack) tl_max_stack = sp;
+        } else if (h0) {
+            pl = c0l;
+            pr = c0r;
+        } else if (h1) {
+            pl = c1l;
+            pr = c1r;
+        } else {
+            bool found = false;
+            while (sp > 0) {
+                --sp;
+                if (stack[sp].tn <= best_t) {
+                    pl = stack[sp].l;
+                    pr = stack[sp].r;
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) return;
+        }
+    }
+}
+
+// GB300 closest hit: the LBVH walk with the GB300 sphere test.  Ties on t go
+// to the smaller sorted slot.
 Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, uint64_t* ns) {
     Hit h{-1, tmax};
     if (B.n == 0) return h;
     RayPre R = prep(o, d);
     float best_t = tmax;
     int32_t best = kNone;
-    auto leaf = [&](int k) {
+    walk_bvh(B, R, tmin, best_t, nv, [&](int k) {
         float t;
         if (ns) ++*ns;
         if (sphere_gb300(R, B.center[k], B.radius[k], tmin, tmax, t) &&
@@ -728,72 +804,7 @@ Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, 
             best_t = t;
             best = k;
         }
-    };
-    for (int32_t k : B.hoist) leaf(k);  // huge spheres first (the ground)
-    if (B.n == 1) {
-        leaf(0);
-    } else {
-        float tn;
-        if (nv) ++*nv;
-        if (box_test(R, B.nodes[0], tmin, best_t, tn)) {
-            struct Ent { int32_t l, r; float tn; };
-            Ent stack[128];
-            int sp = 0;
-            int32_t pl = B.nodes[0].left, pr = B.nodes[0].right;
-            for (;;) {
-                bool h0 = false, h1 = false;
-                float tn0 = 0, tn1 = 0;
-                int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
-                if (pl & kLeaf) {
-                    if (!(pl & kHoisted)) leaf(pl & kSlotMask);
-                } else {
-                    const vo_node& nd = B.nodes[pl];
-                    if (nv) ++*nv;
-                    h0 = box_test(R, nd, tmin, best_t, tn0);
-                    c0l = nd.left;
-                    c0r = nd.right;
-                }
-                if (pr & kLeaf) {
-                    if (!(pr & kHoisted)) leaf(pr & kSlotMask);
-                } else {
-                    const vo_node& nd = B.nodes[pr];
-                    if (nv) ++*nv;
-                    h1 = box_test(R, nd, tmin, best_t, tn1);
-                    c1l = nd.left;
-                    c1r = nd.right;
-                }
-                if (h0 && h1) {
-                    if (tn1 < tn0) {
-                        stack[sp++] = Ent{c0l, c0r, tn0};
-                        pl = c1l;
-                        pr = c1r;
-                    } else {
-                        stack[sp++] = Ent{c1l, c1r, tn1};
-                        pl = c0l;
-                        pr = c0r;
-                    }
-                } else if (h0) {
-                    pl = c0l;
-                    pr = c0r;
-                } else if (h1) {
-                    pl = c1l;
-                    pr = c1r;
-                } else {
-                    bool found = false;
-                    while (sp > 0) {
-                        --sp;
-                        if (stack[sp].tn <= best_t) {
-                            pl = stack[sp].l;
-                            pr = stack[sp].r;
-                            found = true;
-                            break;
-                        }
-                    }
-                    if (!found) break;
-                }
-            }
-        }
-    }
+    });
     if (best != kNone) {
         h.k = best;
         h.t = best_t;
@@ -834,6 +845,35 @@ Hit trace_ref(const vo_sphere* s, uint32_t ns, f3 o, f3 d, float tmin, float tma
                 cur = root;
             }
         }
+    }
+    return h;
+}
+
+// REF-mode closest hit through the LBVH: the reference's intersection
+// program (sphere_ref, Core/RayTracer.cu:229-270) on the spheres the walk
+// reaches, in place of OptiX's hardware traversal.  The accepted hit is the
+// brute force's: the smallest root, exact ties to the smaller original index
+// (the sphere a brute-force loop in index order keeps).  Returns the
+// original index.
+Hit trace_ref_bvh(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, uint64_t* ns) {
+    Hit h{-1, tmax};
+    if (B.n == 0) return h;
+    RayPre R = prep(o, d);
+    float best_t = tmax;
+    int32_t best = -1;
+    walk_bvh(B, R, tmin, best_t, nv, [&](int k) {
+        float root;
+        if (ns) ++*ns;
+        const int32_t id = (int32_t)B.ids[k];
+        if (sphere_ref(o, d, B.center[k], B.radius[k], tmin, best_t, root) &&
+            (best < 0 || root < best_t || (root == best_t && id < best))) {
+            best_t = root;
+            best = id;
+        }
+    });
+    if (best >= 0) {
+        h.k = best;
+        h.t = best_t;
     }
     return h;
 }
@@ -897,6 +937,7 @@ inline float reflectance_gb300(float cosine, float ref_idx) {
 struct Scene {
     const vo_sphere* s;
     uint32_t n;
+    bool ref_bvh = false;  // REF mode: closest hit through the LBVH, not brute force
     Bvh bvh;
     std::vector<vo_sphere> sorted;  // materials in BVH slot order
 };
@@ -912,7 +953,8 @@ f3 path_ref(const Scene& S, f3 o, f3 d, uint32_t seed, int depth, Counters& K) {
     int nchain = 0;
     f3 att;
     for (;;) {
-        Hit h = trace_ref(S.s, S.n, o, d, 0.001f, 1e16f);
+        Hit h = S.ref_bvh ? trace_ref_bvh(S.bvh, o, d, 0.001f, 1e16f, &K.nv, &K.ns)
+                          : trace_ref(S.s, S.n, o, d, 0.001f, 1e16f);
         ++K.segs;
         if (h.k < 0) {
             att = sky_ref(d);
@@ -1025,16 +1067,67 @@ f3 path_gb300(const Scene& S, f3 o, f3 d, uint32_t seed, int depth, Counters& K)
     }
 }
 
+// x^(1/2.4) for x in [2^-126, 1]: the sRGB encode's power in the GB300
+// arithmetic, restating the CUDA kernel's routine operation by operation
+// (IEEE +, -, *, / and fma only, so host and device round identically).
+// x = m 2^e with m in [sqrt(1/2), sqrt(2)); log2 m = s (c1 + c3 s^2 + ...),
+// s = (m-1)/(m+1), the atanh series of ln m = 2 atanh s scaled by 1/ln 2;
+// t = y (e + log2 m) with y e split exactly (TwoProduct); 2^t = 2^n 2^f,
+// n = rint(t), 2^f by its Taylor series to f^7.
+inline float srgb_pow(float x) {
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    int e = (int)(b >> 23) - 127;
+    const uint32_t mb = (b & 0x007fffffu) | 0x3f800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 1.41421353816986083984375f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float tail = std::fma(z, 0.32059890031814575f, 0.41219857335090637f);
+    tail = std::fma(z, tail, 0.5770780444145203f);
+    tail = std::fma(z, tail, 0.9617967009544373f);
+    tail = std::fma(z, tail, 3.8519259e-08f);
+    const float L = std::fma(s, 2.885390043258667f, s * tail);
+    const float y = 0.4166666567325592f;
+    const float fe = (float)e;
+    const float ph = fe * y;
+    const float pl = std::fma(fe, y, -ph);
+    const float q = std::fma(y, L, pl);
+    const float n = std::rint(ph + q);
+    const float f = (ph - n) + q;
+    float p = std::fma(f, 1.5252733646775596e-05f, 1.540352968731895e-04f);
+    p = std::fma(f, p, 1.3333557872101665e-03f);
+    p = std::fma(f, p, 9.618128649890423e-03f);
+    p = std::fma(f, p, 5.550410971045494e-02f);
+    p = std::fma(f, p, 2.4022650718688965e-01f);
+    p = std::fma(f, p, 6.931471824645996e-01f);
+    p = std::fma(f, p, 1.0f);
+    const uint32_t sb = (uint32_t)(127 + (int)n) << 23;
+    float scale;
+    std::memcpy(&scale, &sb, 4);
+    return p * scale;
+}
+
 // Core/RayTracer.cu:16-47
 inline uint8_t quant8(float x) {
     x = clampf(x, 0.0f, 1.0f);
     uint32_t q = (uint32_t)(x * 256.0f);
     return (uint8_t)(q < 255u ? q : 255u);
 }
-inline void make_color(f3 c, uint8_t* out) {
+// ref = false: the GB300 arithmetic's own power routine in place of pow().
+inline void make_color(f3 c, uint8_t* out, bool ref = true) {
     c = mk(clampf(c.x, 0.0f, 1.0f), clampf(c.y, 0.0f, 1.0f), clampf(c.z, 0.0f, 1.0f));
     float inv_gamma = 1.0f / 2.4f;
     float p[3] = {std::pow(c.x, inv_gamma), std::pow(c.y, inv_gamma), std::pow(c.z, inv_gamma)};
+    if (!ref) {
+        p[0] = c.x < 0.0031308f ? 0.0f : srgb_pow(c.x);
+        p[1] = c.y < 0.0031308f ? 0.0f : srgb_pow(c.y);
+        p[2] = c.z < 0.0031308f ? 0.0f : srgb_pow(c.z);
+    }
     float v[3] = {c.x, c.y, c.z};
     for (int i = 0; i < 3; ++i) {
         float srgb = v[i] < 0.0031308f ? 12.92f * v[i] : 1.055f * p[i] - 0.055f;
@@ -1215,6 +1308,18 @@ void vo_trace_bvh(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n
     }
 }
 
+void vo_trace_bvh_stack(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n, float tmin, float tmax,
+                        uint32_t* max_stack) {
+    Bvh B;
+    build_bvh(s, ns, B);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* r = rays + 6 * (size_t)i;
+        tl_max_stack = 0;
+        trace_gb300(B, mk(r[0], r[1], r[2]), mk(r[3], r[4], r[5]), tmin, tmax, nullptr, nullptr);
+        max_stack[i] = (uint32_t)tl_max_stack;
+    }
+}
+
 void vo_trace_ref(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n, float tmin,
                   float tmax, int32_t* id, float* t) {
     for (uint32_t i = 0; i < n; ++i) {
@@ -1239,9 +1344,12 @@ uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t 
     S.s = s;
     S.n = ns;
     const bool gb = opts->mode == VO_MODE_GB300;
-    if (gb) {
+    S.ref_bvh = opts->mode == VO_MODE_REF_BVH;
+    if (gb || S.ref_bvh) {
         build_bvh(s_build ? s_build : s, ns, S.bvh);
         if (s_build) update_bvh(S.bvh, s);
+    }
+    if (gb) {
         S.sorted.resize(ns);
         for (uint32_t k = 0; k < ns; ++k) S.sorted[k] = s[S.bvh.ids[k]];
     }
@@ -1290,7 +1398,7 @@ uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t 
                         float* f = image_f + 4 * (size_t)idx;
                         f[0] = mean.x; f[1] = mean.y; f[2] = mean.z; f[3] = 1.0f;
                     }
-                    if (image8) make_color(mean, image8 + 4 * (size_t)idx);
+                    if (image8) make_color(mean, image8 + 4 * (size_t)idx, false);
                 } else {
                     f3 pc = mk(0, 0, 0);
                     for (uint32_t smp = 0; smp < spp; ++smp) {
@@ -1336,6 +1444,15 @@ uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t 
 
 void vo_make_color(const float* rgb, uint32_t n, uint8_t* out4) {
     for (uint32_t i = 0; i < n; ++i) make_color(mk(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]), out4 + 4 * i);
+}
+
+void vo_make_color_gb300(const float* rgb, uint32_t n, uint8_t* out4) {
+    for (uint32_t i = 0; i < n; ++i)
+        make_color(mk(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]), out4 + 4 * i, false);
+}
+
+void vo_srgb_pow(const float* x, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) out[i] = srgb_pow(x[i]);
 }
 
 }  // extern "C"

@@ -14,6 +14,12 @@
  *                  pow() in Schlick, plain half-b quadratic, spp-sum then
  *                  multiply by 1/spp, lerp across subframes, max depth 4
  *                  unless overridden, brute-force closest hit.
+ *   VO_MODE_REF_BVH  VO_MODE_REF with the closest hit found through the host
+ *                  LBVH instead of by brute force (the reference's
+ *                  intersection program on the spheres the walk reaches;
+ *                  the same hit as the brute force: smallest root, exact
+ *                  ties to the smaller index).  The reference's arithmetic
+ *                  at the cost of an accelerated CPU tracer.
  *   VO_MODE_GB300  the arithmetic the CUDA kernels implement (stable
  *                  quadratic with exact c, FP32 dielectric, pow5 as a product,
  *                  forward throughput, Kahan accumulation, LBVH traversal).
@@ -57,7 +63,7 @@ typedef struct vo_node {
     int32_t right;
 } vo_node;
 
-enum { VO_MODE_REF = 0, VO_MODE_GB300 = 1 };
+enum { VO_MODE_REF = 0, VO_MODE_GB300 = 1, VO_MODE_REF_BVH = 2 };
 
 typedef struct vo_render_opts {
     uint32_t width, height;
@@ -104,6 +110,9 @@ void vo_trace_fp64(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t 
 void vo_trace_bvh(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n,
                   float tmin, float tmax, int32_t* id, float* t, uint32_t* front,
                   uint32_t* nodes_visited, uint32_t* spheres_tested);
+/* Per ray, the deepest traversal stack of vo_trace_bvh's walk (entries). */
+void vo_trace_bvh_stack(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n, float tmin, float tmax,
+                        uint32_t* max_stack);
 /* REF-mode FP32 brute force (reference quadratic, OptiX-like strict tmax). */
 void vo_trace_ref(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n,
                   float tmin, float tmax, int32_t* id, float* t);
@@ -111,7 +120,7 @@ void vo_trace_ref(const vo_sphere* s, uint32_t ns, const float* rays, uint32_t n
 /* --- render ---
  * GB300 mode: accum is 8 floats per pixel {sum.rgb, n, comp.rgb, 0} (the
  *   device layout), updated in place; image_f gets {mean.rgb, 1}.
- * REF mode: accum is 4 floats per pixel {mean.rgb, 1} (Params::accum).
+ * REF / REF_BVH modes: accum is 4 floats per pixel {mean.rgb, 1} (Params::accum).
  * image8 gets sRGB RGBA8 in both modes (may be NULL).
  * samples_out (may be NULL): per (s, pixel) final path radiance, 3 floats,
  *   layout [s][pixel][3] for the rendered rows.
@@ -127,8 +136,12 @@ uint64_t vo_render_refit(const vo_sphere* s_build, const vo_sphere* s, uint32_t 
                          float* image_f, uint8_t* image8, float* samples_out,
                          uint64_t* nodes_visited, uint64_t* spheres_tested);
 
-/* sRGB encode of linear RGB (Core/RayTracer.cu:16-47). */
+/* sRGB encode of linear RGB (Core/RayTracer.cu:16-47) with pow() (REF) and
+ * with the GB300 arithmetic's own power routine (the kernels' bytes). */
 void vo_make_color(const float* rgb, uint32_t n, uint8_t* out4);
+void vo_make_color_gb300(const float* rgb, uint32_t n, uint8_t* out4);
+/* x^(1/2.4) by the GB300 power routine, for x in [2^-126, 1]. */
+void vo_srgb_pow(const float* x, uint64_t n, float* out);
 
 #ifdef __cplusplus
 }

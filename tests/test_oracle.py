@@ -49,6 +49,31 @@ def test_ref_mode_matches_reference_golden(oracle, g):
     assert np.array_equal(r3["accum"].view(np.uint32), g["ref_s3_accum"].view(np.uint32))
 
 
+def test_ref_bvh_mode_matches_reference_golden(oracle, g):
+    """The reference's arithmetic with the closest hit found through the host
+    LBVH (the timed CPU baseline) equals the brute force, and so the
+    reference's own RayTracer.cu built for the host, bit for bit."""
+    spheres, cam, W, H, SPP = _scene_cam(g)
+    r = oracle.render(spheres, cam, W, H, SPP, subframe=0, max_depth=4, mode=pyoracle.MODE_REF_BVH)
+    assert np.array_equal(r["accum"].view(np.uint32), g["ref_s0_accum"].view(np.uint32))
+    r3 = oracle.render(spheres, cam, W, H, 2, subframe=3, max_depth=4, mode=pyoracle.MODE_REF_BVH,
+                       accum=g["ref_s3_prior"].copy())
+    assert np.array_equal(r3["accum"].view(np.uint32), g["ref_s3_accum"].view(np.uint32))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3000])
+def test_ref_bvh_mode_matches_brute_force(oracle, n):
+    sp = oracle.scene_random(n, 7)
+    W, H = 48, 27
+    cam = oracle.camera((60, 15, 60), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    a = oracle.render(sp, cam, W, H, 3, subframe=1, max_depth=50, mode=pyoracle.MODE_REF)
+    b = oracle.render(sp, cam, W, H, 3, subframe=1, max_depth=50, mode=pyoracle.MODE_REF_BVH)
+    assert a["segments"] == b["segments"]
+    assert np.array_equal(a["accum"].view(np.uint32), b["accum"].view(np.uint32))
+    if n > 2:
+        assert b["spheres"] < a["segments"] * n // 10  # the LBVH prunes
+
+
 def test_gb300_mode_golden(oracle, g):
     spheres, cam, W, H, SPP = _scene_cam(g)
     for depth in (4, 50):
@@ -263,3 +288,36 @@ def test_invariant_division_magic():
                  [int(v) for v in rng.integers(0, 1 << 31, 8)]:
             if 0 <= x <= top:
                 assert (x * m) >> (31 + l) == x // d, (x, d)
+
+
+def srgb_pow_inputs(stride=1):
+    """Every float in [0.0031308, 1] (the sRGB power's inputs), every
+    `stride`-th one."""
+    lo = int(np.float32(0.0031308).view(np.uint32))
+    hi = int(np.float32(1.0).view(np.uint32))
+    return np.arange(lo, hi + 1, stride, dtype=np.uint32).view(np.float32)
+
+
+def test_srgb_pow_accuracy(oracle):
+    """The GB300 arithmetic's x^(1/2.4) (oracle restatement of the kernels'
+    routine) against double-precision pow on every input of the sRGB branch:
+    within 1.2 ulp of the exact value."""
+    x = srgb_pow_inputs()
+    y = np.float64(np.float32(1.0) / np.float32(2.4))
+    worst = 0.0
+    for k in range(0, len(x), 1 << 23):
+        xs = x[k:k + (1 << 23)]
+        got = oracle.srgb_pow(xs).astype(np.float64)
+        ref = np.power(xs.astype(np.float64), y)
+        worst = max(worst, float((np.abs(got - ref) / np.spacing(ref.astype(np.float32))).max()))
+    assert worst <= 1.2, worst
+    assert oracle.srgb_pow(np.array([1.0], np.float32))[0] == 1.0
+
+
+def test_srgb_bytes_gb300_vs_pow(oracle):
+    """The GB300 encode differs from the pow() encode only where the value
+    sits on a byte boundary: at most 1 apart, and rarely."""
+    rgb = np.random.default_rng(3).random((200_000, 3)).astype(np.float32)
+    a = oracle.make_color(rgb).astype(int)
+    b = oracle.make_color_gb300(rgb).astype(int)
+    assert np.abs(a - b).max() <= 1 and (a != b).mean() < 1e-3

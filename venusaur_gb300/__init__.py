@@ -17,12 +17,13 @@ from .core import (  # noqa: F401
     generate_random,
     generate_rtiow,
     new_accum,
+    sm_count,
     write_pfm,
     write_ppm,
 )
 
 __all__ = [
     "Batch", "Camera", "CUDAOutputBuffer", "DeviceScene", "Material", "Renderer", "Scene", "Server", "Sphere",
-    "Wavefront", "VenuError", "generate_random", "generate_rtiow", "new_accum", "write_pfm", "write_ppm", "lib",
+    "Wavefront", "VenuError", "generate_random", "generate_rtiow", "new_accum", "sm_count", "write_pfm", "write_ppm", "lib",
     "SPHERE_DTYPE", "CAMERA_DTYPE", "NODE_DTYPE",
 ]

@@ -55,7 +55,8 @@ class RenderStats(C.Structure):
     _fields_ = [("segments", C.c_uint64), ("paths", C.c_uint64), ("waves", C.c_uint32),
                 ("kernel_launches", C.c_uint32), ("nodes_visited", C.c_uint64),
                 ("spheres_tested", C.c_uint64), ("traverse_ms", C.c_float), ("shade_ms", C.c_float),
-                ("traverse_launches", C.c_uint32), ("shade_launches", C.c_uint32)]
+                ("traverse_launches", C.c_uint32), ("shade_launches", C.c_uint32),
+                ("lane_steps", C.c_uint64), ("warp_steps", C.c_uint64)]
 
 
 class Tuning(C.Structure):
@@ -177,7 +178,9 @@ def lib() -> C.CDLL:
     L.venu_server_end_session.argtypes = [vp, C.c_uint64]
     L.venu_renderer_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.venu_renderer_get_tuning.argtypes = [vp, C.POINTER(Tuning)]
-    for name in ("venu_device_check", "venu_scene_generate_random", "venu_scene_create",
+    L.venu_selftest_rng.argtypes = [vp, vp, u32, vp, u32, u32, vp, vp, vp]
+    L.venu_selftest_srgb_pow.argtypes = [vp, C.c_uint64, u32, vp, vp]
+    for name in ("venu_selftest_rng", "venu_selftest_srgb_pow","venu_device_check", "venu_scene_generate_random", "venu_scene_create",
                  "venu_scene_create_device", "venu_scene_update", "venu_scene_update_device",
                  "venu_scene_info_get", "venu_scene_export_bvh",
                  "venu_scene_destroy", "venu_trace", "venu_renderer_create", "venu_render",

@@ -117,6 +117,13 @@ def array_to_spheres(a: np.ndarray):
     return out
 
 
+def sm_count() -> int:
+    """Streaming multiprocessors of the current device (venu_device_check)."""
+    n, major, minor = C.c_int(0), C.c_int(0), C.c_int(0)
+    check(lib().venu_device_check(C.byref(n), C.byref(major), C.byref(minor)))
+    return int(n.value)
+
+
 def generate_rtiow(seed: int = 0) -> np.ndarray:
     buf = np.zeros(600, SPHERE_DTYPE)
     n = lib().venu_scene_generate_rtiow(seed, ptr(buf), len(buf))
@@ -379,7 +386,7 @@ class Wavefront:
         return dict(segments=s.segments, paths=s.paths, waves=s.waves, kernel_launches=s.kernel_launches,
                     nodes_visited=s.nodes_visited, spheres_tested=s.spheres_tested,
                     traverse_ms=s.traverse_ms, shade_ms=s.shade_ms, traverse_launches=s.traverse_launches,
-                    shade_launches=s.shade_launches)
+                    shade_launches=s.shade_launches, lane_steps=s.lane_steps, warp_steps=s.warp_steps)
 
     def close(self) -> None:
         if getattr(self, "handle", None):

@@ -79,17 +79,7 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
         }
     }
     if (overflow) atomicOr(err, 1u);
-    if (COUNT) {
-        unsigned long long a = K.nodes, b = K.spheres;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, off);
-            b += __shfl_xor_sync(0xffffffffu, b, off);
-        }
-        if (lane == 0) {
-            atomicAdd(stats + 1, a);
-            atomicAdd(stats + 2, b);
-        }
-    }
+    if (COUNT) flush_counters(K, stats);
 }
 
 // Persistent lanes: a lane whose ray is finished takes a new one as soon as
@@ -160,17 +150,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
         }
     }
     if (overflow) atomicOr(err, 1u);
-    if (COUNT) {
-        unsigned long long a = K.nodes, b = K.spheres;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, off);
-            b += __shfl_xor_sync(0xffffffffu, b, off);
-        }
-        if (lane == 0) {
-            atomicAdd(stats + 1, a);
-            atomicAdd(stats + 2, b);
-        }
-    }
+    if (COUNT) flush_counters(K, stats);
 }
 
 // One warp-batch loop of the fused kernel.  IN_PLACE (a launch with no more
@@ -266,17 +246,7 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
         trace_shade_loop<COUNT, false, KS>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
     }
     if (overflow) atomicOr(err, 1u);
-    if (COUNT) {
-        unsigned long long a = K.nodes, b = K.spheres;
-        for (int off = 16; off > 0; off >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, off);
-            b += __shfl_xor_sync(0xffffffffu, b, off);
-        }
-        if (lane == 0) {
-            atomicAdd(stats + 1, a);
-            atomicAdd(stats + 2, b);
-        }
-    }
+    if (COUNT) flush_counters(K, stats);
 }
 
 __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
@@ -530,9 +500,9 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     cudaError_t e = cudaMalloc(&r->cnt, sizeof(uint32_t) * (kMaxDepth + 1));
     if (e == cudaSuccess) e = cudaMalloc(&r->work, sizeof(uint32_t) * (kMaxDepth + 1));
     if (e == cudaSuccess) e = cudaMalloc(&r->err, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 6);
     if (e == cudaSuccess) e = cudaMemset(r->err, 0, sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMemset(r->stats, 0, sizeof(unsigned long long) * 4);
+    if (e == cudaSuccess) e = cudaMemset(r->stats, 0, sizeof(unsigned long long) * 6);
     if (e == cudaSuccess) e = configure(r);
     if (e != cudaSuccess) {
         free_renderer(r);
@@ -613,7 +583,7 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     }
     if (opts->flags & VENU_FLAG_RESET_ACCUM)
         VENU_CUDA(cudaMemsetAsync(accum_dev, 0, sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL * npix64, st));
-    VENU_CUDA(cudaMemsetAsync(r->stats, 0, sizeof(unsigned long long) * 4, st));
+    VENU_CUDA(cudaMemsetAsync(r->stats, 0, sizeof(unsigned long long) * 6, st));
     const SceneView S = view_of(scene);
     const bool count = (r->flags & VENU_RENDERER_COUNT) != 0;
     const bool prof = (r->flags & VENU_RENDERER_PROFILE) != 0;
@@ -757,13 +727,15 @@ extern "C" venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* 
         set_error("venu_renderer_stats: NULL argument");
         return VENU_ERR_INVALID;
     }
-    unsigned long long st[4] = {0, 0, 0, 0};
+    unsigned long long st[6] = {0, 0, 0, 0, 0, 0};
     uint32_t err = 0;
     VENU_CUDA(cudaMemcpy(st, r->stats, sizeof(st), cudaMemcpyDeviceToHost));
     VENU_CUDA(cudaMemcpy(&err, r->err, sizeof(err), cudaMemcpyDeviceToHost));
     r->last.segments = st[0];
     r->last.nodes_visited = st[1];
     r->last.spheres_tested = st[2];
+    r->last.lane_steps = st[3];
+    r->last.warp_steps = st[4];
     // event pairs alternate traverse, shade (4 events per bounce)
     float tms = 0.0f, sms = 0.0f;
     uint32_t tn = 0, sn = 0;

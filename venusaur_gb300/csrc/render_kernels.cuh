@@ -163,7 +163,8 @@ __device__ __forceinline__ void kahan_add(float4& a0, float4& a1, float4 v) {
     a0.w = a0.w + 1.0f;
 }
 
-// Core/RayTracer.cu:16-47: clamp, sRGB (powf with 1/2.4), x*256 truncated.
+// Core/RayTracer.cu:16-47: clamp, sRGB (x^(1/2.4) by srgb_pow in place of
+// powf), x*256 truncated.
 __device__ __forceinline__ unsigned char quant8(float x) {
     x = fmaxf(0.0f, fminf(x, 1.0f));
     uint32_t q = (uint32_t)(x * 256.0f);
@@ -171,12 +172,10 @@ __device__ __forceinline__ unsigned char quant8(float x) {
 }
 __device__ __forceinline__ uchar4 make_color(f3 c) {
     float v[3] = {fmaxf(0.0f, fminf(c.x, 1.0f)), fmaxf(0.0f, fminf(c.y, 1.0f)), fmaxf(0.0f, fminf(c.z, 1.0f))};
-    const float inv_gamma = 1.0f / 2.4f;
     unsigned char q[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        float p = powf(v[i], inv_gamma);
-        float srgb = v[i] < 0.0031308f ? 12.92f * v[i] : 1.055f * p - 0.055f;
+        float srgb = v[i] < 0.0031308f ? 12.92f * v[i] : 1.055f * srgb_pow(v[i]) - 0.055f;
         q[i] = quant8(srgb);
     }
     return make_uchar4(q[0], q[1], q[2], 255);

@@ -153,6 +153,48 @@ __device__ __forceinline__ float reflectance(float cosine, float ref_idx) {
     return r0 + (1.0f - r0) * x5;
 }
 
+// x^(1/2.4) for x in [2^-126, 1], the power of the sRGB encode
+// (Core/RayTracer.cu:16-47 calls powf), from IEEE +, -, *, / and fmaf only,
+// so that the host restatement rounds identically and image bytes can be
+// checked exactly.  x = m 2^e with m in [sqrt(1/2), sqrt(2));
+// log2 m = s (c1 + c3 s^2 + c5 s^4 + c7 s^6 + c9 s^8), s = (m-1)/(m+1): the
+// atanh series of ln m = 2 atanh(s) scaled by 1/ln 2 (c_k = 2/(k ln 2), c1
+// as a head and a tail); t = y (e + log2 m) with the product y e split
+// exactly (TwoProduct); 2^t = 2^n 2^f with n = rint(t) and 2^f by its Taylor
+// series to f^7 (coefficients ln(2)^k / k!).  Error at most 1.16 ulp over
+// every float in [0.0031308, 1] (measured against double pow).
+__device__ __forceinline__ float srgb_pow(float x) {
+    const uint32_t b = __float_as_uint(x);
+    int e = (int)(b >> 23) - 127;
+    float m = __uint_as_float((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421353816986083984375f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float tail = fmaf(z, 0.32059890031814575f, 0.41219857335090637f);
+    tail = fmaf(z, tail, 0.5770780444145203f);
+    tail = fmaf(z, tail, 0.9617967009544373f);
+    tail = fmaf(z, tail, 3.8519259e-08f);
+    const float L = fmaf(s, 2.885390043258667f, s * tail);
+    const float y = 0.4166666567325592f;  // 1.0f / 2.4f, the reference's exponent
+    const float fe = (float)e;
+    const float ph = fe * y;
+    const float pl = fmaf(fe, y, -ph);
+    const float q = fmaf(y, L, pl);
+    const float n = rintf(ph + q);
+    const float f = (ph - n) + q;
+    float p = fmaf(f, 1.5252733646775596e-05f, 1.540352968731895e-04f);
+    p = fmaf(f, p, 1.3333557872101665e-03f);
+    p = fmaf(f, p, 9.618128649890423e-03f);
+    p = fmaf(f, p, 5.550410971045494e-02f);
+    p = fmaf(f, p, 2.4022650718688965e-01f);
+    p = fmaf(f, p, 6.931471824645996e-01f);
+    p = fmaf(f, p, 1.0f);
+    return p * __uint_as_float((uint32_t)(127 + (int)n) << 23);
+}
+
 // ---------------------------------------------------------------------------
 // Scene view: LBVH nodes + spheres/materials in Morton (slot) order.
 // ---------------------------------------------------------------------------
@@ -383,9 +425,31 @@ struct StackSmem {
     float* tn;   // [kShared][block]
 };
 
+// Counting builds only.  lane_steps / warp_steps: traversal steps summed over
+// lanes, and over warps (one per step instruction the warp issues, with
+// however many lanes are converged on it): their ratio / 32 is the SIMD
+// utilisation of the traversal loop.
 struct TraceCounters {
-    uint32_t nodes, spheres;
+    uint32_t nodes, spheres, lane_steps, warp_steps;
 };
+
+// Adds a warp's counters to stats[1..4] (nodes, spheres, lane steps, warp
+// steps); every lane of the warp calls it.
+__device__ __forceinline__ void flush_counters(const TraceCounters& K, unsigned long long* stats) {
+    unsigned long long a = K.nodes, b = K.spheres, c = K.lane_steps, d = K.warp_steps;
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, off);
+        b += __shfl_xor_sync(0xffffffffu, b, off);
+        c += __shfl_xor_sync(0xffffffffu, c, off);
+        d += __shfl_xor_sync(0xffffffffu, d, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(stats + 1, a);
+        atomicAdd(stats + 2, b);
+        atomicAdd(stats + 3, c);
+        atomicAdd(stats + 4, d);
+    }
+}
 
 // Per-lane traversal state.  begin() prepares a ray and tests the root;
 // step() tests both children of the current node (from its 64-byte record in
@@ -450,6 +514,11 @@ struct Tracer {
         if (--guard == 0u) {
             overflow = true;
             return false;
+        }
+        if (COUNT) {
+            ++K.lane_steps;
+            const uint32_t am = __activemask();
+            if ((tid & 31u) == (uint32_t)(__ffs(am) - 1)) ++K.warp_steps;
         }
         const float4* T = S.trav + 4 * (size_t)cur;
         const float4 a0 = __ldg(T), b0 = __ldg(T + 1), a1 = __ldg(T + 2), b1 = __ldg(T + 3);
