@@ -104,6 +104,8 @@ typedef struct venu_scene_info {
     uint64_t device_bytes;   /* resident bytes owned by the scene */
     float bounds[6];         /* centroid bounds used for Morton quantisation */
     float build_ms;          /* device time of the last LBVH build */
+    uint32_t num_wide_nodes; /* nodes of the 8-wide traversal tree collapsed from the LBVH */
+    float wide_ms;           /* wall time of that collapse (host-driven, level by level) */
 } venu_scene_info;
 
 typedef struct venu_render_stats {
@@ -288,8 +290,11 @@ typedef struct venu_tuning {
                                         1: idle lanes take new rays;
                                         2: as 0, then the warp shades its 32 hits in the same
                                            kernel (no separate shade launch; default);
-                                        3: 2 for the primary rays, 0 for later bounces */
-    uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
+                                        3: 2 for the primary rays, 0 for later bounces;
+                                        4: as 2, over the 8-wide tree collapsed from the
+                                           LBVH (8 child boxes tested per step);
+                                        5: 2 for the primary rays, then 1 over the 8-wide tree */
+    uint32_t refill_min;             /* variants 1, 5: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
     uint32_t shade_block;            /* threads per shade block: 64..512, multiple of 32 */

@@ -276,6 +276,10 @@ def test_empty_and_tiny_scenes(venu, oracle, cuda):
     dict(traverse_variant=2, refill_min=8, traverse_block=256, shade_block=256, traverse_blocks_per_sm=1),
     dict(traverse_variant=3, refill_min=8, traverse_block=128, shade_block=256),
     dict(traverse_variant=3, refill_min=32, traverse_block=256, shade_block=128, traverse_blocks_per_sm=2),
+    dict(traverse_variant=4, refill_min=32, traverse_block=128, shade_block=256),
+    dict(traverse_variant=4, refill_min=32, traverse_block=64, shade_block=256, traverse_blocks_per_sm=3),
+    dict(traverse_variant=5, refill_min=8, traverse_block=128, shade_block=256),
+    dict(traverse_variant=5, refill_min=1, traverse_block=256, shade_block=128, traverse_blocks_per_sm=2),
 ])
 def test_render_tunings_bit_exact(venu, oracle, cuda, tuning):
     """Launch shapes and traversal variants change speed, never bits."""
@@ -358,7 +362,7 @@ DEEP = [(4000, 12, 0.5, 4), (6000, 10, 0.7, 8)]
 
 
 @pytest.mark.parametrize("n,levels,rfrac,ks", DEEP)
-@pytest.mark.parametrize("variant", [2, 3])
+@pytest.mark.parametrize("variant", [2, 3, 4, 5])
 def test_deep_stack_spills_bit_exact(venu, oracle, cuda, n, levels, rfrac, ks, variant):
     """Scenes whose rays need more stack entries than the shared-memory ring
     holds: the spill to local memory and back keeps every result bit-exact,

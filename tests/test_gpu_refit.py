@@ -22,8 +22,10 @@ def _moved(spheres, seed, scale=1.0, radius=True, material=False):
     return out
 
 
-def _render(venu, torch, ds, cam, W, H, spp, subframe, depth):
+def _render(venu, torch, ds, cam, W, H, spp, subframe, depth, variant=None):
     wf = venu.Wavefront(0, count=True)
+    if variant is not None:
+        wf.set_tuning(traverse_variant=variant)
     acc = venu.new_accum(W, H)
     wf.render(ds, cam, W, H, spp, acc, subframe=subframe, max_depth=depth, reset=True)
     torch.cuda.synchronize()
@@ -57,6 +59,10 @@ def test_refit_nodes_and_render(venu, oracle, cuda, case):
     assert st["nodes_visited"] == want["nodes"] and st["spheres_tested"] == want["spheres"]
     fresh = oracle.render(mv, cam, W, H, spp, subframe=2, max_depth=depth)
     assert np.array_equal(acc.view(np.uint32), fresh["accum"].view(np.uint32))
+    # the 8-wide tree is refit with the binary one
+    acc4, st4 = _render(venu, torch, ds, cam, W, H, spp, 2, depth, variant=4)
+    assert np.array_equal(acc4.view(np.uint32), want["accum"].view(np.uint32))
+    assert st4["segments"] == want["segments"]
 
 
 def test_refit_round_trip_and_limits(venu, oracle, cuda):

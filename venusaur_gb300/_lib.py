@@ -48,7 +48,8 @@ class RenderOpts(C.Structure):
 
 class SceneInfo(C.Structure):
     _fields_ = [("num_spheres", C.c_uint32), ("num_nodes", C.c_uint32), ("device_bytes", C.c_uint64),
-                ("bounds", C.c_float * 6), ("build_ms", C.c_float)]
+                ("bounds", C.c_float * 6), ("build_ms", C.c_float), ("num_wide_nodes", C.c_uint32),
+                ("wide_ms", C.c_float)]
 
 
 class RenderStats(C.Structure):

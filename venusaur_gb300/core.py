@@ -314,7 +314,8 @@ class DeviceScene:
         si = SceneInfo()
         check(lib().venu_scene_info_get(self.handle, C.byref(si)))
         return dict(num_spheres=si.num_spheres, num_nodes=si.num_nodes, device_bytes=si.device_bytes,
-                    bounds=np.array(si.bounds[:], np.float32), build_ms=si.build_ms)
+                    bounds=np.array(si.bounds[:], np.float32), build_ms=si.build_ms,
+                    num_wide_nodes=si.num_wide_nodes, wide_ms=si.wide_ms)
 
     def export_bvh(self) -> dict:
         n = self.info()["num_spheres"]

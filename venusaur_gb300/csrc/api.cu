@@ -448,6 +448,8 @@ extern "C" venu_status venu_scene_info_get(const venu_scene* s, venu_scene_info*
     out->device_bytes = s->bytes;
     std::memcpy(out->bounds, s->bounds, sizeof(out->bounds));
     out->build_ms = s->build_ms;
+    out->num_wide_nodes = s->nwide;
+    out->wide_ms = s->wide_ms;
     return VENU_OK;
 }
 

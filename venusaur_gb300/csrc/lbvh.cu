@@ -16,6 +16,7 @@
 #include "venu_internal.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -565,6 +566,166 @@ __global__ void k_trav_layout(const float4* __restrict__ nodes, const float4* __
     trav[4 * (size_t)p + 2 * c + 1] = b;
 }
 
+// ---------------------------------------------------------------------------
+// The 8-wide traversal tree (renderer variant 4), collapsed from the binary
+// LBVH after its build.  A wide node stands for a binary node r and holds up
+// to 8 of r's descendants: starting from r's two children, the internal entry
+// of largest box surface area (the first such entry on ties) is replaced by
+// its two children until there are 8 entries or only leaves.  Internal
+// entries become wide nodes themselves.  The wide nodes are numbered in
+// increasing order of the binary nodes they stand for (root first), so the
+// tree is deterministic.  Results do not depend on it: the closest hit is the
+// same for any conservative traversal (minimum t, ties to the smaller slot).
+//
+// Node layout (16 float4 = 256 bytes, two cache lines):
+//   [0..11]  child boxes, structure of arrays in two halves of four children:
+//            lo.x c0-3, lo.x c4-7, hi.x c0-3, hi.x c4-7, then y, then z
+//   [12..13] child words c0-3, c4-7: an internal child's wide index, or a
+//            leaf's 0x80000000 | slot (an unused entry or a hoisted leaf:
+//            0x80000000 | 0x40000000, never tested)
+//   [14]     {valid mask | leaf mask << 8 (int bits), 0, 0, 0}
+//   [15]     unused
+// wide_src[8 w + c] keeps the binary word of child c (internal node index or
+// leaf word), so a refit of moved spheres can recompute the boxes in place.
+// ---------------------------------------------------------------------------
+constexpr int kWideChildren = 8;
+
+__device__ __forceinline__ float box_area(float4 lo, float4 hi) {
+    const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+    return dx * dy + dy * dz + dz * dx;
+}
+
+__device__ int wide_collapse(const float4* __restrict__ nodes, int32_t r, int32_t w[kWideChildren]) {
+    w[0] = __float_as_int(nodes[2 * r].w);
+    w[1] = __float_as_int(nodes[2 * r + 1].w);
+    int cnt = 2;
+    while (cnt < kWideChildren) {
+        int best = -1;
+        float best_a = -1.0f;
+        for (int i = 0; i < cnt; ++i) {
+            if (w[i] & kLeaf) continue;
+            const float a = box_area(nodes[2 * w[i]], nodes[2 * w[i] + 1]);
+            if (a > best_a) {
+                best_a = a;
+                best = i;
+            }
+        }
+        if (best < 0) break;
+        const int32_t q = w[best];
+        w[best] = __float_as_int(nodes[2 * q].w);
+        w[cnt++] = __float_as_int(nodes[2 * q + 1].w);
+    }
+    return cnt;
+}
+
+// One level of the collapse: every binary node of the frontier expands;
+// its internal entries are flagged as wide nodes and form the next frontier.
+__global__ void k_wide_frontier(const float4* __restrict__ nodes, const int32_t* __restrict__ fin, uint32_t nin,
+                                int32_t* __restrict__ fout, uint32_t* __restrict__ nout, uint32_t* __restrict__ flag) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nin) return;
+    int32_t w[kWideChildren];
+    const int c = wide_collapse(nodes, fin[i], w);
+    for (int j = 0; j < c; ++j) {
+        if (w[j] & kLeaf) continue;
+        flag[w[j]] = 1u;
+        fout[atomicAdd(nout, 1u)] = w[j];
+    }
+}
+
+// Box of a leaf: the sphere's box rounded outwards (as k_refit makes it).
+__device__ __forceinline__ void leaf_box(float4 s4, float4& lo, float4& hi) {
+    const float r = fabsf(s4.w);
+    lo = make_float4(__fsub_rd(s4.x, r) + 0.0f, __fsub_rd(s4.y, r) + 0.0f, __fsub_rd(s4.z, r) + 0.0f, 0.0f);
+    hi = make_float4(__fadd_ru(s4.x, r), __fadd_ru(s4.y, r), __fadd_ru(s4.z, r), 0.0f);
+}
+
+// Writes wide node w from the binary words of its children (src[0..7];
+// kLeaf | kHoisted for an unused entry).  idx maps a binary internal node to
+// its wide index.
+__device__ void wide_write_node(const float4* __restrict__ nodes, const float4* __restrict__ sph,
+                                const uint32_t* __restrict__ idx, const int32_t* src, float4* __restrict__ W) {
+    float lo[3][kWideChildren], hi[3][kWideChildren];
+    int32_t word[kWideChildren];
+    uint32_t valid = 0, leafm = 0;
+    for (int c = 0; c < kWideChildren; ++c) {
+        const int32_t b = src[c];
+        float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f), h = l;
+        if (b & kLeaf) {
+            word[c] = b;
+            if (!(b & kHoisted)) {
+                leaf_box(sph[b & kSlotMask], l, h);
+                valid |= 1u << c;
+                leafm |= 1u << c;
+            }
+        } else {
+            l = nodes[2 * b];
+            h = nodes[2 * b + 1];
+            word[c] = (int32_t)idx[b];
+            valid |= 1u << c;
+        }
+        lo[0][c] = l.x; lo[1][c] = l.y; lo[2][c] = l.z;
+        hi[0][c] = h.x; hi[1][c] = h.y; hi[2][c] = h.z;
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int half = 0; half < 2; ++half) {
+            const int c = 4 * half;
+            W[4 * a + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
+            W[4 * a + 2 + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
+        }
+    }
+    W[12] = make_float4(__int_as_float(word[0]), __int_as_float(word[1]), __int_as_float(word[2]),
+                        __int_as_float(word[3]));
+    W[13] = make_float4(__int_as_float(word[4]), __int_as_float(word[5]), __int_as_float(word[6]),
+                        __int_as_float(word[7]));
+    W[14] = make_float4(__int_as_float((int)(valid | (leafm << 8))), 0.0f, 0.0f, 0.0f);
+    W[15] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// One thread per binary internal node; the flagged ones write their wide node.
+__global__ void k_wide_write(const float4* __restrict__ nodes, const float4* __restrict__ sph, uint32_t n,
+                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx,
+                             float4* __restrict__ wide, int32_t* __restrict__ wide_src) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n - 1 || !flag[r]) return;
+    int32_t w[kWideChildren];
+    const int c = wide_collapse(nodes, (int32_t)r, w);
+    for (int j = c; j < kWideChildren; ++j) w[j] = kLeaf | kHoisted;
+    const uint32_t k = idx[r];
+    for (int j = 0; j < kWideChildren; ++j) wide_src[(size_t)kWideChildren * k + j] = w[j];
+    wide_write_node(nodes, sph, idx, w, wide + 16 * (size_t)k);
+}
+
+// Refit of moved spheres: the same topology, boxes recomputed from the
+// refit binary nodes and the new spheres.  idx is not needed: the child
+// words of internal children stay as they are.
+__global__ void k_wide_refit(const float4* __restrict__ nodes, const float4* __restrict__ sph, uint32_t nwide,
+                             const int32_t* __restrict__ wide_src, float4* __restrict__ wide) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nwide) return;
+    float4* W = wide + 16 * (size_t)k;
+    float lo[3][kWideChildren], hi[3][kWideChildren];
+    for (int c = 0; c < kWideChildren; ++c) {
+        const int32_t b = wide_src[(size_t)kWideChildren * k + c];
+        float4 l = make_float4(0.0f, 0.0f, 0.0f, 0.0f), h = l;
+        if (b & kLeaf) {
+            if (!(b & kHoisted)) leaf_box(sph[b & kSlotMask], l, h);
+        } else {
+            l = nodes[2 * b];
+            h = nodes[2 * b + 1];
+        }
+        lo[0][c] = l.x; lo[1][c] = l.y; lo[2][c] = l.z;
+        hi[0][c] = h.x; hi[1][c] = h.y; hi[2][c] = h.z;
+    }
+    for (int a = 0; a < 3; ++a) {
+        for (int half = 0; half < 2; ++half) {
+            const int c = 4 * half;
+            W[4 * a + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
+            W[4 * a + 2 + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
+        }
+    }
+}
+
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 // Device buffers of one LBVH build: outputs and scratch.  trav may be null
@@ -629,10 +790,79 @@ void free_scene(venu_scene* s) {
     cudaFree(s->meta);
     cudaFree(s->keys);
     cudaFree(s->parents);
+    cudaFree(s->wide);
+    cudaFree(s->wide_src);
+    s->wide = nullptr;
+    s->wide_src = nullptr;
+    s->nwide = 0;
     s->parents = nullptr;
     s->nodes = s->trav = nullptr;
     s->sph = s->mat = nullptr;
     s->meta = s->keys = nullptr;
+}
+
+// The wide tree of a built scene (n > 1): the collapse level by level from
+// the root (the host reads each level's size), then one write pass.
+venu_status build_wide(venu_scene* S, cudaStream_t st) {
+    const uint32_t n = S->n;
+    if (n < 2) return VENU_OK;
+    const uint32_t nint = n - 1;
+    uint32_t *flag = nullptr, *idx = nullptr, *cnt = nullptr;
+    int32_t *fa = nullptr, *fb = nullptr;
+    venu_status rc = VENU_OK;
+    uint32_t nwide = 0;
+#define WSTEP(call)                    \
+    do {                               \
+        cudaError_t _e = (call);       \
+        if (_e != cudaSuccess) {       \
+            rc = cuda_fail(_e, #call); \
+            goto wdone;                \
+        }                              \
+    } while (0)
+    WSTEP(cudaMalloc(&flag, sizeof(uint32_t) * nint));
+    WSTEP(cudaMalloc(&idx, sizeof(uint32_t) * nint));
+    WSTEP(cudaMalloc(&cnt, sizeof(uint32_t)));
+    WSTEP(cudaMalloc(&fa, sizeof(int32_t) * nint));
+    WSTEP(cudaMalloc(&fb, sizeof(int32_t) * nint));
+    WSTEP(cudaMemsetAsync(flag, 0, sizeof(uint32_t) * nint, st));
+    WSTEP(cudaMemsetAsync(flag, 0x01, 1, st));  // the root
+    WSTEP(cudaMemsetAsync(fa, 0, sizeof(int32_t), st));
+    {
+        uint32_t nin = 1;
+        for (int level = 0; nin > 0 && level < 256; ++level) {
+            WSTEP(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), st));
+            k_wide_frontier<<<cdiv(nin, 128), 128, 0, st>>>(S->nodes, fa, nin, fb, cnt, flag);
+            WSTEP(cudaGetLastError());
+            WSTEP(cudaMemcpyAsync(&nin, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            WSTEP(cudaStreamSynchronize(st));
+            std::swap(fa, fb);
+        }
+    }
+    WSTEP(cudaMemcpyAsync(idx, flag, sizeof(uint32_t) * nint, cudaMemcpyDeviceToDevice, st));
+    k_scan<<<1, 1024, 0, st>>>(idx, nint);
+    WSTEP(cudaGetLastError());
+    {
+        uint32_t last_idx = 0, last_flag = 0;
+        WSTEP(cudaMemcpyAsync(&last_idx, idx + nint - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        WSTEP(cudaMemcpyAsync(&last_flag, flag + nint - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        WSTEP(cudaStreamSynchronize(st));
+        nwide = last_idx + last_flag;
+    }
+    WSTEP(cudaMalloc(&S->wide, sizeof(float4) * 16 * (size_t)nwide));
+    WSTEP(cudaMalloc(&S->wide_src, sizeof(int32_t) * kWideChildren * (size_t)nwide));
+    S->nwide = nwide;
+    S->bytes += sizeof(float4) * 16 * (size_t)nwide + sizeof(int32_t) * kWideChildren * (size_t)nwide;
+    k_wide_write<<<cdiv(nint, 128), 128, 0, st>>>(S->nodes, S->sph, n, flag, idx, S->wide, S->wide_src);
+    WSTEP(cudaGetLastError());
+    WSTEP(cudaStreamSynchronize(st));
+#undef WSTEP
+wdone:
+    cudaFree(flag);
+    cudaFree(idx);
+    cudaFree(cnt);
+    cudaFree(fa);
+    cudaFree(fb);
+    return rc;
 }
 
 venu_status build_scene(const venu_sphere* spheres_dev, uint32_t n, cudaStream_t st, venu_scene* S) {
@@ -716,6 +946,11 @@ done:
     cudaFree(B.leafbox);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
+    if (rc == VENU_OK) {
+        const auto t0 = std::chrono::steady_clock::now();
+        rc = build_wide(S, st);
+        S->wide_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
     return rc;
 }
 
@@ -738,6 +973,8 @@ venu_status update_scene(venu_scene* S, const venu_sphere* s, cudaStream_t st) {
         k_refit<<<cdiv(n, 256), 256, 0, st>>>(s, S->meta, 0x3fffffffu, (int)n, S->nodes, S->parents,
                                               S->parents + (n - 1), leafbox, arrive);
         k_trav_layout<<<cdiv(2 * (n - 1), 256), 256, 0, st>>>(S->nodes, S->sph, n, S->trav, nullptr);
+        if (S->nwide) k_wide_refit<<<cdiv(S->nwide, 128), 128, 0, st>>>(S->nodes, S->sph, S->nwide, S->wide_src,
+                                                                      S->wide);
         e = cudaGetLastError();
     }
     cudaFreeAsync(leafbox, st);

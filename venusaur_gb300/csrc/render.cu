@@ -85,8 +85,9 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
 // Persistent lanes: a lane whose ray is finished takes a new one as soon as
 // at least `refill_min` lanes of its warp are idle (one atomic per refill),
 // so warps stay full while the queue lasts instead of waiting for their
-// slowest ray (dynamic fetch, Aila & Laine 2009).
-template <bool COUNT>
+// slowest ray (dynamic fetch, Aila & Laine 2009).  WIDE: over the 8-wide
+// tree (variant 5), whose fewer, heavier steps make a refill relatively cheap.
+template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                       uint32_t* __restrict__ work, int2* __restrict__ hits,
                                                       uint32_t* __restrict__ err,
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
     TraceCounters K{0, 0};
     bool overflow = false;
-    Tracer<COUNT> T;
+    typename std::conditional<WIDE, WideTracer<COUNT>, Tracer<COUNT>>::type T;
     int spill[kSpill];
     float spill_tn[kSpill];
     uint32_t ray = 0;
@@ -125,8 +126,8 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                         // the per-axis loop, on this lane's free stack; the lane
                         // stays idle
                         float t;
-                        const int32_t kk = trace_closest_as<COUNT, true>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x,
-                                                                         blockDim.x, overflow, K);
+                        const int32_t kk = trace_closest_as<COUNT, true, kShared, WIDE>(
+                            S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
                         hits[my] = make_int2(__float_as_int(t), kk);
                     } else if (T.begin(S, R, 0.001f, 1e16f, K)) {
                         active = true;
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
 // find no rays); the output queue is unused then, and its throughput slot i
 // carries ray i's state between bounces.  A separate instantiation, so the
 // ordinary loop keeps its registers.
-template <bool COUNT, bool IN_PLACE, int KS>
+template <bool COUNT, bool IN_PLACE, int KS, bool WIDE>
 __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue& qin, uint32_t n,
                                                  uint32_t* __restrict__ work, const Queue& qout,
                                                  uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
@@ -189,8 +190,8 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
             for (bool first = true;; first = false) {
                 RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
                 float t;
-                const int32_t k =
-                    trace_closest<COUNT, KS>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+                const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x,
+                                                                 overflow, K);
                 const float4 t4 = (IN_PLACE && !first) ? qout.t[i]
                                   : gen.path_seeds     ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
                                                        : qin.t[i];
@@ -217,12 +218,14 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
 // then shades all 32 together once the warp has reconverged and appends the
 // continuing paths with one ballot and one atomic.  Saves the hit record
 // round trip, the second read of the rays and one launch per bounce.
-template <bool COUNT, int KS>
-__global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
-                                                     uint32_t* __restrict__ work, Queue qout,
-                                                     uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
-                                                     uint32_t* __restrict__ err,
-                                                     unsigned long long* __restrict__ stats, PrimaryGen gen) {
+// WIDE: the 8-wide tree instead of the binary traversal layout (variant 4,
+// k_trace_shade_wide, with its own register cap).
+template <bool COUNT, int KS, bool WIDE>
+__device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue& qin,
+                                                 const uint32_t* __restrict__ cnt_in, uint32_t* __restrict__ work,
+                                                 const Queue& qout, uint32_t* __restrict__ cnt_out,
+                                                 float4* __restrict__ slots, uint32_t* __restrict__ err,
+                                                 unsigned long long* __restrict__ stats, const PrimaryGen& gen) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
@@ -239,14 +242,34 @@ __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const ui
     bool overflow = false;
     uint32_t extra = 0;  // segments traced in place after a ray's first
     if (n <= gridDim.x * blockDim.x) {
-        trace_shade_loop<COUNT, true, KS>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
+        trace_shade_loop<COUNT, true, KS, WIDE>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K,
+                                                extra);
         for (int off = 16; off > 0; off >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, off);
         if (lane == 0 && extra) atomicAdd(stats, (unsigned long long)extra);
     } else {
-        trace_shade_loop<COUNT, false, KS>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K, extra);
+        trace_shade_loop<COUNT, false, KS, WIDE>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K,
+                                                 extra);
     }
     if (overflow) atomicOr(err, 1u);
     if (COUNT) flush_counters(K, stats);
+}
+
+template <bool COUNT, int KS>
+__global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+                                                uint32_t* __restrict__ work, Queue qout,
+                                                uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
+                                                uint32_t* __restrict__ err, unsigned long long* __restrict__ stats,
+                                                PrimaryGen gen) {
+    trace_shade_body<COUNT, KS, false>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
+}
+
+template <bool COUNT, int KS>
+__global__ void VENU_WIDE_BOUNDS k_trace_shade_wide(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+                                                    uint32_t* __restrict__ work, Queue qout,
+                                                    uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
+                                                    uint32_t* __restrict__ err,
+                                                    unsigned long long* __restrict__ stats, PrimaryGen gen) {
+    trace_shade_body<COUNT, KS, true>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
 }
 
 __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
@@ -339,6 +362,7 @@ SceneView view_of(const venu_scene* s) {
     v.mat = s->mat;
     v.meta = s->meta;
     v.trav = s->trav;
+    v.wide = s->wide;
     v.n = s->n;
     v.nhoist = s->nhoist;
     for (int i = 0; i < kMaxHoisted; ++i) v.hoist[i] = s->hoist[i];
@@ -394,7 +418,21 @@ cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
     const size_t sm = traverse_smem((int)t.traverse_block);
     cudaError_t e;
-    if (t.traverse_variant >= 2) {  // the fused kernel: every bounce (2), the primary one (3)
+    if (t.traverse_variant == 4) {  // the fused kernel over the 8-wide tree
+        e = occupancy_grid(k_trace_shade_wide<false, kShared>, (int)t.traverse_block, sm,
+                           t.traverse_blocks_per_sm, r->fused_blocks);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade_wide<true, kShared>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sm);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade_wide<false, kSharedShallow>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_trace_shade_wide<true, kSharedShallow>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e != cudaSuccess) return e;
+        r->trav_blocks = r->fused_blocks;
+    } else if (t.traverse_variant >= 2) {  // the fused kernel: every bounce (2), the primary one (3, 5)
         e = occupancy_grid(k_trace_shade<false, kShared>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm,
                            r->fused_blocks);
         if (e == cudaSuccess)
@@ -408,7 +446,13 @@ cudaError_t configure(venu_renderer* r) {
                                      (int)sm);
         if (e != cudaSuccess) return e;
     }
-    if (t.traverse_variant == 0 || t.traverse_variant == 3) {
+    if (t.traverse_variant == 4) {
+    } else if (t.traverse_variant == 5) {  // later bounces: dynamic fetch over the wide tree
+        e = occupancy_grid(k_traverse_dyn<false, true>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm,
+                           r->trav_blocks);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_traverse_dyn<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    } else if (t.traverse_variant == 0 || t.traverse_variant == 3) {
         e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     } else if (t.traverse_variant == 2) {
@@ -519,7 +563,7 @@ extern "C" venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tun
         set_error("venu_renderer_set_tuning: NULL argument");
         return VENU_ERR_INVALID;
     }
-    const bool ok = t->traverse_variant <= 3u && t->refill_min >= 1u && t->refill_min <= 32u &&
+    const bool ok = t->traverse_variant <= 5u && t->refill_min >= 1u && t->refill_min <= 32u &&
                     (t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) &&
                     t->shade_block >= 64u && t->shade_block <= 512u && (t->shade_block % 32u) == 0u &&
                     t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u;
@@ -652,24 +696,36 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                 }
                 // variant 3: the coherent primary rays fused, the divergent
                 // later bounces with the separate traversal kernel
-                const uint32_t v = tu.traverse_variant <= 2u ? tu.traverse_variant : (b == 0 ? 2u : 0u);
-                if (v == 2) {
+                const uint32_t v = tu.traverse_variant <= 2u ? tu.traverse_variant
+                                   : tu.traverse_variant == 4u ? 4u
+                                   : tu.traverse_variant == 5u ? (b == 0 ? 2u : 5u)
+                                                               : (b == 0 ? 2u : 0u);
+                if ((v == 4 || v == 5) && scene->nwide == 0u && scene->n > 1u) {
+                    set_error("venu_render: the scene has no wide tree");
+                    return VENU_ERR_INVALID;
+                }
+                if (v == 2 || v == 4) {
                     pg.path_seeds = (b == 0) ? path_seeds : nullptr;
-                    if (shallow) {
-                        const size_t fsm = traverse_smem(tb, kSharedShallow);
-                        if (count)
-                            k_trace_shade<true, kSharedShallow><<<r->fused_blocks, tb, fsm, st>>>(
-                                S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
-                        else
-                            k_trace_shade<false, kSharedShallow><<<r->fused_blocks, tb, fsm, st>>>(
-                                S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
-                    } else if (count) {
-                        k_trace_shade<true, kShared><<<r->fused_blocks, tb, tsm, st>>>(
-                            S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                    const size_t fsm = shallow ? traverse_smem(tb, kSharedShallow) : tsm;
+#define VENU_FUSED(KERNEL, C, KS)                                                                      \
+    KERNEL<C, KS><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, \
+                                                    r->slots, r->err, r->stats, pg)
+                    if (v == 4) {
+                        if (shallow) {
+                            if (count) VENU_FUSED(k_trace_shade_wide, true, kSharedShallow);
+                            else VENU_FUSED(k_trace_shade_wide, false, kSharedShallow);
+                        } else {
+                            if (count) VENU_FUSED(k_trace_shade_wide, true, kShared);
+                            else VENU_FUSED(k_trace_shade_wide, false, kShared);
+                        }
+                    } else if (shallow) {
+                        if (count) VENU_FUSED(k_trace_shade, true, kSharedShallow);
+                        else VENU_FUSED(k_trace_shade, false, kSharedShallow);
                     } else {
-                        k_trace_shade<false, kShared><<<r->fused_blocks, tb, tsm, st>>>(
-                            S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, r->slots, r->err, r->stats, pg);
+                        if (count) VENU_FUSED(k_trace_shade, true, kShared);
+                        else VENU_FUSED(k_trace_shade, false, kShared);
                     }
+#undef VENU_FUSED
                     if (prof) {
                         VENU_CUDA(cudaEventRecord(e1, st));
                         VENU_CUDA(cudaEventRecord(e2, st));
@@ -688,6 +744,13 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                     else
                         k_traverse<false><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,
                                                                           r->err, r->stats);
+                } else if (v == 5) {
+                    if (count)
+                        k_traverse_dyn<true, true><<<r->trav_blocks, tb, tsm, st>>>(
+                            S, qi, r->cnt + b, r->work + b, r->hits, r->err, r->stats, tu.refill_min);
+                    else
+                        k_traverse_dyn<false, true><<<r->trav_blocks, tb, tsm, st>>>(
+                            S, qi, r->cnt + b, r->work + b, r->hits, r->err, r->stats, tu.refill_min);
                 } else {
                     if (count)
                         k_traverse_dyn<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,

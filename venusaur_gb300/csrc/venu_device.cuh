@@ -11,6 +11,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "../../include/venu.h"
 
 #ifndef VENU_MINMAX3
@@ -25,6 +27,12 @@
 #define VENU_TRACE_MAXREG 64
 #endif
 #define VENU_TRACE_BOUNDS __maxnreg__(VENU_TRACE_MAXREG)
+// Register cap of the fused kernel over the 8-wide tree: its step holds a
+// node's 8 sort keys and half a node of boxes, and spills heavily at 64.
+#ifndef VENU_WIDE_MAXREG
+#define VENU_WIDE_MAXREG 80
+#endif
+#define VENU_WIDE_BOUNDS __maxnreg__(VENU_WIDE_MAXREG)
 // The multi-job kernel of the batch engine keeps a per-ray scene view.
 #ifndef VENU_TRACE_MULTI_MAXREG
 #define VENU_TRACE_MULTI_MAXREG 64
@@ -209,6 +217,7 @@ constexpr int kMaxHoisted = 4;
 struct SceneView {
     const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
     const float4* __restrict__ trav;   // 4 float4 per internal node: both children, see lbvh.cu
+    const float4* __restrict__ wide;   // 16 float4 per node of the 8-wide tree, see lbvh.cu
     const float4* __restrict__ sph;    // {center, radius} per slot
     const float4* __restrict__ mat;    // {albedo, fuzz or ir} per slot
     const uint32_t* __restrict__ meta; // original id | material << 30
@@ -599,12 +608,215 @@ struct Tracer {
     }
 };
 
-template <bool COUNT, bool AXIS, int KS = kShared>
+// ---------------------------------------------------------------------------
+// Closest-hit traversal of the 8-wide tree (node layout in lbvh.cu).
+//
+// A step loads one node and tests all eight child boxes with the same
+// instructions in every lane (two halves of four, structure-of-arrays
+// loads), orders the hit internal children by entry distance with a sorting
+// network on 8 keys and pushes them farthest first onto the same
+// shared-memory / local-memory stack as the binary traversal, tests the
+// spheres of the leaf children whose boxes were hit, and pops the next node:
+// the nearest pushed child unless a sphere hit now culls it (popped entries
+// are culled against the closest hit).
+// ---------------------------------------------------------------------------
+template <bool AXIS>
+__device__ __forceinline__ bool box_test_s(const RayPre& R, float lx, float ly, float lz, float hx, float hy,
+                                           float hz, float tmin, float tcap, float& tnear) {
+    const f3 nh = AXIS ? R.n1 : R.n0;
+    float t0x = fmaf(lx, R.inv.x, R.n0.x), t1x = fmaf(hx, R.inv.x, nh.x);
+    float t0y = fmaf(ly, R.inv.y, R.n0.y), t1y = fmaf(hy, R.inv.y, nh.y);
+    float t0z = fmaf(lz, R.inv.z, R.n0.z), t1z = fmaf(hz, R.inv.z, nh.z);
+    float tn = fmax3(fminf(t0x, t1x), fminf(t0y, t1y), fmaxf(fminf(t0z, t1z), tmin));
+    float tf = fmin3(fmaxf(t0x, t1x), fmaxf(t0y, t1y), fminf(fmaxf(t0z, t1z), tcap));
+    tnear = tn;
+    return AXIS ? tn <= tf * 1.00000095367431640625f : tn <= fmaf(tf, 1.00000095367431640625f, R.n1.x);
+}
+
+__device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// Batcher's odd-even merge sort of 8 keys, ascending (19 comparators).
+__device__ __forceinline__ void sort8(uint32_t k[8]) {
+    cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
+    cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
+    cswap(k[1], k[2]); cswap(k[5], k[6]);
+    cswap(k[0], k[4]); cswap(k[1], k[5]); cswap(k[2], k[6]); cswap(k[3], k[7]);
+    cswap(k[2], k[4]); cswap(k[3], k[5]);
+    cswap(k[1], k[2]); cswap(k[3], k[4]); cswap(k[5], k[6]);
+}
+
+template <bool COUNT, bool AXIS = false, int KS = kShared>
+struct WideTracer {
+    RayPre R;
+    float tmin, tmax, best_t;
+    int32_t best, cur;
+    int sp;
+    uint32_t guard;
+
+    __device__ __forceinline__ void leaf(int32_t k, float4 s4, TraceCounters& K) {
+        float t;
+        if (COUNT) ++K.spheres;
+        if (sphere_test(R, s4, tmin, tmax, t) && (t < best_t || (t == best_t && k < best))) {
+            best_t = t;
+            best = k;
+        }
+    }
+
+    __device__ __forceinline__ bool begin(const SceneView& S, const RayPre& R_, float tmin_, float tmax_,
+                                          TraceCounters& K) {
+        R = R_;
+        tmin = tmin_;
+        tmax = tmax_;
+        best_t = tmax_;
+        best = kNone;
+        sp = 0;
+        const uint32_t n = S.n;
+        if (n == 0) return false;
+        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
+        if (n == 1) {
+            leaf(0, __ldg(S.sph), K);
+            return false;
+        }
+        float tn;
+        float4 rlo = __ldg(S.nodes + 0), rhi = __ldg(S.nodes + 1);
+        if (COUNT) ++K.nodes;
+        if (!box_test<AXIS>(R, rlo, rhi, tmin, best_t, tn)) return false;
+        cur = 0;
+        // every wide node is expanded at most once per ray, and there are
+        // fewer than n of them: the guard turns a cyclic tree into an error
+        guard = n + 8u;
+        return true;
+    }
+
+    __device__ __forceinline__ void push(StackSmem sm, uint32_t tid, uint32_t bdim, int* spill, float* spill_tn,
+                                         bool& overflow, int32_t node, float tn) {
+        const uint32_t j = (uint32_t)(sp & (KS - 1)) * bdim + tid;
+        if (sp >= KS) {
+            const int g = sp - KS;
+            if (g >= kSpill) {
+                overflow = true;
+                return;
+            }
+            spill[g] = sm.node[j];
+            spill_tn[g] = sm.tn[j];
+        }
+        sm.node[j] = node;
+        sm.tn[j] = tn;
+        ++sp;
+    }
+
+    __device__ __forceinline__ bool step(const SceneView& S, StackSmem sm, uint32_t tid, uint32_t bdim,
+                                         int* spill, float* spill_tn, bool& overflow, TraceCounters& K) {
+        if (--guard == 0u) {
+            overflow = true;
+            return false;
+        }
+        if (COUNT) {
+            ++K.lane_steps;
+            const uint32_t am = __activemask();
+            if ((tid & 31u) == (uint32_t)(__ffs(am) - 1)) ++K.warp_steps;
+        }
+        const float4* N = S.wide + 16 * (size_t)cur;
+        const uint32_t masks = __float_as_uint(__ldg(N + 14).x);
+        const uint32_t leafm = (masks >> 8) & 0xffu, intm = masks & ~leafm & 0xffu;
+        // key of child c: its entry distance's bits with c in the low three
+        // bits (distances are >= tmin > 0, so the bits order like the
+        // values; the cut makes a key's distance a lower bound), all ones
+        // unless it is a hit internal child
+        uint32_t key[8];
+        uint32_t lhit = 0;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const float4 lx = __ldg(N + h), hx = __ldg(N + 2 + h);
+            const float4 ly = __ldg(N + 4 + h), hy = __ldg(N + 6 + h);
+            const float4 lz = __ldg(N + 8 + h), hz = __ldg(N + 10 + h);
+            float t;
+#define VENU_WIDE_CHILD(J, C)                                                                       \
+    {                                                                                               \
+        const bool ok = box_test_s<AXIS>(R, lx.C, ly.C, lz.C, hx.C, hy.C, hz.C, tmin, best_t, t); \
+        lhit |= (uint32_t)ok << (J);                                                                \
+        key[J] = (ok && ((intm >> (J)) & 1u)) ? ((__float_as_uint(t) & ~7u) | (uint32_t)(J)) : 0xffffffffu; \
+    }
+            VENU_WIDE_CHILD(4 * h + 0, x)
+            VENU_WIDE_CHILD(4 * h + 1, y)
+            VENU_WIDE_CHILD(4 * h + 2, z)
+            VENU_WIDE_CHILD(4 * h + 3, w)
+#undef VENU_WIDE_CHILD
+        }
+        lhit &= leafm;
+        if (COUNT) K.nodes += (uint32_t)__popc(masks & 0xffu);
+        const int32_t* words = reinterpret_cast<const int32_t*>(N + 12);
+        // hit internal children onto the stack, farthest first, so the
+        // nearest is popped first: one or two hits without sorting
+        const uint32_t k01 = min(key[0], key[1]), k23 = min(key[2], key[3]);
+        const uint32_t k45 = min(key[4], key[5]), k67 = min(key[6], key[7]);
+        const uint32_t kmin = min(min(k01, k23), min(k45, k67));
+        if (kmin != 0xffffffffu) {
+            uint32_t nhit = 0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) nhit += key[c] != 0xffffffffu;
+            if (nhit <= 2u) {
+                uint32_t kmax = 0;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) kmax = key[c] != 0xffffffffu ? max(kmax, key[c]) : kmax;
+                if (nhit == 2u) push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (kmax & 7u)),
+                                     __uint_as_float(kmax & ~7u));
+                push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (kmin & 7u)),
+                     __uint_as_float(kmin & ~7u));
+            } else {
+                sort8(key);
+#pragma unroll
+                for (int i = 7; i >= 0; --i) {
+                    if (key[i] != 0xffffffffu)
+                        push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (key[i] & 7u)),
+                             __uint_as_float(key[i] & ~7u));
+                }
+            }
+            if (overflow) return false;
+        }
+        // then the spheres of the hit leaf children, which may shorten the
+        // ray and cull the pushed entries
+        for (uint32_t lm = lhit; lm; lm &= lm - 1u) {
+            const int32_t k = __ldg(words + (__ffs(lm) - 1)) & kSlotMask;
+            leaf(k, __ldg(S.sph + k), K);
+        }
+        while (sp > 0) {
+            --sp;
+            const uint32_t j = (uint32_t)(sp & (KS - 1)) * bdim + tid;
+            const int32_t e = sm.node[j];
+            const float etn = sm.tn[j];
+            if (sp >= KS) {
+                sm.node[j] = spill[sp - KS];
+                sm.tn[j] = spill_tn[sp - KS];
+            }
+            if (etn <= best_t) {
+                cur = e;
+                return true;
+            }
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ int32_t result(float& t) const {
+        if (best == kNone) {
+            t = tmax;
+            return -1;
+        }
+        t = best_t;
+        return best;
+    }
+};
+
+template <bool COUNT, bool AXIS, int KS = kShared, bool WIDE = false>
 __device__ __forceinline__ int32_t trace_closest_as(const SceneView& S, const RayPre& R, float tmin,
                                                     float tmax, float& t_out, StackSmem sm,
                                                     uint32_t tid, uint32_t bdim, bool& overflow,
                                                     TraceCounters& K) {
-    Tracer<COUNT, AXIS, KS> T;
+    typename std::conditional<WIDE, WideTracer<COUNT, AXIS, KS>, Tracer<COUNT, AXIS, KS>>::type T;
     int spill[kSpill];
     float spill_tn[kSpill];
     if (T.begin(S, R, tmin, tmax, K))
@@ -616,13 +828,14 @@ __device__ __forceinline__ int32_t trace_closest_as(const SceneView& S, const Ra
 // Closest hit of one ray (R from prep): the shared-margin loop, or the
 // per-axis one for the rare near-axis-parallel ray.  KS: shared-memory stack
 // entries per thread (the kernel's StackSmem holds KS of them).
-template <bool COUNT, int KS = kShared>
+template <bool COUNT, int KS = kShared, bool WIDE = false>
 __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPre& R, float tmin,
                                                  float tmax, float& t_out, StackSmem sm,
                                                  uint32_t tid, uint32_t bdim, bool& overflow,
                                                  TraceCounters& K) {
-    if (R.axis) return trace_closest_as<COUNT, true, KS>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
-    return trace_closest_as<COUNT, false, KS>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
+    if (R.axis)
+        return trace_closest_as<COUNT, true, KS, WIDE>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
+    return trace_closest_as<COUNT, false, KS, WIDE>(S, R, tmin, tmax, t_out, sm, tid, bdim, overflow, K);
 }
 
 // ---------------------------------------------------------------------------

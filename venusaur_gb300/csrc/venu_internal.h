@@ -33,10 +33,14 @@ struct venu_scene {
     uint32_t* meta = nullptr;  // original id | material << 30
     uint32_t* keys = nullptr;  // sorted Morton codes
     int32_t* parents = nullptr;  // [n-1] parent of each internal node, then [n] of each leaf (for refits)
+    float4* wide = nullptr;      // 16 per wide node: the 8-wide traversal tree (lbvh.cu)
+    int32_t* wide_src = nullptr; // 8 per wide node: binary word of each child (for refits)
+    uint32_t nwide = 0;
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     uint32_t nhoist = 0;          // huge spheres tested before traversal
     int32_t hoist[4] = {0, 0, 0, 0};
     float build_ms = 0.0f;
+    float wide_ms = 0.0f;         // wall time of the wide tree's collapse
     uint64_t bytes = 0;
 };
 
