@@ -277,6 +277,49 @@ def profile_mixed(venu, torch, args):
     print(json.dumps({"profile_mixed": b.stats()}))
 
 
+def batch_ceiling(venu, torch, wf, jobs, cams, scenes, sat_paths=64 << 20):
+    """What batching can recover on this job set at most, with these kernels:
+    every job rendered alone by the plain method (device time, CUDA events),
+    against the time its segments take at the rate the plain method reaches
+    on the same scene, camera and resolution when the GPU is saturated (the
+    job re-rendered with its samples per pixel raised to at least `sat_paths`
+    paths).  A batcher that ran every job at its scene's saturated rate would
+    take sum(ideal); plain takes sum(alone): their ratio bounds the speed-up
+    of any batching of these jobs."""
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    alone_ms, ideal_ms, rows = 0.0, 0.0, []
+    for j, cam in zip(jobs, cams):
+        W, H = j["W"], j["H"]
+        acc = venu.new_accum(W, H)
+        ds = scenes[j["key"]]
+
+        def once(spp, sub):
+            e0.record()
+            wf.render(ds, cam, W, H, spp, acc, subframe=sub, max_depth=j["depth"], reset=True)
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1), wf.stats()["segments"]
+
+        once(j["spp"], j["subframe"])  # warm
+        t_ms, segs = once(j["spp"], j["subframe"])
+        sat_spp = max(j["spp"], -(-sat_paths // (W * H)))
+        st_ms, st_segs = once(sat_spp, j["subframe"])
+        rate = st_segs / st_ms
+        alone_ms += t_ms
+        ideal_ms += segs / rate
+        rows.append((W * H * j["spp"], t_ms, segs / rate))
+        del acc
+    rows.sort()
+    half = len(rows) // 2
+    return {"plain_alone_ms": alone_ms, "ideal_ms": ideal_ms, "max_speedup": alone_ms / ideal_ms,
+            "smaller_half": {"plain_alone_ms": sum(r[1] for r in rows[:half]),
+                             "ideal_ms": sum(r[2] for r in rows[:half])},
+            "larger_half": {"plain_alone_ms": sum(r[1] for r in rows[half:]),
+                            "ideal_ms": sum(r[2] for r in rows[half:])},
+            "method": "each job alone by the plain method vs its segments at its scene's saturated plain rate "
+                      f"(same scene, camera and resolution, spp raised to >= {sat_paths >> 20} Mi paths)"}
+
+
 def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune=True):
     """The plain method (one venu_render per job, in sequence) against the
     batched engine (all jobs in one shared pool, one graph launch) on the
@@ -346,6 +389,7 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
     segs = (b.stats()["segments"] - seg0) // 2
     p_ms, p_wall = timed(plain)
     same_all = all(torch.equal(acc_plain[i], acc_batch[i]) for i in range(len(jobs)))
+    ceiling = None if small else batch_ceiling(venu, torch, wf, jobs, cams, scenes)
     desc = (f"{len(jobs)} RTIOW scenes (seeds 0..{len(jobs) - 1}), 256x144, 4 spp, depth 50" if small else
             f"{n_jobs} scenes, spheres log-uniform 100..200000, resolutions {{256x256, 512x512, 640x360, "
             f"1024x1024}}, spp {{4, 16, 64}}, depth 50 (seeded)")
@@ -359,6 +403,7 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
                     "method": "one shared path pool, one graph launch", "tuning": batch_tuning},
         "speedup": p_ms / b_ms,
         "identical_accumulators": bool(same_all),
+        "ceiling": ceiling,
     }
 
 

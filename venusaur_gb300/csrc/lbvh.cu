@@ -383,13 +383,23 @@ __device__ __forceinline__ int32_t child_word(const float4* nodes, int32_t p, in
     return __float_as_int(__ldcg(&nodes[2 * p + side].w));
 }
 
-__device__ void restructure_treelet(int32_t N, int n, float4* nodes, int32_t* parent_int, int32_t* parent_leaf,
-                                    const float4* leafbox) {
+// Restructures the treelet rooted at N with the whole warp: every lane grows
+// the same treelet (the same loads), the DP's subsets of one size are shared
+// out over the lanes (each subset's cost is computed exactly as a single
+// thread would: the same members in the same order, the same partition
+// order and tie rule), and lane 0 rewires the treelet.  cost / split: this
+// warp's shared-memory DP tables.  Every lane of the warp calls it with the
+// same N.
+__device__ void restructure_treelet_warp(int32_t N, int n, float4* nodes, int32_t* parent_int,
+                                         int32_t* parent_leaf, const float4* leafbox, float* cost,
+                                         uint8_t* split) {
+    const int lane = threadIdx.x & 31;
     int32_t L[kTreeletLeaves], internals[kTreeletLeaves - 1];
     int nl = 0, ni = 0;
     L[nl++] = child_word(nodes, N, 0);
     L[nl++] = child_word(nodes, N, 1);
     internals[ni++] = N;
+    bool bad = false;
     while (nl < kTreeletLeaves) {
         int pick = -1;
         float pa = -1.0f;
@@ -403,111 +413,149 @@ __device__ void restructure_treelet(int32_t N, int n, float4* nodes, int32_t* pa
             }
         if (pick < 0) break;
         const int32_t c = L[pick];
-        if ((uint32_t)c >= (uint32_t)(n - 1)) return;  // never for a sound tree
+        if ((uint32_t)c >= (uint32_t)(n - 1)) {  // never for a sound tree
+            bad = true;
+            break;
+        }
         internals[ni++] = c;
         L[pick] = child_word(nodes, c, 0);
         L[nl++] = child_word(nodes, c, 1);
     }
     for (int i = 0; i < nl; ++i)
-        if ((L[i] & kLeaf) ? (L[i] & kSlotMask) >= n : (uint32_t)L[i] >= (uint32_t)(n - 1)) return;
-    if (nl < 3) return;
+        if ((L[i] & kLeaf) ? (L[i] & kSlotMask) >= n : (uint32_t)L[i] >= (uint32_t)(n - 1)) bad = true;
+    if (bad || nl < 3) return;  // the same decision in every lane
     const int full = (1 << nl) - 1;
     TBox bx[kTreeletLeaves];
     for (int i = 0; i < nl; ++i) bx[i] = tbox_of(nodes, leafbox, L[i]);
-    float cost[1 << kTreeletLeaves];
-    uint8_t split[1 << kTreeletLeaves];
-    for (int S = 1; S <= full; ++S) {
-        split[S] = 0;
+    for (int S = 1 + lane; S <= full; S += 32)
         if ((S & (S - 1)) == 0) {
             cost[S] = 0.0f;
-            continue;
+            split[S] = 0;
         }
-        TBox u;
-        for (int a = 0; a < 3; ++a) {
-            u.lo[a] = INFINITY;
-            u.hi[a] = -INFINITY;
-        }
-        for (int i = 0; i < nl; ++i)
-            if (S >> i & 1)
-                for (int a = 0; a < 3; ++a) {
-                    u.lo[a] = fminf(u.lo[a], bx[i].lo[a]);
-                    u.hi[a] = fmaxf(u.hi[a], bx[i].hi[a]);
-                }
-        const float area = tbox_area(u);
-        const int low = S & -S, rest = S ^ low;
-        float bc = INFINITY;
-        int bp = 0;
-        for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {  // the subsets of rest but rest, largest first
-            const int P = Q | low;
-            const float c = cost[P] + cost[S ^ P];
-            if (c < bc) {
-                bc = c;
-                bp = P;
+    for (int k = 2; k <= nl; ++k) {
+        __syncwarp();
+        for (int S = 1 + lane; S <= full; S += 32) {
+            if (__popc(S) != k) continue;
+            TBox u;
+            for (int a = 0; a < 3; ++a) {
+                u.lo[a] = INFINITY;
+                u.hi[a] = -INFINITY;
             }
-            if (Q == 0) break;
+            for (int i = 0; i < nl; ++i)
+                if (S >> i & 1)
+                    for (int a = 0; a < 3; ++a) {
+                        u.lo[a] = fminf(u.lo[a], bx[i].lo[a]);
+                        u.hi[a] = fmaxf(u.hi[a], bx[i].hi[a]);
+                    }
+            const float area = tbox_area(u);
+            const int low = S & -S, rest = S ^ low;
+            float bc = INFINITY;
+            int bp = 0;
+            for (int Q = (rest - 1) & rest;; Q = (Q - 1) & rest) {  // the subsets of rest but rest, largest first
+                const int P = Q | low;
+                const float c = cost[P] + cost[S ^ P];
+                if (c < bc) {
+                    bc = c;
+                    bp = P;
+                }
+                if (Q == 0) break;
+            }
+            cost[S] = area + bc;
+            split[S] = (uint8_t)bp;
         }
-        cost[S] = area + bc;
-        split[S] = (uint8_t)bp;
     }
+    __syncwarp();
     float current = 0.0f;
     for (int i = 0; i < ni; ++i) current = current + tbox_area(tbox_of(nodes, leafbox, internals[i]));
-    if (!(cost[full] < current)) return;
-    // order[i]: the subset of the i-th internal node in depth-first preorder;
-    // it is given internals[i]
-    int order[kTreeletLeaves - 1];
-    int no = 0;
-    {
-        int stack[kTreeletLeaves];
-        int sp = 0;
-        stack[sp++] = full;
-        while (sp > 0) {
-            const int S = stack[--sp];
-            if ((S & (S - 1)) == 0) continue;
-            order[no++] = S;
-            stack[sp++] = S ^ split[S];
-            stack[sp++] = split[S];
+    const bool better = cost[full] < current;
+    __syncwarp();
+    if (better && lane == 0) {
+        // order[i]: the subset of the i-th internal node in depth-first
+        // preorder; it is given internals[i]
+        int order[kTreeletLeaves - 1];
+        int no = 0;
+        {
+            int stack[kTreeletLeaves];
+            int sp = 0;
+            stack[sp++] = full;
+            while (sp > 0) {
+                const int S = stack[--sp];
+                if ((S & (S - 1)) == 0) continue;
+                order[no++] = S;
+                stack[sp++] = S ^ split[S];
+                stack[sp++] = split[S];
+            }
+        }
+        auto word = [&](int T) -> int32_t {
+            if ((T & (T - 1)) == 0) return L[__ffs(T) - 1];
+            for (int i = 0; i < no; ++i)
+                if (order[i] == T) return internals[i];
+            return internals[0];  // unreachable: every internal subset is in order[]
+        };
+        for (int i = 0; i < no; ++i) {
+            const int S = order[i];
+            const int32_t me = internals[i];
+            const int32_t l = word(split[S]), r = word(S ^ split[S]);
+            nodes[2 * me].w = __int_as_float(l);
+            nodes[2 * me + 1].w = __int_as_float(r);
+            if (l & kLeaf) parent_leaf[l & kSlotMask] = me;
+            else parent_int[l] = me;
+            if (r & kLeaf) parent_leaf[r & kSlotMask] = me;
+            else parent_int[r] = me;
+        }
+        for (int i = no - 1; i >= 0; --i) {
+            const int32_t me = internals[i];
+            const TBox bl = tbox_of(nodes, leafbox, child_word(nodes, me, 0));
+            const TBox br = tbox_of(nodes, leafbox, child_word(nodes, me, 1));
+            const int32_t lw = child_word(nodes, me, 0), rw = child_word(nodes, me, 1);
+            nodes[2 * me] = make_float4(fminf(bl.lo[0], br.lo[0]), fminf(bl.lo[1], br.lo[1]),
+                                        fminf(bl.lo[2], br.lo[2]), __int_as_float(lw));
+            nodes[2 * me + 1] = make_float4(fmaxf(bl.hi[0], br.hi[0]), fmaxf(bl.hi[1], br.hi[1]),
+                                            fmaxf(bl.hi[2], br.hi[2]), __int_as_float(rw));
         }
     }
-    auto word = [&](int T) -> int32_t {
-        if ((T & (T - 1)) == 0) return L[__ffs(T) - 1];
-        for (int i = 0; i < no; ++i)
-            if (order[i] == T) return internals[i];
-        return internals[0];  // unreachable: every internal subset is in order[]
-    };
-    for (int i = 0; i < no; ++i) {
-        const int S = order[i];
-        const int32_t me = internals[i];
-        const int32_t l = word(split[S]), r = word(S ^ split[S]);
-        nodes[2 * me].w = __int_as_float(l);
-        nodes[2 * me + 1].w = __int_as_float(r);
-        if (l & kLeaf) parent_leaf[l & kSlotMask] = me;
-        else parent_int[l] = me;
-        if (r & kLeaf) parent_leaf[r & kSlotMask] = me;
-        else parent_int[r] = me;
-    }
-    for (int i = no - 1; i >= 0; --i) {
-        const int32_t me = internals[i];
-        const TBox bl = tbox_of(nodes, leafbox, child_word(nodes, me, 0));
-        const TBox br = tbox_of(nodes, leafbox, child_word(nodes, me, 1));
-        const int32_t lw = child_word(nodes, me, 0), rw = child_word(nodes, me, 1);
-        nodes[2 * me] = make_float4(fminf(bl.lo[0], br.lo[0]), fminf(bl.lo[1], br.lo[1]), fminf(bl.lo[2], br.lo[2]),
-                                    __int_as_float(lw));
-        nodes[2 * me + 1] = make_float4(fmaxf(bl.hi[0], br.hi[0]), fmaxf(bl.hi[1], br.hi[1]),
-                                        fmaxf(bl.hi[2], br.hi[2]), __int_as_float(rw));
-    }
+    // lane 0's rewiring is published before any lane moves on (the arrival
+    // atomics order it for the other warps)
+    __syncwarp();
+    __threadfence();
 }
 
-__global__ void k_treelets(int n, float4* nodes, int32_t* parent_int, int32_t* parent_leaf,
-                           const float4* __restrict__ leafbox, uint32_t* __restrict__ arrive) {
+// One thread per leaf walks up as in k_refit; a node is restructured once
+// both of its subtrees are final, by the warp of the thread that arrived
+// second.  Every lane of a warp stays in the loop until none of them is
+// walking, so that it can help: the lanes that won a node in a round are
+// served one after another by the whole warp.
+constexpr int kTreeletBlock = 128;
+__global__ void __launch_bounds__(kTreeletBlock) k_treelets(int n, float4* nodes, int32_t* parent_int,
+                                                             int32_t* parent_leaf, const float4* __restrict__ leafbox,
+                                                             uint32_t* __restrict__ arrive) {
+    __shared__ float s_cost[kTreeletBlock / 32][1 << kTreeletLeaves];
+    __shared__ uint8_t s_split[kTreeletBlock / 32][1 << kTreeletLeaves];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int p = parent_leaf[k];
-    for (int level = 0; p >= 0 && p < n - 1 && level < 128; ++level) {
-        __threadfence();
-        if (atomicAdd(arrive + p, 1u) == 0u) return;  // the other subtree is not final yet
-        __threadfence();
-        restructure_treelet(p, n, nodes, parent_int, parent_leaf, leafbox);
-        p = __ldcg(parent_int + p);
+    const int w = threadIdx.x >> 5;
+    int p = k < n ? parent_leaf[k] : -1;
+    bool walking = k < n;
+    for (int level = 0; level < 128; ++level) {
+        bool want = false;
+        if (walking) {
+            if (p < 0 || p >= n - 1) {
+                walking = false;
+            } else {
+                __threadfence();
+                if (atomicAdd(arrive + p, 1u) == 0u) {
+                    walking = false;  // the other subtree is not final yet
+                } else {
+                    __threadfence();
+                    want = true;
+                }
+            }
+        }
+        for (uint32_t m = __ballot_sync(0xffffffffu, want); m; m &= m - 1u) {
+            const int32_t q = __shfl_sync(0xffffffffu, p, __ffs(m) - 1);
+            restructure_treelet_warp(q, n, nodes, parent_int, parent_leaf, leafbox, s_cost[w], s_split[w]);
+        }
+        if (want) p = __ldcg(parent_int + p);
+        if (!__any_sync(0xffffffffu, walking)) break;
     }
 }
 
@@ -768,7 +816,8 @@ cudaError_t launch_lbvh(const venu_sphere* s, uint32_t n, cudaStream_t st, const
                                               B.arrive);
         e = cudaMemsetAsync(B.arrive, 0, sizeof(uint32_t) * nint, st);
         if (e != cudaSuccess) return e;
-        k_treelets<<<cdiv(n, 128), 128, 0, st>>>((int)n, B.nodes, B.pint, B.pleaf, B.leafbox, B.arrive);
+        k_treelets<<<cdiv(n, kTreeletBlock), kTreeletBlock, 0, st>>>((int)n, B.nodes, B.pint, B.pleaf, B.leafbox,
+                                                                     B.arrive);
     }
     k_gather<<<cdiv(n, 256), 256, 0, st>>>(s, B.vals, 0xffffffffu, n, B.sph, B.mat, B.meta);
     if (n > 1) {
