@@ -407,135 +407,180 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
     }
 
 
-def run_served(venu, torch, tuning, n_requests=100, util=0.8, budget=150 << 30, iters=64):
-    """Serving: a Poisson request stream at ~80 % of the server's capacity
-    through the render server (continuous batching, resident BVHs, 150 GB HBM
-    budget) in two configurations -- one lane, FIFO, 64 Mi-path pool; and an
-    express lane for requests of at most 4 Mi paths ahead of a sequential
-    64 Mi-path bulk lane that yields every 4 Mi rays -- against the plain
-    method serving the same stream
-    one job at a time.  All scenes are resident before each stream starts,
-    for every method."""
-    import threading
+def run_served(venu, torch, tuning, n_sessions=40, util=0.8, budget=150 << 30):
+    """Serving, BASELINE config 5: progressive sessions (requests of 8, 8, 16,
+    32, 64 spp, each submitted when the previous image is back, accumulated
+    on the device) on scenes from the 1M-sphere distribution (100..1M
+    spheres, one scene per session, its BVH built when its first request is
+    admitted and kept resident for the rest), four resolutions, depth 50.
+
+    Each method's capacity is measured at saturation (every session starting
+    at once); each then serves a Poisson stream of session starts at `util`
+    of its own capacity.  Methods: the render server (continuous batching,
+    150 GB HBM budget; one lane FIFO, and an express lane for requests of
+    at most 4 Mi paths ahead of a sequential bulk lane), and the plain
+    method serving requests one at a time in arrival order.  A last run
+    serves the server's stream under a budget small enough to bind, so that
+    admission waits and scenes are evicted (an evicted scene is sent again
+    by its session's next request)."""
+    import heapq
 
     from venusaur_gb300 import workloads
+    from venusaur_gb300._lib import lib
 
-    scenes = {}
+    base = workloads.serving_sessions(n_sessions)
+    spheres = [venu.generate_random(s["n"], s["scene_seed"]) for s in base]
+    cams = [venu.Camera.look_at(s["eye"], (0, 0, 0), 20.0, s["W"] / s["H"], 0.1, 10.0) for s in base]
+    n_req = sum(len(s["steps"]) for s in base)
 
-    def skey(j):
-        return (j["scene_seed"], j["n"])
-
-    def spheres_of(j):
-        if skey(j) not in scenes:
-            scenes[skey(j)] = venu.generate_random(j["n"], j["scene_seed"])
-        return scenes[skey(j)]
-
-    def cam_of(j):
-        return venu.Camera.look_at(j["eye"], (0, 0, 0), 20.0, j["W"] / j["H"], 0.1, 10.0)
-
-    class Client:
-        def __init__(self, srv):
-            self.srv, self.keys = srv, {}
-
-        def submit(self, j):
-            k = self.keys.get(skey(j))
-            if k is None:
-                k = self.keys[skey(j)] = 1 + len(self.keys)
-                return self.srv.submit(cam_of(j), j["W"], j["H"], j["spp"], spheres=spheres_of(j), scene_key=k,
-                                       max_depth=j["depth"])
-            return self.srv.submit(cam_of(j), j["W"], j["H"], j["spp"], scene_key=k, max_depth=j["depth"])
-
-        def warm(self, jobs):  # every scene resident
-            for j in jobs:
-                self.srv.wait(self.submit(dict(j, W=16, H=16, spp=1)))
-
-    # capacity: a burst of requests all at once through the one-lane server
-    srv = venu.Server(budget, pool_paths=64 << 20, max_jobs=256, iterations_per_step=iters)
-    cl = Client(srv)
-    calib = workloads.serving_jobs(24, rate_per_s=1.0, seed=2)
-    cl.warm(calib)
-    t0 = time.perf_counter()
-    ids = [cl.submit(j) for j in calib]
-    for i in ids:
-        assert srv.wait(i)["status"] == 0
-    cap_jobs_per_s = len(calib) / (time.perf_counter() - t0)
-    lam = util * cap_jobs_per_s
-    jobs = workloads.serving_jobs(n_requests, rate_per_s=lam, seed=3)
-    small = np.array([j["W"] * j["H"] * j["spp"] <= (4 << 20) for j in jobs])
-
-    def split(lat):
+    def pct(lat):
+        lat = np.asarray(lat)
         return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                "p50_ms_small": float(np.percentile(lat[small], 50)),
-                "p50_ms_large": float(np.percentile(lat[~small], 50))}
+                "max_ms": float(lat.max())}
 
-    def stream(cl):
-        srv = cl.srv
-        seg0 = srv.stats()["segments"]
-        ids = [None] * len(jobs)
+    def serve(srv, arrivals):
+        """Drives the server: one thread per session, requests in order."""
+        lat, first, segs0 = [], [], srv.stats()["segments"]
+        failed = [0]
+        lock = threading.Lock()
         start = time.perf_counter()
 
-        def client():
-            for k, j in enumerate(jobs):
-                dt = start + j["arrival"] - time.perf_counter()
-                if dt > 0:
-                    time.sleep(dt)
-                ids[k] = cl.submit(j)
+        def session(i):
+            s = base[i]
+            dt = start + arrivals[i] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            sub = 1
+            for k, spp in enumerate(s["steps"]):
+                kw = dict(scene_key=i + 1, session=i + 1, subframe=sub, max_depth=s["depth"], reset=(k == 0))
+                rid = srv.submit(cams[i], s["W"], s["H"], spp, spheres=spheres[i] if k == 0 else None, **kw)
+                r = srv.wait(rid)
+                if r["status"] == 1 and k > 0:  # its scene was evicted: send it again
+                    rid = srv.submit(cams[i], s["W"], s["H"], spp, spheres=spheres[i], **kw)
+                    r = srv.wait(rid)
+                with lock:
+                    if r["status"] != 0:
+                        failed[0] += 1
+                    lat.append(r["latency_ms"])
+                    if k == 0:
+                        first.append(r["latency_ms"])
+                sub += spp
+            srv.end_session(i + 1)
 
-        th = threading.Thread(target=client)
-        th.start()
-        th.join()
-        res = [srv.wait(i) for i in ids]
-        makespan = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
-        lat = np.array([r["latency_ms"] for r in res])
-        segs = srv.stats()["segments"] - seg0
-        out = split(lat)
-        out.update({"value": segs / makespan, "unit": UNIT, "makespan_s": makespan,
-                    "failed": int(sum(r["status"] != 0 for r in res))})
-        return out, segs
+        ths = [threading.Thread(target=session, args=(i,)) for i in range(len(base))]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        makespan = time.perf_counter() - start
+        st = srv.stats()
+        out = pct(lat)
+        out.update({"p50_ms_first": float(np.percentile(first, 50)), "requests": len(lat), "failed": failed[0],
+                    "makespan_s": makespan, "value": (st["segments"] - segs0) / makespan, "unit": UNIT,
+                    "evictions": int(st["evictions"]), "admission_waits": int(st["admission_waits"]),
+                    "peak_resident_gb": st["peak_resident_bytes"] / 2**30, "budget_gb": st["budget_bytes"] / 2**30})
+        return out
 
-    out = {}
-    cl.warm(jobs)
-    out["server_fifo"], segs = stream(cl)
-    out["server_fifo"]["config"] = "one lane, FIFO plan order, 64 Mi-path pool"
-    srv.close()
-    srv = venu.Server(budget, pool_paths=64 << 20, max_jobs=256, iterations_per_step=iters, express_paths=4 << 20)
-    srv.set_policy("sequential")
-    cl = Client(srv)
-    cl.warm(jobs)
-    out["server_express"], segs = stream(cl)
-    out["server_express"]["config"] = ("express lane (2 Mi-path pool) for requests of <= 4 Mi paths, "
-                                       "sequential bulk lane with a 64 Mi-path pool yielding every 4 Mi rays")
-    srv.close()
+    def new_server(kind, budget_bytes):
+        if kind == "fifo":
+            return venu.Server(budget_bytes, pool_paths=64 << 20, max_jobs=256, iterations_per_step=64)
+        srv = venu.Server(budget_bytes, pool_paths=64 << 20, max_jobs=256, iterations_per_step=64,
+                          express_paths=4 << 20)
+        srv.set_policy("sequential")
+        return srv
 
-    # the plain method: one job at a time, same arrivals, resident BVHs,
-    # waves of up to 128 Mi paths (every path of a request in one wave)
     wf = venu.Wavefront(128 << 20)
     if tuning:
         wf.set_tuning(**tuning)
-    dscenes = {k: venu.DeviceScene(v) for k, v in scenes.items()}
-    plain_lat = []
-    start = time.perf_counter()
-    tfree = 0.0
-    for j in jobs:
-        now = time.perf_counter() - start
-        if now < j["arrival"]:
-            time.sleep(j["arrival"] - now)
-        acc = venu.new_accum(j["W"], j["H"])
-        img = torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda")
-        wf.render(dscenes[skey(j)], cam_of(j), j["W"], j["H"], j["spp"], acc, subframe=1,
-                  max_depth=j["depth"], reset=True, image8=img)
-        img.cpu()
-        tfree = time.perf_counter() - start
-        plain_lat.append(1000.0 * (tfree - j["arrival"]))
-    plat = np.array(plain_lat)
-    plain_makespan = tfree - jobs[0]["arrival"]
-    out["plain"] = split(plat)
-    out["plain"].update({"value": segs / plain_makespan, "unit": UNIT, "makespan_s": plain_makespan,
-                         "method": "venu_render one job at a time (FIFO), same arrivals"})
-    out["workload"] = (f"{n_requests} requests, Poisson arrivals at {lam:.2f}/s (~{int(100 * util)} % of the "
-                       f"server's measured capacity {cap_jobs_per_s:.2f} jobs/s), scenes from 16 resident scenes "
-                       "with 100..200000 spheres, resolutions {256x256, 512x512, 640x360, 1024x1024}, spp "
-                       "{8, 16, 32, 64, 128}, depth 50, HBM budget 150 GB; small = at most 4 Mi paths")
+
+    def serve_plain(arrivals):
+        """The plain method: one request at a time, in the order they become
+        ready (a session's next request when its previous image is back);
+        each session's BVH built on its first request, its accumulator kept."""
+        ready = [(arrivals[i], i, i, 0) for i in range(len(base))]
+        heapq.heapify(ready)
+        seq = len(base)
+        dscenes, accs, sub = {}, {}, [1] * len(base)
+        lat, first, segs = [], [], 0
+        start = time.perf_counter()
+        while ready:
+            t_ready, _, i, k = heapq.heappop(ready)
+            now = time.perf_counter() - start
+            if now < t_ready:
+                time.sleep(t_ready - now)
+            s = base[i]
+            if k == 0:
+                dscenes[i] = venu.DeviceScene(spheres[i])
+                accs[i] = venu.new_accum(s["W"], s["H"])
+            img = torch.empty((s["W"] * s["H"], 4), dtype=torch.uint8, device="cuda")
+            spp = s["steps"][k]
+            wf.render(dscenes[i], cams[i], s["W"], s["H"], spp, accs[i], subframe=sub[i], max_depth=s["depth"],
+                      reset=(k == 0), image8=img)
+            img.cpu()
+            segs += wf.stats()["segments"]
+            sub[i] += spp
+            t_done = time.perf_counter() - start
+            lat.append(1000.0 * (t_done - t_ready))
+            if k == 0:
+                first.append(lat[-1])
+            if k + 1 < len(s["steps"]):
+                heapq.heappush(ready, (t_done, seq, i, k + 1))
+                seq += 1
+            else:
+                del dscenes[i], accs[i]
+        makespan = time.perf_counter() - start
+        out = pct(lat)
+        out.update({"p50_ms_first": float(np.percentile(first, 50)), "requests": len(lat), "failed": 0,
+                    "makespan_s": makespan, "value": segs / makespan, "unit": UNIT})
+        return out
+
+    unit = workloads.serving_sessions(n_sessions, rate_per_s=1.0)
+    unit_arr = [s["arrival"] for s in unit]
+    burst = [0.0] * len(base)
+    out = {}
+    # capacities at saturation
+    cap = {}
+    for kind in ("fifo", "express"):
+        srv = new_server(kind, budget)
+        r = serve(srv, burst)
+        srv.close()
+        cap[kind] = {"sessions_per_s": len(base) / r["makespan_s"], "requests_per_s": n_req / r["makespan_s"],
+                     "value": r["value"], "p99_ms": r["p99_ms"], "peak_resident_gb": r["peak_resident_gb"]}
+    r = serve_plain(burst)
+    cap["plain"] = {"sessions_per_s": len(base) / r["makespan_s"], "requests_per_s": n_req / r["makespan_s"],
+                    "value": r["value"], "p99_ms": r["p99_ms"]}
+    out["capacity"] = cap
+    # streams at util of each method's own capacity
+    for kind in ("fifo", "express"):
+        lam = util * cap[kind]["sessions_per_s"]
+        srv = new_server(kind, budget)
+        out[f"server_{kind}"] = serve(srv, [t / lam for t in unit_arr])
+        out[f"server_{kind}"]["sessions_per_s"] = lam
+        srv.close()
+    lam_p = util * cap["plain"]["sessions_per_s"]
+    out["plain"] = serve_plain([t / lam_p for t in unit_arr])
+    out["plain"]["sessions_per_s"] = lam_p
+    # the plain method's stream through the express server as well: the same
+    # offered load for both
+    srv = new_server("express", budget)
+    out["server_express_at_plain_load"] = serve(srv, [t / lam_p for t in unit_arr])
+    srv.close()
+    # a budget that binds: room for the largest request (its job, image and
+    # scene) and every session's accumulator, plus a quarter
+    need = max(int(lib().venu_batch_job_bytes(s["W"], s["H"], spp)) + s["W"] * s["H"] * 36 + 240 * s["n"] + 4096
+               for s in base for spp in s["steps"])
+    accs = sum(s["W"] * s["H"] * 32 for s in base)
+    tight = int(1.25 * (need + accs))
+    lam = util * cap["express"]["sessions_per_s"]
+    srv = new_server("express", tight)
+    out["server_express_tight_budget"] = serve(srv, [t / lam for t in unit_arr])
+    srv.close()
+    wf.close()
+    out["workload"] = (f"{n_sessions} progressive sessions ({n_req} requests of 8, 8, 16, 32, 64 spp, 128 "
+                       "accumulated), scenes from the 1M-sphere distribution (sphere counts log-uniform "
+                       "100..1000000, one per session), resolutions {256x256, 512x512, 640x360, 1024x1024}, depth "
+                       f"50; Poisson session starts at {int(100 * util)} % of each method's capacity measured at "
+                       f"saturation; HBM budget 150 GB (tight run: {tight / 2**30:.2f} GB)")
     return out
 
 

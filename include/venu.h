@@ -443,6 +443,9 @@ typedef struct venu_server_stats {
     uint32_t active, pending;
     double p50_ms, p99_ms;      /* request latency (submit -> image on host), completed requests */
     double busy_seconds;        /* wall time with at least one admitted job */
+    uint64_t evictions;         /* resident scenes evicted to make room under the budget */
+    uint64_t admission_waits;   /* server steps at which the next request waited for room */
+    uint64_t peak_resident_bytes; /* most device bytes held at once (scenes, jobs, sessions) */
 } venu_server_stats;
 
 /* Test hooks: make the next admission fail as if its allocation failed

@@ -98,7 +98,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("resident_bytes", C.c_uint64), ("budget_bytes", C.c_uint64), ("segments", C.c_uint64),
                 ("active", C.c_uint32), ("pending", C.c_uint32), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
-                ("busy_seconds", C.c_double)]
+                ("busy_seconds", C.c_double), ("evictions", C.c_uint64), ("admission_waits", C.c_uint64),
+                ("peak_resident_bytes", C.c_uint64)]
 
 
 BATCH_NO_GRAPH = 1

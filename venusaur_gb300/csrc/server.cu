@@ -77,7 +77,12 @@ constexpr uint64_t kPrivateKey = 1ull << 63;  // scenes of requests without a ke
 constexpr uint32_t kExpressPool = 2u << 20;    // paths in flight in the express lane
 constexpr uint32_t kBulkChunk = 4u << 20;      // bulk rays per step while the express lane is on
 
-uint64_t scene_estimate(uint32_t n) { return (uint64_t)n * 72u + 256u; }
+// Device bytes of a scene of n spheres, for admission before it is built:
+// binary nodes 32 + traversal records 64 + spheres, materials 32 + meta,
+// keys 8 + parent links 8 bytes per sphere, and the 8-wide tree (at most
+// about one node of 256 + 32 bytes per three spheres).  Once built, the
+// scene's own byte count replaces the estimate.
+uint64_t scene_estimate(uint32_t n) { return (uint64_t)n * 240u + 4096u; }
 uint64_t image_bytes(const venu_render_opts& o) {
     return (uint64_t)o.width * o.height * (sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL + 4u);
 }
@@ -119,6 +124,10 @@ struct venu_server {
     std::unordered_map<uint64_t, Session> sessions;
     std::vector<uint64_t> sessions_to_end;  // guarded by mu; ended by the server thread
     uint64_t resident = 0, use_clock = 0;
+    // guarded by mu
+    uint64_t evictions = 0;        // scenes evicted to make room
+    uint64_t admission_waits = 0;  // steps at which the queue head waited for room
+    uint64_t peak_resident = 0;    // most device bytes held at once
     size_t n_active_all() const { return active[0].size() + active[1].size(); }
     venu_batch* lane(int l) const { return l ? express : batch; }
 };
@@ -163,6 +172,8 @@ void evict_for(venu_server* s, uint64_t need) {
         venu_scene_destroy(s->scenes[victim].scene);
         s->resident -= s->scenes[victim].bytes;
         s->scenes.erase(victim);
+        std::lock_guard<std::mutex> lock(s->mu);
+        ++s->evictions;
     }
 }
 
@@ -422,7 +433,11 @@ void server_loop(venu_server* s) {
                 continue;
             }
             if (s->resident + need > s->budget) evict_for(s, need);
-            if (s->resident + need > s->budget || s->n_active_all() >= s->max_jobs) break;  // wait for room
+            if (s->resident + need > s->budget || s->n_active_all() >= s->max_jobs) {  // wait for room
+                std::lock_guard<std::mutex> lock(s->mu);
+                ++s->admission_waits;
+                break;
+            }
             {
                 std::lock_guard<std::mutex> lock(s->mu);
                 s->pending.pop_front();
@@ -433,6 +448,7 @@ void server_loop(venu_server* s) {
             std::lock_guard<std::mutex> lock(s->mu);
             s->n_active = (uint32_t)s->n_active_all();
             s->resident_shared = s->resident;
+            s->peak_resident = std::max(s->peak_resident, s->resident);
         }
         if (s->n_active_all() == 0) {
             std::unique_lock<std::mutex> lock(s->mu);
@@ -693,6 +709,9 @@ extern "C" venu_status venu_server_stats_get(venu_server* s, venu_server_stats* 
     out->p50_ms = pct(0.50);
     out->p99_ms = pct(0.99);
     out->busy_seconds = s->busy;
+    out->evictions = s->evictions;
+    out->admission_waits = s->admission_waits;
+    out->peak_resident_bytes = s->peak_resident;
     return VENU_OK;
 }
 

@@ -8,6 +8,13 @@ camera at (60, 15, 60) looking at the origin (vfov 20, aperture 0.1, focus 10).
 
 serving_jobs(): the same scene/resolution distribution with spp uniform from
 {8, 16, 32, 64, 128} and Poisson arrival times.
+
+serving_sessions(): progressive render sessions, each on its own scene drawn
+from the 1M-sphere scene's distribution (the same generator, sphere counts
+log-uniform in [100, 1 000 000]), one of the four resolutions, and five
+requests of 8, 8, 16, 32 and 64 samples per pixel (8 to 128 accumulated),
+each submitted when the previous one's image is back; sessions start with
+Poisson arrivals.
 """
 from __future__ import annotations
 
@@ -66,3 +73,28 @@ def small_jobs(n_jobs: int = 128, W: int = 256, H: int = 144, spp: int = 4, dept
 
 def paths(jobs) -> int:
     return sum(j["W"] * j["H"] * j["spp"] for j in jobs)
+
+
+SESSION_STEPS = (8, 8, 16, 32, 64)  # samples per request; 8, 16, 32, 64, 128 accumulated
+
+
+def serving_sessions(n_sessions: int, rate_per_s: float = 0.0, seed: int = 5, nmin: int = 100,
+                     nmax: int = 1_000_000, depth: int = 50):
+    """Sessions with their start times.  The sessions themselves (scene,
+    resolution) depend only on `seed`; the start times are the same unit
+    Poisson draws scaled by 1 / rate_per_s (all at 0 when the rate is 0),
+    so one set of sessions can be offered at several rates."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_sessions):
+        n, W, H, _ = _draw(rng, SPP_SERVING, nmin, nmax)
+        out.append(dict(n=n, scene_seed=7000 + i, W=W, H=H, steps=SESSION_STEPS, depth=depth, eye=EYE))
+    gaps = np.random.default_rng(seed + 1).exponential(1.0, size=n_sessions)
+    t = np.cumsum(gaps) - gaps[0]
+    for s, ti in zip(out, t):
+        s["arrival"] = float(ti / rate_per_s) if rate_per_s > 0 else 0.0
+    return out
+
+
+def session_paths(sessions) -> int:
+    return sum(s["W"] * s["H"] * sum(s["steps"]) for s in sessions)
