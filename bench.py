@@ -320,6 +320,25 @@ def batch_ceiling(venu, torch, wf, jobs, cams, scenes, sat_paths=64 << 20):
                       f"(same scene, camera and resolution, spp raised to >= {sat_paths >> 20} Mi paths)"}
 
 
+def profile_render(venu, torch, cfg, args):
+    """One warm-up render and one render of the configuration (for a
+    profiler's launch list: the second render's launches follow the first's)."""
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    ds = venu.DeviceScene(make_scene(venu, cfg["scene"]))
+    cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    wf = venu.Wavefront(int(min(256 << 20, W * H * spp)))
+    wf.set_tuning(**(json.loads(args.tuning) if args.tuning else dict(traverse_variant=2, traverse_block=128)))
+    acc = venu.new_accum(W, H)
+    out = []
+    for sub in (1, 2):
+        wf.render(ds, cam, W, H, spp, acc, subframe=sub, max_depth=depth, reset=True)
+        torch.cuda.synchronize()
+        st = wf.stats()
+        out.append({"segments": st["segments"], "paths": st["paths"], "kernel_launches": st["kernel_launches"]})
+    print(json.dumps({"profile_render": cfg["workload"], "tuning": wf.tuning(), "renders": out,
+                      "kernel_sources_sha": kernel_sources_sha()}))
+
+
 def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune=True):
     """The plain method (one venu_render per job, in sequence) against the
     batched engine (all jobs in one shared pool, one graph launch) on the
@@ -560,11 +579,12 @@ def run_served(venu, torch, tuning, n_sessions=40, util=0.8, budget=150 << 30):
     lam_p = util * cap["plain"]["sessions_per_s"]
     out["plain"] = serve_plain([t / lam_p for t in unit_arr])
     out["plain"]["sessions_per_s"] = lam_p
-    # the plain method's stream through the express server as well: the same
-    # offered load for both
-    srv = new_server("express", budget)
-    out["server_express_at_plain_load"] = serve(srv, [t / lam_p for t in unit_arr])
-    srv.close()
+    # the plain method's stream through both servers as well: the same
+    # offered load for every method
+    for kind in ("fifo", "express"):
+        srv = new_server(kind, budget)
+        out[f"server_{kind}_at_plain_load"] = serve(srv, [t / lam_p for t in unit_arr])
+        srv.close()
     # a budget that binds: room for the largest request (its job, image and
     # scene) and every session's accumulator, plus a quarter
     need = max(int(lib().venu_batch_job_bytes(s["W"], s["H"], spp)) + s["W"] * s["H"] * 36 + 240 * s["n"] + 4096
@@ -822,6 +842,10 @@ def main():
                          "device) through the batch engine's host-driven loop (ncu cannot profile kernels "
                          "inside conditional graphs) and exit")
     ap.add_argument("--no-batched", action="store_true", help="skip the mixed-scene batched/plain comparison")
+    ap.add_argument("--profile-render", action="store_true",
+                    help="only render the configuration once (after one warm-up render) with the launch shapes of "
+                         "--tuning (default: variant 2, 128-thread blocks) and print its segment count: the "
+                         "case the ncu figures of the roofline are taken on")
     ap.add_argument("--no-configs", action="store_true", help="skip the other configurations' blocks")
     args = ap.parse_args()
     cfg = dict(CONFIGS[args.config])
@@ -845,6 +869,9 @@ def main():
     vb.build()
     if args.profile_mixed:
         profile_mixed(venu, torch, args)
+        return
+    if args.profile_render:
+        profile_render(venu, torch, cfg, args)
         return
     # CPU baseline first, on an idle host (rank 0, single process only): the
     # reference's arithmetic on the fixed sample of this configuration, every

@@ -42,7 +42,9 @@ def test_server_results_match_oracle(venu, oracle, cuda):
 
 def test_server_budget_fifo_and_faults(venu, oracle, cuda):
     sp, cam, want = _case(oracle, 0, 24, 16, 2)
-    job = venu.Batch.job_bytes(24, 16, 2) + 24 * 16 * 36 + 485 * 72 + 256
+    # the server's admission estimate: job, image and accumulator, and the
+    # scene at 240 bytes per sphere + 4096 (binary and 8-wide trees)
+    job = venu.Batch.job_bytes(24, 16, 2) + 24 * 16 * 36 + 485 * 240 + 4096
     # room for about one job at a time: requests queue and run in order
     srv = venu.Server(hbm_budget_bytes=job + 40000, pool_paths=1000, max_jobs=4, iterations_per_step=2)
     too_big = srv.submit(cam, 2000, 2000, 64, spheres=sp)
