@@ -291,10 +291,10 @@ typedef struct venu_tuning {
                                         2: as 0, then the warp shades its 32 hits in the same
                                            kernel (no separate shade launch; default);
                                         3: 2 for the primary rays, 0 for later bounces;
-                                        4: as 2, over the 8-wide tree collapsed from the
-                                           LBVH (8 child boxes tested per step);
-                                        5: 2 for the primary rays, then 1 over the 8-wide tree */
-    uint32_t refill_min;             /* variants 1, 5: refill when >= this many lanes are idle (1..32) */
+                                        4: as 2, over the 4-wide tree collapsed from the
+                                           LBVH (4 child boxes tested per step);
+                                        5: 2 for the primary rays, then 0 over the 4-wide tree */
+    uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
     uint32_t shade_block;            /* threads per shade block: 64..512, multiple of 32 */

@@ -10,19 +10,19 @@ from venusaur_gb300 import tune
 def test_candidate_space():
     c = list(tune.candidates())
     # variant 1 x refill {4,8,16} x traverse block {64,128,256} x shade {128,256},
-    # variants 0 and 3 x traverse block x shade block, variants 2 and 4 x traverse block
-    assert len(c) == 3 * 3 * 2 + 2 * 3 * 2 + 2 * 3
+    # variants 0, 3 and 5 x traverse block x shade block, variants 2 and 4 x traverse block
+    assert len(c) == 3 * 3 * 2 + 3 * 3 * 2 + 2 * 3
     assert len({tuple(sorted(x.items())) for x in c}) == len(c)
     for x in c:
         assert x["traverse_variant"] in (0, 1, 2, 3, 4, 5)
-        if x["traverse_variant"] not in (1, 5):
+        if x["traverse_variant"] != 1:
             assert x["refill_min"] == 32
         if x["traverse_variant"] in (2, 4):
             assert x["shade_block"] == 256
     small = list(tune.candidates({"traverse_variant": (2,), "traverse_block": (128,)}))
     assert len(small) == 1
     v5 = list(tune.candidates({"traverse_variant": (5,)}))
-    assert len(v5) == 3 * 3 * 2 and all(x["traverse_variant"] == 5 for x in v5)
+    assert len(v5) == 3 * 2 and all(x["traverse_variant"] == 5 for x in v5)
 
 
 @pytest.mark.gpu

@@ -615,28 +615,30 @@ __global__ void k_trav_layout(const float4* __restrict__ nodes, const float4* __
 }
 
 // ---------------------------------------------------------------------------
-// The 8-wide traversal tree (renderer variant 4), collapsed from the binary
-// LBVH after its build.  A wide node stands for a binary node r and holds up
-// to 8 of r's descendants: starting from r's two children, the internal entry
-// of largest box surface area (the first such entry on ties) is replaced by
-// its two children until there are 8 entries or only leaves.  Internal
-// entries become wide nodes themselves.  The wide nodes are numbered in
-// increasing order of the binary nodes they stand for (root first), so the
-// tree is deterministic.  Results do not depend on it: the closest hit is the
-// same for any conservative traversal (minimum t, ties to the smaller slot).
+// The wide traversal tree (renderer variants 4 and 5), collapsed from the
+// binary LBVH after its build.  A wide node stands for a binary node r and
+// holds up to kWideW (4) of r's descendants: starting from r's two
+// children, the internal entry of largest box surface area (the first such
+// entry on ties) is replaced by its two children until there are kWideW
+// entries or only leaves.  Internal entries become wide nodes themselves.
+// The wide nodes are numbered in increasing order of the binary nodes they
+// stand for (root first), so the tree is deterministic.  Results do not
+// depend on it: the closest hit is the same for any conservative traversal
+// (minimum t, ties to the smaller slot).
 //
-// Node layout (16 float4 = 256 bytes, two cache lines):
-//   [0..11]  child boxes, structure of arrays in two halves of four children:
-//            lo.x c0-3, lo.x c4-7, hi.x c0-3, hi.x c4-7, then y, then z
-//   [12..13] child words c0-3, c4-7: an internal child's wide index, or a
-//            leaf's 0x80000000 | slot (an unused entry or a hoisted leaf:
-//            0x80000000 | 0x40000000, never tested)
-//   [14]     {valid mask | leaf mask << 8 (int bits), 0, 0, 0}
-//   [15]     unused
-// wide_src[8 w + c] keeps the binary word of child c (internal node index or
-// leaf word), so a refit of moved spheres can recompute the boxes in place.
+// Node layout (kWideF4 float4s: 128 bytes for 4 children, 256 for 8), with
+// H = kWideW / 4 float4s per plane:
+//   [0, 6H)   child boxes, structure of arrays: lo.x, hi.x, lo.y, hi.y,
+//             lo.z, hi.z, each H float4s of four children
+//   [6H, 7H)  child words: an internal child's wide index, or a leaf's
+//             0x80000000 | slot (an unused entry or a hoisted leaf:
+//             0x80000000 | 0x40000000, never tested)
+//   [7H]      {valid mask | leaf mask << 8 (int bits), 0, 0, 0}
+// wide_src[kWideW w + c] keeps the binary word of child c (internal node
+// index or leaf word), so a refit of moved spheres can recompute the boxes
+// in place.
 // ---------------------------------------------------------------------------
-constexpr int kWideChildren = 8;
+constexpr int kWideChildren = kWideW;
 
 __device__ __forceinline__ float box_area(float4 lo, float4 hi) {
     const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
@@ -716,18 +718,19 @@ __device__ void wide_write_node(const float4* __restrict__ nodes, const float4* 
         hi[0][c] = h.x; hi[1][c] = h.y; hi[2][c] = h.z;
     }
     for (int a = 0; a < 3; ++a) {
-        for (int half = 0; half < 2; ++half) {
+        for (int half = 0; half < kWideH; ++half) {
             const int c = 4 * half;
-            W[4 * a + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
-            W[4 * a + 2 + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
+            W[2 * a * kWideH + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
+            W[(2 * a + 1) * kWideH + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
         }
     }
-    W[12] = make_float4(__int_as_float(word[0]), __int_as_float(word[1]), __int_as_float(word[2]),
-                        __int_as_float(word[3]));
-    W[13] = make_float4(__int_as_float(word[4]), __int_as_float(word[5]), __int_as_float(word[6]),
-                        __int_as_float(word[7]));
-    W[14] = make_float4(__int_as_float((int)(valid | (leafm << 8))), 0.0f, 0.0f, 0.0f);
-    W[15] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (int half = 0; half < kWideH; ++half) {
+        const int c = 4 * half;
+        W[6 * kWideH + half] = make_float4(__int_as_float(word[c]), __int_as_float(word[c + 1]),
+                                           __int_as_float(word[c + 2]), __int_as_float(word[c + 3]));
+    }
+    W[7 * kWideH] = make_float4(__int_as_float((int)(valid | (leafm << 8))), 0.0f, 0.0f, 0.0f);
+    if (kWideH == 2) W[15] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // One thread per binary internal node; the flagged ones write their wide node.
@@ -741,7 +744,7 @@ __global__ void k_wide_write(const float4* __restrict__ nodes, const float4* __r
     for (int j = c; j < kWideChildren; ++j) w[j] = kLeaf | kHoisted;
     const uint32_t k = idx[r];
     for (int j = 0; j < kWideChildren; ++j) wide_src[(size_t)kWideChildren * k + j] = w[j];
-    wide_write_node(nodes, sph, idx, w, wide + 16 * (size_t)k);
+    wide_write_node(nodes, sph, idx, w, wide + kWideF4 * (size_t)k);
 }
 
 // Refit of moved spheres: the same topology, boxes recomputed from the
@@ -751,7 +754,7 @@ __global__ void k_wide_refit(const float4* __restrict__ nodes, const float4* __r
                              const int32_t* __restrict__ wide_src, float4* __restrict__ wide) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nwide) return;
-    float4* W = wide + 16 * (size_t)k;
+    float4* W = wide + kWideF4 * (size_t)k;
     float lo[3][kWideChildren], hi[3][kWideChildren];
     for (int c = 0; c < kWideChildren; ++c) {
         const int32_t b = wide_src[(size_t)kWideChildren * k + c];
@@ -766,10 +769,10 @@ __global__ void k_wide_refit(const float4* __restrict__ nodes, const float4* __r
         hi[0][c] = h.x; hi[1][c] = h.y; hi[2][c] = h.z;
     }
     for (int a = 0; a < 3; ++a) {
-        for (int half = 0; half < 2; ++half) {
+        for (int half = 0; half < kWideH; ++half) {
             const int c = 4 * half;
-            W[4 * a + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
-            W[4 * a + 2 + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
+            W[2 * a * kWideH + half] = make_float4(lo[a][c], lo[a][c + 1], lo[a][c + 2], lo[a][c + 3]);
+            W[(2 * a + 1) * kWideH + half] = make_float4(hi[a][c], hi[a][c + 1], hi[a][c + 2], hi[a][c + 3]);
         }
     }
 }
@@ -897,10 +900,10 @@ venu_status build_wide(venu_scene* S, cudaStream_t st) {
         WSTEP(cudaStreamSynchronize(st));
         nwide = last_idx + last_flag;
     }
-    WSTEP(cudaMalloc(&S->wide, sizeof(float4) * 16 * (size_t)nwide));
+    WSTEP(cudaMalloc(&S->wide, sizeof(float4) * kWideF4 * (size_t)nwide));
     WSTEP(cudaMalloc(&S->wide_src, sizeof(int32_t) * kWideChildren * (size_t)nwide));
     S->nwide = nwide;
-    S->bytes += sizeof(float4) * 16 * (size_t)nwide + sizeof(int32_t) * kWideChildren * (size_t)nwide;
+    S->bytes += sizeof(float4) * kWideF4 * (size_t)nwide + sizeof(int32_t) * kWideChildren * (size_t)nwide;
     k_wide_write<<<cdiv(nint, 128), 128, 0, st>>>(S->nodes, S->sph, n, flag, idx, S->wide, S->wide_src);
     WSTEP(cudaGetLastError());
     WSTEP(cudaStreamSynchronize(st));

@@ -50,7 +50,8 @@ __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, u
     seeds[pix] = seed;
 }
 
-template <bool COUNT>
+// WIDE: over the 8-wide (or 4-wide) tree (variant 5's later bounces).
+template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                   uint32_t* __restrict__ work, int2* __restrict__ hits,
                                                   uint32_t* __restrict__ err,
@@ -74,7 +75,8 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
             float4 o4 = q.o[i], d4 = q.d[i];
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
             float t;
-            int32_t k = trace_closest<COUNT>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            int32_t k = trace_closest<COUNT, kShared, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x,
+                                                           overflow, K);
             hits[i] = make_int2(__float_as_int(t), k);
         }
     }
@@ -85,9 +87,8 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
 // Persistent lanes: a lane whose ray is finished takes a new one as soon as
 // at least `refill_min` lanes of its warp are idle (one atomic per refill),
 // so warps stay full while the queue lasts instead of waiting for their
-// slowest ray (dynamic fetch, Aila & Laine 2009).  WIDE: over the 8-wide
-// tree (variant 5), whose fewer, heavier steps make a refill relatively cheap.
-template <bool COUNT, bool WIDE = false>
+// slowest ray (dynamic fetch, Aila & Laine 2009).
+template <bool COUNT>
 __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                       uint32_t* __restrict__ work, int2* __restrict__ hits,
                                                       uint32_t* __restrict__ err,
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stats, (unsigned long long)n);
     TraceCounters K{0, 0};
     bool overflow = false;
-    typename std::conditional<WIDE, WideTracer<COUNT>, Tracer<COUNT>>::type T;
+    Tracer<COUNT> T;
     int spill[kSpill];
     float spill_tn[kSpill];
     uint32_t ray = 0;
@@ -126,8 +127,8 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                         // the per-axis loop, on this lane's free stack; the lane
                         // stays idle
                         float t;
-                        const int32_t kk = trace_closest_as<COUNT, true, kShared, WIDE>(
-                            S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+                        const int32_t kk = trace_closest_as<COUNT, true>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x,
+                                                                         blockDim.x, overflow, K);
                         hits[my] = make_int2(__float_as_int(t), kk);
                     } else if (T.begin(S, R, 0.001f, 1e16f, K)) {
                         active = true;
@@ -447,11 +448,11 @@ cudaError_t configure(venu_renderer* r) {
         if (e != cudaSuccess) return e;
     }
     if (t.traverse_variant == 4) {
-    } else if (t.traverse_variant == 5) {  // later bounces: dynamic fetch over the wide tree
-        e = occupancy_grid(k_traverse_dyn<false, true>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm,
+    } else if (t.traverse_variant == 5) {  // later bounces: the separate traversal over the wide tree
+        e = occupancy_grid(k_traverse<false, true>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm,
                            r->trav_blocks);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_traverse_dyn<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+            e = cudaFuncSetAttribute(k_traverse<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     } else if (t.traverse_variant == 0 || t.traverse_variant == 3) {
         e = occupancy_grid(k_traverse<false>, (int)t.traverse_block, sm, t.traverse_blocks_per_sm, r->trav_blocks);
         if (e == cudaSuccess) e = cudaFuncSetAttribute(k_traverse<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -746,11 +747,11 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                                                                           r->err, r->stats);
                 } else if (v == 5) {
                     if (count)
-                        k_traverse_dyn<true, true><<<r->trav_blocks, tb, tsm, st>>>(
-                            S, qi, r->cnt + b, r->work + b, r->hits, r->err, r->stats, tu.refill_min);
+                        k_traverse<true, true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b,
+                                                                               r->hits, r->err, r->stats);
                     else
-                        k_traverse_dyn<false, true><<<r->trav_blocks, tb, tsm, st>>>(
-                            S, qi, r->cnt + b, r->work + b, r->hits, r->err, r->stats, tu.refill_min);
+                        k_traverse<false, true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b,
+                                                                                r->hits, r->err, r->stats);
                 } else {
                     if (count)
                         k_traverse_dyn<true><<<r->trav_blocks, tb, tsm, st>>>(S, qi, r->cnt + b, r->work + b, r->hits,

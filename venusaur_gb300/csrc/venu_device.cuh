@@ -214,6 +214,19 @@ constexpr int32_t kSlotMask = 0x3fffffff;
 constexpr int32_t kNone = 0x7fffffff;
 constexpr int kMaxHoisted = 4;
 
+// Children per node of the wide traversal tree (4; 8 measured slower on
+// every workload here) and its node layout in float4s: per axis a
+// the lo planes of the children at 2a*H + h and the hi planes at
+// (2a+1)*H + h (h = 0..H-1, four children per float4), then the child words
+// at 6H + h and the masks at 7H.
+#ifndef VENU_WIDE_CHILDREN
+#define VENU_WIDE_CHILDREN 4
+#endif
+constexpr int kWideW = VENU_WIDE_CHILDREN;
+constexpr int kWideH = kWideW / 4;
+constexpr int kWideF4 = 8 * kWideH;
+static_assert(kWideW == 4 || kWideW == 8, "the wide tree has 4 or 8 children per node");
+
 struct SceneView {
     const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
     const float4* __restrict__ trav;   // 4 float4 per internal node: both children, see lbvh.cu
@@ -609,16 +622,16 @@ struct Tracer {
 };
 
 // ---------------------------------------------------------------------------
-// Closest-hit traversal of the 8-wide tree (node layout in lbvh.cu).
+// Closest-hit traversal of the wide tree (node layout in lbvh.cu).
 //
-// A step loads one node and tests all eight child boxes with the same
-// instructions in every lane (two halves of four, structure-of-arrays
-// loads), orders the hit internal children by entry distance with a sorting
-// network on 8 keys and pushes them farthest first onto the same
-// shared-memory / local-memory stack as the binary traversal, tests the
-// spheres of the leaf children whose boxes were hit, and pops the next node:
-// the nearest pushed child unless a sphere hit now culls it (popped entries
-// are culled against the closest hit).
+// A step loads one node and tests all of its child boxes with the same
+// instructions in every lane (structure-of-arrays loads, four children per
+// float4), pushes the hit internal children but the nearest farthest first
+// onto the same shared-memory / local-memory stack as the binary traversal
+// (ordered by a sorting network on keys of entry distance and child number
+// when more than two are hit), tests the spheres of the leaf children whose
+// boxes were hit, then descends to the nearest child unless a sphere hit now
+// culls it, else pops (popped entries are culled against the closest hit).
 // ---------------------------------------------------------------------------
 template <bool AXIS>
 __device__ __forceinline__ bool box_test_s(const RayPre& R, float lx, float ly, float lz, float hx, float hy,
@@ -640,6 +653,12 @@ __device__ __forceinline__ void cswap(uint32_t& a, uint32_t& b) {
 }
 
 // Batcher's odd-even merge sort of 8 keys, ascending (19 comparators).
+__device__ __forceinline__ void sort4(uint32_t k[4]) {
+    cswap(k[0], k[1]); cswap(k[2], k[3]);
+    cswap(k[0], k[2]); cswap(k[1], k[3]);
+    cswap(k[1], k[2]);
+}
+
 __device__ __forceinline__ void sort8(uint32_t k[8]) {
     cswap(k[0], k[1]); cswap(k[2], k[3]); cswap(k[4], k[5]); cswap(k[6], k[7]);
     cswap(k[0], k[2]); cswap(k[1], k[3]); cswap(k[4], k[6]); cswap(k[5], k[7]);
@@ -720,20 +739,20 @@ struct WideTracer {
             const uint32_t am = __activemask();
             if ((tid & 31u) == (uint32_t)(__ffs(am) - 1)) ++K.warp_steps;
         }
-        const float4* N = S.wide + 16 * (size_t)cur;
-        const uint32_t masks = __float_as_uint(__ldg(N + 14).x);
+        const float4* N = S.wide + kWideF4 * (size_t)cur;
+        const uint32_t masks = __float_as_uint(__ldg(N + 7 * kWideH).x);
         const uint32_t leafm = (masks >> 8) & 0xffu, intm = masks & ~leafm & 0xffu;
         // key of child c: its entry distance's bits with c in the low three
         // bits (distances are >= tmin > 0, so the bits order like the
         // values; the cut makes a key's distance a lower bound), all ones
         // unless it is a hit internal child
-        uint32_t key[8];
+        uint32_t key[kWideW];
         uint32_t lhit = 0;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const float4 lx = __ldg(N + h), hx = __ldg(N + 2 + h);
-            const float4 ly = __ldg(N + 4 + h), hy = __ldg(N + 6 + h);
-            const float4 lz = __ldg(N + 8 + h), hz = __ldg(N + 10 + h);
+        for (int h = 0; h < kWideH; ++h) {
+            const float4 lx = __ldg(N + h), hx = __ldg(N + kWideH + h);
+            const float4 ly = __ldg(N + 2 * kWideH + h), hy = __ldg(N + 3 * kWideH + h);
+            const float4 lz = __ldg(N + 4 * kWideH + h), hz = __ldg(N + 5 * kWideH + h);
             float t;
 #define VENU_WIDE_CHILD(J, C)                                                                       \
     {                                                                                               \
@@ -749,28 +768,27 @@ struct WideTracer {
         }
         lhit &= leafm;
         if (COUNT) K.nodes += (uint32_t)__popc(masks & 0xffu);
-        const int32_t* words = reinterpret_cast<const int32_t*>(N + 12);
-        // hit internal children onto the stack, farthest first, so the
-        // nearest is popped first: one or two hits without sorting
-        const uint32_t k01 = min(key[0], key[1]), k23 = min(key[2], key[3]);
-        const uint32_t k45 = min(key[4], key[5]), k67 = min(key[6], key[7]);
-        const uint32_t kmin = min(min(k01, k23), min(k45, k67));
+        const int32_t* words = reinterpret_cast<const int32_t*>(N + 6 * kWideH);
+        // the hit internal children but the nearest onto the stack, farthest
+        // first (one or two hits without sorting); the nearest is descended
+        // unless the leaf tests below cull it
+        uint32_t kmin = key[0];
+#pragma unroll
+        for (int c = 1; c < kWideW; ++c) kmin = min(kmin, key[c]);
         if (kmin != 0xffffffffu) {
             uint32_t nhit = 0;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) nhit += key[c] != 0xffffffffu;
-            if (nhit <= 2u) {
+            for (int c = 0; c < kWideW; ++c) nhit += key[c] != 0xffffffffu;
+            if (nhit == 2u) {
                 uint32_t kmax = 0;
 #pragma unroll
-                for (int c = 0; c < 8; ++c) kmax = key[c] != 0xffffffffu ? max(kmax, key[c]) : kmax;
-                if (nhit == 2u) push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (kmax & 7u)),
-                                     __uint_as_float(kmax & ~7u));
-                push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (kmin & 7u)),
-                     __uint_as_float(kmin & ~7u));
-            } else {
-                sort8(key);
+                for (int c = 0; c < kWideW; ++c) kmax = key[c] != 0xffffffffu ? max(kmax, key[c]) : kmax;
+                push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (kmax & 7u)),
+                     __uint_as_float(kmax & ~7u));
+            } else if (nhit > 2u) {
+                if (kWideW == 8) sort8(key); else sort4(key);
 #pragma unroll
-                for (int i = 7; i >= 0; --i) {
+                for (int i = kWideW - 1; i >= 1; --i) {
                     if (key[i] != 0xffffffffu)
                         push(sm, tid, bdim, spill, spill_tn, overflow, __ldg(words + (key[i] & 7u)),
                              __uint_as_float(key[i] & ~7u));
@@ -779,10 +797,14 @@ struct WideTracer {
             if (overflow) return false;
         }
         // then the spheres of the hit leaf children, which may shorten the
-        // ray and cull the pushed entries
+        // ray and cull the pushed entries and the nearest child
         for (uint32_t lm = lhit; lm; lm &= lm - 1u) {
             const int32_t k = __ldg(words + (__ffs(lm) - 1)) & kSlotMask;
             leaf(k, __ldg(S.sph + k), K);
+        }
+        if (kmin != 0xffffffffu && __uint_as_float(kmin & ~7u) <= best_t) {
+            cur = __ldg(words + (kmin & 7u));
+            return true;
         }
         while (sp > 0) {
             --sp;

@@ -13,9 +13,7 @@ import itertools
 from .core import DeviceScene, Wavefront, new_accum
 
 DEFAULT_SPACE = {
-    # variant 5 (dynamic fetch over the 8-wide tree) is never the fastest on
-    # the measured workloads and is left out of the default search
-    "traverse_variant": (0, 1, 2, 3, 4),
+    "traverse_variant": (0, 1, 2, 3, 4, 5),
     "refill_min": (4, 8, 16),
     "traverse_block": (64, 128, 256),
     "shade_block": (128, 256),
@@ -29,7 +27,7 @@ def candidates(space=None):
                                           space["traverse_block"], space["shade_block"]):
         # the refill threshold matters to the dynamic-fetch variants only, the
         # shade block to the variants with a separate shade kernel only
-        key = (v, r if v in (1, 5) else 32, tb, sb if v not in (2, 4) else 256)
+        key = (v, r if v == 1 else 32, tb, sb if v not in (2, 4) else 256)
         if key in seen:
             continue
         seen.add(key)
