@@ -383,50 +383,64 @@ __device__ __forceinline__ int32_t child_word(const float4* nodes, int32_t p, in
     return __float_as_int(__ldcg(&nodes[2 * p + side].w));
 }
 
-// Restructures the treelet rooted at N with the whole warp: every lane grows
-// the same treelet (the same loads), the DP's subsets of one size are shared
-// out over the lanes (each subset's cost is computed exactly as a single
-// thread would: the same members in the same order, the same partition
-// order and tie rule), and lane 0 rewires the treelet.  cost / split: this
-// warp's shared-memory DP tables.  Every lane of the warp calls it with the
-// same N.
+// Restructures the treelet rooted at N with the whole warp.  The treelet's
+// entries are spread over lanes 0..6 (lane i holds entry i), so every
+// memory round trip serves all entries at once: the growth step reads the
+// open entries' boxes in parallel and picks the largest area (first on
+// ties) with a warp reduction; the DP's subsets of one size are shared out
+// over the lanes (each subset's cost computed exactly as a single thread
+// would: the same members in the same order, the same partition order and
+// tie rule); lane 0 rewires the treelet, and each rewired node's box is the
+// union of its subset's entry boxes (min / max are exact, so this equals
+// refitting it from its children).  Every lane of the warp calls it with
+// the same N.  cost / split: this warp's shared-memory DP tables.
 __device__ void restructure_treelet_warp(int32_t N, int n, float4* nodes, int32_t* parent_int,
                                          int32_t* parent_leaf, const float4* leafbox, float* cost,
                                          uint8_t* split) {
     const int lane = threadIdx.x & 31;
-    int32_t L[kTreeletLeaves], internals[kTreeletLeaves - 1];
-    int nl = 0, ni = 0;
-    L[nl++] = child_word(nodes, N, 0);
-    L[nl++] = child_word(nodes, N, 1);
+    int32_t internals[kTreeletLeaves - 1];
+    int nl = 2, ni = 0;
+    int32_t mine = lane < 2 ? child_word(nodes, N, lane) : 0;  // entry `lane` of the treelet
     internals[ni++] = N;
     bool bad = false;
     while (nl < kTreeletLeaves) {
-        int pick = -1;
-        float pa = -1.0f;
-        for (int i = 0; i < nl; ++i)
-            if (!(L[i] & kLeaf)) {
-                const float a = tbox_area(tbox_of(nodes, leafbox, L[i]));
-                if (a > pa) {
-                    pa = a;
-                    pick = i;
-                }
+        float a = -1.0f;
+        if (lane < nl && !(mine & kLeaf)) a = tbox_area(tbox_of(nodes, leafbox, mine));
+        float ba = a;
+        int bi = lane;
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oa = __shfl_xor_sync(0xffffffffu, ba, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (oa > ba || (oa == ba && oi < bi)) {
+                ba = oa;
+                bi = oi;
             }
-        if (pick < 0) break;
-        const int32_t c = L[pick];
+        }
+        if (ba < 0.0f) break;  // no internal entry left
+        const int32_t c = __shfl_sync(0xffffffffu, mine, bi);
         if ((uint32_t)c >= (uint32_t)(n - 1)) {  // never for a sound tree
             bad = true;
             break;
         }
         internals[ni++] = c;
-        L[pick] = child_word(nodes, c, 0);
-        L[nl++] = child_word(nodes, c, 1);
+        if (lane == bi) mine = child_word(nodes, c, 0);
+        if (lane == nl) mine = child_word(nodes, c, 1);
+        ++nl;
     }
-    for (int i = 0; i < nl; ++i)
-        if ((L[i] & kLeaf) ? (L[i] & kSlotMask) >= n : (uint32_t)L[i] >= (uint32_t)(n - 1)) bad = true;
+    const bool my_bad = lane < nl && ((mine & kLeaf) ? (mine & kSlotMask) >= n : (uint32_t)mine >= (uint32_t)(n - 1));
+    if (__any_sync(0xffffffffu, my_bad)) bad = true;
     if (bad || nl < 3) return;  // the same decision in every lane
     const int full = (1 << nl) - 1;
     TBox bx[kTreeletLeaves];
-    for (int i = 0; i < nl; ++i) bx[i] = tbox_of(nodes, leafbox, L[i]);
+    {
+        TBox b{};
+        if (lane < nl) b = tbox_of(nodes, leafbox, mine);
+        for (int i = 0; i < nl; ++i)
+            for (int ax = 0; ax < 3; ++ax) {
+                bx[i].lo[ax] = __shfl_sync(0xffffffffu, b.lo[ax], i);
+                bx[i].hi[ax] = __shfl_sync(0xffffffffu, b.hi[ax], i);
+            }
+    }
     for (int S = 1 + lane; S <= full; S += 32)
         if ((S & (S - 1)) == 0) {
             cost[S] = 0.0f;
@@ -437,15 +451,15 @@ __device__ void restructure_treelet_warp(int32_t N, int n, float4* nodes, int32_
         for (int S = 1 + lane; S <= full; S += 32) {
             if (__popc(S) != k) continue;
             TBox u;
-            for (int a = 0; a < 3; ++a) {
-                u.lo[a] = INFINITY;
-                u.hi[a] = -INFINITY;
+            for (int ax = 0; ax < 3; ++ax) {
+                u.lo[ax] = INFINITY;
+                u.hi[ax] = -INFINITY;
             }
             for (int i = 0; i < nl; ++i)
                 if (S >> i & 1)
-                    for (int a = 0; a < 3; ++a) {
-                        u.lo[a] = fminf(u.lo[a], bx[i].lo[a]);
-                        u.hi[a] = fmaxf(u.hi[a], bx[i].hi[a]);
+                    for (int ax = 0; ax < 3; ++ax) {
+                        u.lo[ax] = fminf(u.lo[ax], bx[i].lo[ax]);
+                        u.hi[ax] = fmaxf(u.hi[ax], bx[i].hi[ax]);
                     }
             const float area = tbox_area(u);
             const int low = S & -S, rest = S ^ low;
@@ -465,9 +479,20 @@ __device__ void restructure_treelet_warp(int32_t N, int n, float4* nodes, int32_
         }
     }
     __syncwarp();
+    // the treelet's current internal area, summed in the same order as a
+    // single thread would (internals[0], [1], ...)
+    float my_area = 0.0f;
+    {
+        int32_t my_int = 0;
+        for (int i = 0; i < ni; ++i)
+            if (lane == i) my_int = internals[i];
+        if (lane < ni) my_area = tbox_area(tbox_of(nodes, leafbox, my_int));
+    }
     float current = 0.0f;
-    for (int i = 0; i < ni; ++i) current = current + tbox_area(tbox_of(nodes, leafbox, internals[i]));
+    for (int i = 0; i < ni; ++i) current = current + __shfl_sync(0xffffffffu, my_area, i);
     const bool better = cost[full] < current;
+    int32_t L[kTreeletLeaves];
+    for (int i = 0; i < nl; ++i) L[i] = __shfl_sync(0xffffffffu, mine, i);
     __syncwarp();
     if (better && lane == 0) {
         // order[i]: the subset of the i-th internal node in depth-first
@@ -496,22 +521,23 @@ __device__ void restructure_treelet_warp(int32_t N, int n, float4* nodes, int32_
             const int S = order[i];
             const int32_t me = internals[i];
             const int32_t l = word(split[S]), r = word(S ^ split[S]);
-            nodes[2 * me].w = __int_as_float(l);
-            nodes[2 * me + 1].w = __int_as_float(r);
+            TBox u;
+            for (int ax = 0; ax < 3; ++ax) {
+                u.lo[ax] = INFINITY;
+                u.hi[ax] = -INFINITY;
+            }
+            for (int j = 0; j < nl; ++j)
+                if (S >> j & 1)
+                    for (int ax = 0; ax < 3; ++ax) {
+                        u.lo[ax] = fminf(u.lo[ax], bx[j].lo[ax]);
+                        u.hi[ax] = fmaxf(u.hi[ax], bx[j].hi[ax]);
+                    }
+            nodes[2 * me] = make_float4(u.lo[0], u.lo[1], u.lo[2], __int_as_float(l));
+            nodes[2 * me + 1] = make_float4(u.hi[0], u.hi[1], u.hi[2], __int_as_float(r));
             if (l & kLeaf) parent_leaf[l & kSlotMask] = me;
             else parent_int[l] = me;
             if (r & kLeaf) parent_leaf[r & kSlotMask] = me;
             else parent_int[r] = me;
-        }
-        for (int i = no - 1; i >= 0; --i) {
-            const int32_t me = internals[i];
-            const TBox bl = tbox_of(nodes, leafbox, child_word(nodes, me, 0));
-            const TBox br = tbox_of(nodes, leafbox, child_word(nodes, me, 1));
-            const int32_t lw = child_word(nodes, me, 0), rw = child_word(nodes, me, 1);
-            nodes[2 * me] = make_float4(fminf(bl.lo[0], br.lo[0]), fminf(bl.lo[1], br.lo[1]),
-                                        fminf(bl.lo[2], br.lo[2]), __int_as_float(lw));
-            nodes[2 * me + 1] = make_float4(fmaxf(bl.hi[0], br.hi[0]), fmaxf(bl.hi[1], br.hi[1]),
-                                            fmaxf(bl.hi[2], br.hi[2]), __int_as_float(rw));
         }
     }
     // lane 0's rewiring is published before any lane moves on (the arrival
