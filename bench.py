@@ -74,8 +74,18 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # count).  dram_b_per_seg = (dram__bytes_read.sum + dram__bytes_write.sum) /
 # segments; lanes_per_inst = smsp__thread_inst_executed_per_inst_executed.ratio
 # (active lanes per issued instruction, all instructions).  `sha` is
-# kernel_sources_sha() of the captured build.
-NCU_FIGURES = {"sha": None, "figures": {}}
+# kernel_sources_sha() of the captured build.  Each figure is summed over the
+# k_trace_shade (and, for variant 3, k_traverse) launches of two renders of
+# `bench.py --config <c> --spp <s> --profile-render --tuning <variant>`
+# (c2: 4 spp, c3: 2 spp, c1: its own 16 spp) under ncu --metrics
+# dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
+# smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
+NCU_FIGURES = {"sha": "9410bd96f961f749", "commit": "635a4cb", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.71, "lanes_per_inst": 13.32, "warp_inst_per_seg": 94.8},
+    "c3/v3": {"dram_b_per_seg": 59.87, "lanes_per_inst": 6.19, "warp_inst_per_seg": 693.9},
+    "c3/v2": {"dram_b_per_seg": 126.51, "lanes_per_inst": 6.07, "warp_inst_per_seg": 755.3},
+    "c1/v2": {"dram_b_per_seg": 39.04, "lanes_per_inst": 10.92, "warp_inst_per_seg": 127.5},
+}}
 
 
 def kernel_sources_sha() -> str:
@@ -767,7 +777,9 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
         "dram_bytes_per_segment": fig["dram_b_per_seg"] if fig else None,
         "dram_frac": dram_frac,
         "lanes_per_inst_ncu": fig["lanes_per_inst"] if fig else None,
-        "ncu_kernel_sources_sha": NCU_FIGURES["sha"], "kernel_sources_sha": sha,
+        "warp_inst_per_segment_ncu": fig["warp_inst_per_seg"] if fig else None,
+        "ncu_kernel_sources_sha": NCU_FIGURES["sha"], "ncu_commit": NCU_FIGURES["commit"],
+        "kernel_sources_sha": sha,
         "ncu_note": None if fig else ("no ncu figures for these kernel sources and this variant: traffic, "
                                       "dram_frac and lanes_per_inst_ncu are null"),
         "kernel_share": stp["traverse_ms"] / max(1e-9, ms / steps),

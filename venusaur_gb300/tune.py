@@ -149,3 +149,74 @@ def autotune_jobs(jobs, pools=(16 << 20, 32 << 20, 64 << 20), blocks=(64, 128, 2
                 best_batch = (ms, dict(pool_paths=pool, traverse_block=tb))
         b.close()
     return best_plain[1], best_batch[1], results
+
+
+def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5), blocks=(128, 256), reps=3):
+    """Times every traversal variant x block shape on one render (the mean
+    of `reps` renders after a warm-up) and, per variant, a counting render:
+    box and sphere tests per segment, traversal steps per segment and the
+    SIMD utilisation of the traversal loop.  Also checks that every setting
+    gives the same accumulator.  Returns a list of dicts."""
+    import torch
+
+    out, ref = [], None
+    accum = new_accum(W, H)
+    for v in variants:
+        for tb in blocks:
+            wf = Wavefront(min(256 << 20, W * H * spp))
+            wf.set_tuning(traverse_variant=v, traverse_block=tb)
+            rate, ms = time_render(wf, scene, cam, W, H, spp, depth, accum, reps)
+            same = None
+            if ref is None:
+                ref = accum.clone()
+            else:
+                same = bool(torch.equal(ref, accum))
+            wf.close()
+            out.append(dict(traverse_variant=v, traverse_block=tb, segments_per_s=rate, ms=ms, identical=same))
+        wf = Wavefront(min(256 << 20, W * H * spp), count=True)
+        wf.set_tuning(traverse_variant=v, traverse_block=blocks[0])
+        wf.render(scene, cam, W, H, spp, accum, subframe=1 + reps, max_depth=depth, reset=True)
+        torch.cuda.synchronize()
+        st = wf.stats()
+        wf.close()
+        seg = max(1, st["segments"])
+        out.append(dict(traverse_variant=v, counting=True, boxes_per_segment=st["nodes_visited"] / seg,
+                        spheres_per_segment=st["spheres_tested"] / seg, steps_per_segment=st["lane_steps"] / seg,
+                        simd_utilization=st["lane_steps"] / max(1, 32 * st["warp_steps"])))
+    return out
+
+
+def main(argv=None) -> None:
+    """python -m venusaur_gb300.tune --scene rtiow|random [--n N --seed S]
+    --width W --height H --spp K [--variants 2,3,4,5] [--blocks 128,256]:
+    prints compare()'s rows as JSON lines (one GPU, the current device)."""
+    import argparse
+    import json
+
+    from .core import Camera, generate_random, generate_rtiow
+
+    ap = argparse.ArgumentParser(prog="python -m venusaur_gb300.tune")
+    ap.add_argument("--scene", choices=("rtiow", "random"), default="rtiow")
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=8)
+    ap.add_argument("--depth", type=int, default=50)
+    ap.add_argument("--variants", default="2,3,4,5")
+    ap.add_argument("--blocks", default="128,256")
+    a = ap.parse_args(argv)
+    sp = generate_rtiow(a.seed) if a.scene == "rtiow" else generate_random(a.n, a.seed)
+    eye = (13.0, 2.0, 3.0) if a.scene == "rtiow" else (60.0, 15.0, 60.0)
+    cam = Camera.look_at(eye, (0.0, 0.0, 0.0), 20.0, a.width / a.height, 0.1, 10.0)
+    ds = DeviceScene(sp)
+    info = ds.info()
+    print(json.dumps(dict(scene=a.scene, spheres=len(sp), width=a.width, height=a.height, spp=a.spp,
+                          build_ms=info["build_ms"], wide_nodes=info["num_wide_nodes"], wide_ms=info["wide_ms"])))
+    for row in compare(ds, cam, a.width, a.height, a.spp, a.depth, [int(x) for x in a.variants.split(",")],
+                       [int(x) for x in a.blocks.split(",")]):
+        print(json.dumps(row), flush=True)
+
+
+if __name__ == "__main__":
+    main()
