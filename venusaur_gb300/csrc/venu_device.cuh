@@ -27,10 +27,12 @@
 #define VENU_TRACE_MAXREG 64
 #endif
 #define VENU_TRACE_BOUNDS __maxnreg__(VENU_TRACE_MAXREG)
-// Register cap of the fused kernel over the 8-wide tree: its step holds a
-// node's 8 sort keys and half a node of boxes, and spills heavily at 64.
+// Register cap of the fused kernel over the wide tree.  With 4 children per
+// node, 64 registers (8 resident 128-thread blocks per SM, a few spilled
+// bytes) beat 72 and 80 (6 and 5 blocks) on RTIOW (+5 %) and 1M spheres
+// (+7 %), and lose 3 % on 5k spheres.
 #ifndef VENU_WIDE_MAXREG
-#define VENU_WIDE_MAXREG 80
+#define VENU_WIDE_MAXREG 64
 #endif
 #define VENU_WIDE_BOUNDS __maxnreg__(VENU_WIDE_MAXREG)
 // The multi-job kernel of the batch engine keeps a per-ray scene view.
