@@ -155,18 +155,14 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
     if (COUNT) flush_counters(K, stats);
 }
 
-// One warp-batch loop of the fused kernel.  IN_PLACE (a launch with no more
-// rays than the grid has threads): each path is finished in place, bounce
-// after bounce, instead of going through the next queue (whose launches then
-// find no rays); the output queue is unused then, and its throughput slot i
-// carries ray i's state between bounces.  A separate instantiation, so the
-// ordinary loop keeps its registers.
-template <bool COUNT, bool IN_PLACE, int KS, bool WIDE>
+// One warp-batch loop of the fused kernel: each warp takes 32 rays, traces
+// and shades them, and appends the continuing paths to the next queue.
+template <bool COUNT, int KS, bool WIDE>
 __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue& qin, uint32_t n,
                                                  uint32_t* __restrict__ work, const Queue& qout,
                                                  uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                  const PrimaryGen& gen, const DevCamera& cam, StackSmem sm,
-                                                 bool& overflow, TraceCounters& K, uint32_t& extra) {
+                                                 bool& overflow, TraceCounters& K) {
     const uint32_t lane = threadIdx.x & 31;
     for (;;) {
         uint32_t base = 0;
@@ -188,21 +184,12 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
                 d4 = qin.d[i];
             }
             slot = (uint32_t)__float_as_int(o4.w);
-            for (bool first = true;; first = false) {
-                RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-                float t;
-                const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x,
-                                                                 overflow, K);
-                const float4 t4 = (IN_PLACE && !first) ? qout.t[i]
-                                  : gen.path_seeds     ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
-                                                       : qin.t[i];
-                r = shade_one(S, o4, d4, t4, make_int2(__float_as_int(t), k));
-                if (!IN_PLACE || !r.cont) break;
-                o4 = r.o;
-                d4 = r.d;
-                qout.t[i] = r.t;
-                ++extra;
-            }
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float t;
+            const int32_t k =
+                trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
+            const float4 t4 = gen.path_seeds ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
+            r = shade_one(S, o4, d4, t4, make_int2(__float_as_int(t), k));
         }
         const uint32_t pos = warp_append(r.cont, cnt_out);
         if (r.cont) {
@@ -211,6 +198,80 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
             qout.t[pos] = r.t;
         } else if (valid) {
             slots[slot] = r.result;
+        }
+    }
+}
+
+// The in-place launch (no more rays than the grid has threads): block b
+// takes rays [b * blockDim, (b + 1) * blockDim) and finishes them bounce by
+// bounce.  Between bounces the block's surviving paths are compacted to its
+// first threads (their state staged through the unused output queue, at the
+// block's own positions), so its warps stay full while paths end at
+// different bounces instead of idling around the few long paths.  Each path
+// goes through exactly the same arithmetic as in the ordinary loop; only
+// the thread that runs it changes.
+template <bool COUNT, int KS, bool WIDE>
+__device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Queue& qin, uint32_t n,
+                                                     const Queue& qout, float4* __restrict__ slots,
+                                                     const PrimaryGen& gen, const DevCamera& cam, StackSmem sm,
+                                                     bool& overflow, TraceCounters& K, uint32_t& extra) {
+    __shared__ uint32_t warp_live[32];
+    const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+    const uint32_t base = blockIdx.x * blockDim.x;
+    const uint32_t i = base + t;  // this thread's state lives at i
+    bool live = i < n;
+    float4 o4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), d4 = o4;
+    if (live) {
+        uint32_t seed = 0;
+        if (gen.path_seeds) {
+            gen_primary(gen, cam, i, o4, d4, seed);
+            qout.t[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
+        } else {
+            o4 = qin.o[i];
+            d4 = qin.d[i];
+            qout.t[i] = qin.t[i];
+        }
+    }
+    uint32_t held = (uint32_t)__syncthreads_count(live);  // threads holding a state, from thread 0 on
+    for (bool first = true;; first = false) {
+        const uint32_t cnt = (uint32_t)__syncthreads_count(live);
+        if (cnt == 0) break;
+        if (cnt < held) {
+            // compaction: the live states to threads [0, cnt)
+            const uint32_t m = __ballot_sync(0xffffffffu, live);
+            if (lane == 0) warp_live[w] = (uint32_t)__popc(m);
+            float4 t4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (live) t4 = qout.t[i];
+            __syncthreads();
+            uint32_t pos = (uint32_t)__popc(m & ((1u << lane) - 1u));
+            for (uint32_t v = 0; v < w; ++v) pos += warp_live[v];
+            if (live) {
+                qout.o[base + pos] = o4;
+                qout.d[base + pos] = d4;
+                qout.t[base + pos] = t4;
+            }
+            __syncthreads();
+            live = t < cnt;
+            if (live) {
+                o4 = qout.o[i];
+                d4 = qout.d[i];
+            }
+            held = cnt;
+        }
+        if (live) {
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float th;
+            const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, th, sm, t, blockDim.x, overflow, K);
+            const ShadeOut r = shade_one(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
+            if (!first) ++extra;
+            if (r.cont) {
+                o4 = r.o;
+                d4 = r.d;
+                qout.t[i] = r.t;
+            } else {
+                slots[(uint32_t)__float_as_int(o4.w)] = r.result;
+                live = false;
+            }
         }
     }
 }
@@ -243,13 +304,11 @@ __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue
     bool overflow = false;
     uint32_t extra = 0;  // segments traced in place after a ray's first
     if (n <= gridDim.x * blockDim.x) {
-        trace_shade_loop<COUNT, true, KS, WIDE>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K,
-                                                extra);
+        trace_shade_in_place<COUNT, KS, WIDE>(S, qin, n, qout, slots, gen, cam, sm, overflow, K, extra);
         for (int off = 16; off > 0; off >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, off);
         if (lane == 0 && extra) atomicAdd(stats, (unsigned long long)extra);
     } else {
-        trace_shade_loop<COUNT, false, KS, WIDE>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K,
-                                                 extra);
+        trace_shade_loop<COUNT, KS, WIDE>(S, qin, n, work, qout, cnt_out, slots, gen, cam, sm, overflow, K);
     }
     if (overflow) atomicOr(err, 1u);
     if (COUNT) flush_counters(K, stats);
