@@ -80,11 +80,14 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # (c2: 4 spp, c3: 2 spp, c1: its own 16 spp) under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "9410bd96f961f749", "commit": "635a4cb", "figures": {
-    "c2/v2": {"dram_b_per_seg": 62.71, "lanes_per_inst": 13.32, "warp_inst_per_seg": 94.8},
-    "c3/v3": {"dram_b_per_seg": 59.87, "lanes_per_inst": 6.19, "warp_inst_per_seg": 693.9},
-    "c3/v2": {"dram_b_per_seg": 126.51, "lanes_per_inst": 6.07, "warp_inst_per_seg": 755.3},
-    "c1/v2": {"dram_b_per_seg": 39.04, "lanes_per_inst": 10.92, "warp_inst_per_seg": 127.5},
+NCU_FIGURES = {"sha": "37e5dc735d5278dc", "commit": "82e234c", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.4, "lanes_per_inst": 14.25, "warp_inst_per_seg": 89.1},
+    "c2/v4": {"dram_b_per_seg": 64.41, "lanes_per_inst": 16.96, "warp_inst_per_seg": 88.4},
+    "c1/v2": {"dram_b_per_seg": 37.71, "lanes_per_inst": 13.25, "warp_inst_per_seg": 109.2},
+    "c1/v4": {"dram_b_per_seg": 42.27, "lanes_per_inst": 15.0, "warp_inst_per_seg": 110.8},
+    "c3/v3": {"dram_b_per_seg": 59.83, "lanes_per_inst": 6.19, "warp_inst_per_seg": 693.9},
+    "c3/v2": {"dram_b_per_seg": 125.34, "lanes_per_inst": 6.06, "warp_inst_per_seg": 755.2},
+    "c3/v5": {"dram_b_per_seg": 65.63, "lanes_per_inst": 8.1, "warp_inst_per_seg": 664.2},
 }}
 
 
