@@ -6,7 +6,8 @@
 // image size comes from the command line (the reference fixes 1200 wide at
 // 3:2).  Used by tests/test_cpp_dropin.py.
 //
-//   render_main <width> <height> <frames> <out.ppm> <out.rgba> [out.pfm]
+//   render_main <width> <height> <frames> <out.ppm> <out.rgba> [out.pfm] [zero_copy]
+//   render_main gl        (constructs a GL_INTEROP buffer: must throw, exit 0 if it does)
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -16,6 +17,14 @@
 using namespace venu_core;
 
 int main(int argc, char** argv) {
+    if (argc == 2 && std::string(argv[1]) == "gl") {
+        try {
+            CUDAOutputBuffer<uchar4> gl(CUDAOutputBufferType::GL_INTEROP, 4, 4);
+        } catch (const Exception& e) {
+            return e.status == VENU_ERR_INVALID ? 0 : 4;
+        }
+        return 5;
+    }
     if (argc < 6) {
         std::fprintf(stderr, "usage: %s W H frames out.ppm out.rgba [out.pfm]\n", argv[0]);
         return 2;
@@ -35,6 +44,19 @@ int main(int argc, char** argv) {
         Renderer optix_renderer;                                                 // Core/Core.cpp:31
         std::string ptxSource;  // no PTX: the kernels are in libvenusaur_gb300
         optix_renderer.Init(scene, ptxSource);  // Core/Core.cpp:246
+        const bool zero_copy = argc > 7 && std::string(argv[7]) == "zero_copy";
+        if (zero_copy) {  // the ZERO_COPY type: the pixels in mapped host memory
+            CUDAOutputBuffer<uchar4> zc(CUDAOutputBufferType::ZERO_COPY, image_width, image_height);
+            camera.SetForward(lookat - lookfrom);
+            for (int f = 0; f < frames; ++f) optix_renderer.Draw(camera, zc);
+            const uchar4* px = zc.getHostPointer();
+            FILE* g = std::fopen(argv[5], "wb");
+            if (!g) return 3;
+            std::fwrite(px, sizeof(uchar4), (size_t)image_width * image_height, g);
+            std::fclose(g);
+            optix_renderer.Cleanup();
+            return 0;
+        }
         CUDAOutputBuffer<uchar4> outputBuffer(CUDAOutputBufferType::CUDA_DEVICE, image_width, image_height);  // Core/Core.cpp:252
         camera.SetForward(lookat - lookfrom);  // Core/Core.cpp:353
         for (int f = 0; f < frames; ++f) {
