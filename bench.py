@@ -35,6 +35,7 @@ import argparse
 import hashlib
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -80,7 +81,7 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # (c2: 4 spp, c3: 2 spp, c1: its own 16 spp) under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "37e5dc735d5278dc", "commit": "82e234c", "figures": {
+NCU_FIGURES = {"sha": "40d7f87b59d5def3", "commit": "82e234c", "figures": {
     "c2/v2": {"dram_b_per_seg": 62.4, "lanes_per_inst": 14.25, "warp_inst_per_seg": 89.1},
     "c2/v4": {"dram_b_per_seg": 64.41, "lanes_per_inst": 16.96, "warp_inst_per_seg": 88.4},
     "c1/v2": {"dram_b_per_seg": 37.71, "lanes_per_inst": 13.25, "warp_inst_per_seg": 109.2},
@@ -92,10 +93,16 @@ NCU_FIGURES = {"sha": "37e5dc735d5278dc", "commit": "82e234c", "figures": {
 
 
 def kernel_sources_sha() -> str:
+    """Hash of the kernel code: the sources with comments removed and
+    whitespace collapsed, so that only a change of code invalidates the ncu
+    figures."""
     h = hashlib.sha256()
     for f in KERNEL_SOURCES:
-        with open(os.path.join(ROOT, f), "rb") as fh:
-            h.update(fh.read())
+        with open(os.path.join(ROOT, f), encoding="utf-8") as fh:
+            code = fh.read()
+        code = re.sub(r"/\*.*?\*/", " ", code, flags=re.S)
+        code = re.sub(r"//[^\n]*", " ", code)
+        h.update(" ".join(code.split()).encode())
     return h.hexdigest()[:16]
 
 

@@ -104,7 +104,7 @@ typedef struct venu_scene_info {
     uint64_t device_bytes;   /* resident bytes owned by the scene */
     float bounds[6];         /* centroid bounds used for Morton quantisation */
     float build_ms;          /* device time of the last LBVH build */
-    uint32_t num_wide_nodes; /* nodes of the 8-wide traversal tree collapsed from the LBVH */
+    uint32_t num_wide_nodes; /* nodes of the 4-wide traversal tree collapsed from the LBVH */
     float wide_ms;           /* wall time of that collapse (host-driven, level by level) */
 } venu_scene_info;
 

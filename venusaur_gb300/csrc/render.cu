@@ -50,7 +50,7 @@ __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, u
     seeds[pix] = seed;
 }
 
-// WIDE: over the 8-wide (or 4-wide) tree (variant 5's later bounces).
+// WIDE: over the 4-wide tree (variant 5's later bounces).
 template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                   uint32_t* __restrict__ work, int2* __restrict__ hits,
@@ -280,7 +280,7 @@ __device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Q
 // then shades all 32 together once the warp has reconverged and appends the
 // continuing paths with one ballot and one atomic.  Saves the hit record
 // round trip, the second read of the rays and one launch per bounce.
-// WIDE: the 8-wide tree instead of the binary traversal layout (variant 4,
+// WIDE: the 4-wide tree instead of the binary traversal layout (variant 4,
 // k_trace_shade_wide, with its own register cap).
 template <bool COUNT, int KS, bool WIDE>
 __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue& qin,
@@ -478,7 +478,7 @@ cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
     const size_t sm = traverse_smem((int)t.traverse_block);
     cudaError_t e;
-    if (t.traverse_variant == 4) {  // the fused kernel over the 8-wide tree
+    if (t.traverse_variant == 4) {  // the fused kernel over the 4-wide tree
         e = occupancy_grid(k_trace_shade_wide<false, kShared>, (int)t.traverse_block, sm,
                            t.traverse_blocks_per_sm, r->fused_blocks);
         if (e == cudaSuccess)

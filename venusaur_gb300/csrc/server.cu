@@ -79,8 +79,8 @@ constexpr uint32_t kBulkChunk = 4u << 20;      // bulk rays per step while the e
 
 // Device bytes of a scene of n spheres, for admission before it is built:
 // binary nodes 32 + traversal records 64 + spheres, materials 32 + meta,
-// keys 8 + parent links 8 bytes per sphere, and the 8-wide tree (at most
-// about one node of 256 + 32 bytes per three spheres).  Once built, the
+// keys 8 + parent links 8 bytes per sphere, and the 4-wide tree (about one
+// node of 128 + 16 bytes per two spheres).  Once built, the
 // scene's own byte count replaces the estimate.
 uint64_t scene_estimate(uint32_t n) { return (uint64_t)n * 240u + 4096u; }
 uint64_t image_bytes(const venu_render_opts& o) {

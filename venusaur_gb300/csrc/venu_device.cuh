@@ -232,7 +232,7 @@ static_assert(kWideW == 4 || kWideW == 8, "the wide tree has 4 or 8 children per
 struct SceneView {
     const float4* __restrict__ nodes;  // 2 float4 per internal node: {lo, left} {hi, right}
     const float4* __restrict__ trav;   // 4 float4 per internal node: both children, see lbvh.cu
-    const float4* __restrict__ wide;   // 16 float4 per node of the 8-wide tree, see lbvh.cu
+    const float4* __restrict__ wide;   // kWideF4 float4 per node of the wide tree, see lbvh.cu
     const float4* __restrict__ sph;    // {center, radius} per slot
     const float4* __restrict__ mat;    // {albedo, fuzz or ir} per slot
     const uint32_t* __restrict__ meta; // original id | material << 30
