@@ -906,14 +906,21 @@ venu_status build_wide(venu_scene* S, cudaStream_t st) {
     WSTEP(cudaMemsetAsync(flag, 0x01, 1, st));  // the root
     WSTEP(cudaMemsetAsync(fa, 0, sizeof(int32_t), st));
     {
+        // a binary tree over n leaves has fewer than n levels, and each level
+        // of the collapse takes at least one of them
         uint32_t nin = 1;
-        for (int level = 0; nin > 0 && level < 256; ++level) {
+        for (uint32_t level = 0; nin > 0 && level < n; ++level) {
             WSTEP(cudaMemsetAsync(cnt, 0, sizeof(uint32_t), st));
             k_wide_frontier<<<cdiv(nin, 128), 128, 0, st>>>(S->nodes, fa, nin, fb, cnt, flag);
             WSTEP(cudaGetLastError());
             WSTEP(cudaMemcpyAsync(&nin, cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
             WSTEP(cudaStreamSynchronize(st));
             std::swap(fa, fb);
+        }
+        if (nin > 0) {  // a cyclic (corrupt) binary tree: no wide tree
+            set_error("venu_scene_create: the wide-tree collapse did not end");
+            rc = VENU_ERR_INVALID;
+            goto wdone;
         }
     }
     WSTEP(cudaMemcpyAsync(idx, flag, sizeof(uint32_t) * nint, cudaMemcpyDeviceToDevice, st));
