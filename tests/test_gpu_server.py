@@ -154,3 +154,29 @@ def test_server_progressive_session(venu, oracle, cuda):
     assert np.array_equal(r["image"], want["image8"].reshape(r["image"].shape))
     assert srv.stats()["failed"] == 0
     srv.close()
+
+
+def test_server_lru_eviction_counted(venu, oracle, cuda):
+    """A budget with room for one resident scene and one small job: a second
+    keyed scene evicts the first (least recently used, unreferenced), the
+    first's key is then no longer resident (a request relying on it fails
+    with VENU_ERR_INVALID and succeeds when the spheres are sent again), and
+    the server counts the evictions and the peak of resident bytes."""
+    sp0, cam, want0 = _case(oracle, 0, 24, 16, 2)
+    sp1, _, want1 = _case(oracle, 1, 24, 16, 2)
+    job = venu.Batch.job_bytes(24, 16, 2) + 24 * 16 * 36
+    scene = 488 * 240 + 4096  # the server's estimate of an RTIOW scene, above its built size
+    srv = venu.Server(hbm_budget_bytes=job + scene + 1024, pool_paths=1000, max_jobs=4, iterations_per_step=2)
+    r = srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp0, scene_key=1, max_depth=6))
+    assert r["status"] == 0 and np.array_equal(r["image"], want0["image8"].reshape(r["image"].shape))
+    r = srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp1, scene_key=2, max_depth=6))
+    assert r["status"] == 0 and np.array_equal(r["image"], want1["image8"].reshape(r["image"].shape))
+    st = srv.stats()
+    assert st["evictions"] >= 1
+    assert 0 < st["peak_resident_bytes"] <= st["budget_bytes"]
+    r = srv.wait(srv.submit(cam, 24, 16, 2, spheres=None, scene_key=1, max_depth=6))
+    assert r["status"] == 1  # VENU_ERR_INVALID: key 1 was evicted
+    r = srv.wait(srv.submit(cam, 24, 16, 2, spheres=sp0, scene_key=1, max_depth=6))
+    assert r["status"] == 0 and np.array_equal(r["image"], want0["image8"].reshape(r["image"].shape))
+    assert srv.stats()["evictions"] >= 2
+    srv.close()
