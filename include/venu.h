@@ -299,6 +299,9 @@ typedef struct venu_tuning {
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
     uint32_t shade_block;            /* threads per shade block: 64..512, multiple of 32 */
     uint32_t shade_blocks_per_sm;    /* 0 = as many as fit */
+    uint32_t in_place_factor;        /* fused variants: a launch with at most this many rays per
+                                        thread of its grid finishes its paths in place, bounce
+                                        after bounce, refilling finished threads (1..16; 0 = 1) */
 } venu_tuning;
 VENU_API venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tuning* t);
 VENU_API venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tuning* t);

@@ -280,6 +280,8 @@ def test_empty_and_tiny_scenes(venu, oracle, cuda):
     dict(traverse_variant=4, refill_min=32, traverse_block=64, shade_block=256, traverse_blocks_per_sm=3),
     dict(traverse_variant=5, refill_min=8, traverse_block=128, shade_block=256),
     dict(traverse_variant=5, refill_min=1, traverse_block=256, shade_block=128, traverse_blocks_per_sm=2),
+    dict(traverse_variant=2, refill_min=32, traverse_block=128, shade_block=256, in_place_factor=8),
+    dict(traverse_variant=4, refill_min=32, traverse_block=64, shade_block=256, in_place_factor=16),
 ])
 def test_render_tunings_bit_exact(venu, oracle, cuda, tuning):
     """Launch shapes and traversal variants change speed, never bits."""
@@ -387,3 +389,28 @@ def test_deep_stack_spills_bit_exact(venu, oracle, cuda, n, levels, rfrac, ks, v
     want = oracle.render(sp, cam, W, H, spp, subframe=1, max_depth=6, mode=pyoracle.MODE_GB300)
     assert np.array_equal(acc.cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
     assert st["segments"] == want["segments"]
+
+
+@pytest.mark.parametrize("scene", ["rtiow", "random"])
+def test_in_place_refill_bit_exact(venu, oracle, cuda, scene):
+    """Launches with more rays than the grid has threads finished in place
+    (in_place_factor 8: blocks take rays with an atomic, compact their
+    survivors and refill finished threads between bounces) give the same
+    accumulator and segment count as the oracle."""
+    torch = cuda
+    if scene == "rtiow":
+        sp, eye = oracle.scene_rtiow(0), (13, 2, 3)
+    else:
+        sp, eye = oracle.scene_random(20_000, 3), (60, 15, 60)
+    W, H, spp, depth = 400, 225, 4, 12  # 360 k paths: more than the grid's threads, fewer than 8x
+    cam = oracle.camera(eye, (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    ds = venu.DeviceScene(sp)
+    want = oracle.render(sp, cam, W, H, spp, subframe=1, max_depth=depth, mode=pyoracle.MODE_GB300)
+    for variant in (2, 4):
+        wf = venu.Wavefront(0)
+        wf.set_tuning(traverse_variant=variant, traverse_block=128, in_place_factor=8)
+        acc = venu.new_accum(W, H)
+        wf.render(ds, cam, W, H, spp, acc, subframe=1, max_depth=depth, reset=True)
+        torch.cuda.synchronize()
+        assert np.array_equal(acc.cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
+        assert wf.stats()["segments"] == want["segments"]

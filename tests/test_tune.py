@@ -10,8 +10,9 @@ from venusaur_gb300 import tune
 def test_candidate_space():
     c = list(tune.candidates())
     # variant 1 x refill {4,8,16} x traverse block {64,128,256} x shade {128,256},
-    # variants 0, 3 and 5 x traverse block x shade block, variants 2 and 4 x traverse block
-    assert len(c) == 3 * 3 * 2 + 3 * 3 * 2 + 2 * 3
+    # variants 0, 3 and 5 x traverse block x shade block, variants 2 and 4 x
+    # traverse block x in-place factor
+    assert len(c) == 3 * 3 * 2 + 3 * 3 * 2 + 2 * 3 * 2
     assert len({tuple(sorted(x.items())) for x in c}) == len(c)
     for x in c:
         assert x["traverse_variant"] in (0, 1, 2, 3, 4, 5)
@@ -19,7 +20,9 @@ def test_candidate_space():
             assert x["refill_min"] == 32
         if x["traverse_variant"] in (2, 4):
             assert x["shade_block"] == 256
-    small = list(tune.candidates({"traverse_variant": (2,), "traverse_block": (128,)}))
+        else:
+            assert x["in_place_factor"] == 1
+    small = list(tune.candidates({"traverse_variant": (2,), "traverse_block": (128,), "in_place_factor": (1,)}))
     assert len(small) == 1
     v5 = list(tune.candidates({"traverse_variant": (5,)}))
     assert len(v5) == 3 * 2 and all(x["traverse_variant"] == 5 for x in v5)
@@ -32,7 +35,8 @@ def test_autotune_render_and_jobs(venu, oracle, cuda):
     sp = oracle.scene_rtiow(0)
     cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
     ds = venu.DeviceScene(sp)
-    space = {"traverse_variant": (0, 2), "refill_min": (8,), "traverse_block": (64, 256), "shade_block": (256,)}
+    space = {"traverse_variant": (0, 2), "refill_min": (8,), "traverse_block": (64, 256), "shade_block": (256,),
+             "in_place_factor": (1,)}
     best, mp, res = tune.autotune(ds, cam, W, H, spp, depth, space=space, max_paths=(1 << 20,))
     assert mp == 1 << 20 and len(res) == 4
     assert best in [{k: v for k, v in r.items() if k in best} for r in res]

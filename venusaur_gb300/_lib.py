@@ -63,7 +63,7 @@ class RenderStats(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("traverse_variant", C.c_uint32), ("refill_min", C.c_uint32), ("traverse_block", C.c_uint32),
                 ("traverse_blocks_per_sm", C.c_uint32), ("shade_block", C.c_uint32),
-                ("shade_blocks_per_sm", C.c_uint32)]
+                ("shade_blocks_per_sm", C.c_uint32), ("in_place_factor", C.c_uint32)]
 
 
 class CameraC(C.Structure):

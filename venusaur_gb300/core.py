@@ -17,7 +17,7 @@ from . import _lib
 from ._lib import CAMERA_DTYPE, NODE_DTYPE, SPHERE_DTYPE, RenderOpts, RenderStats, SceneInfo, Tuning, check, lib, ptr
 
 TUNING_FIELDS = ("traverse_variant", "refill_min", "traverse_block", "traverse_blocks_per_sm", "shade_block",
-                 "shade_blocks_per_sm")
+                 "shade_blocks_per_sm", "in_place_factor")
 
 
 def _torch():
@@ -545,7 +545,7 @@ class Batch:
 
     def set_tuning(self, **kw) -> None:
         base = dict(traverse_variant=2, refill_min=8, traverse_block=256, traverse_blocks_per_sm=0,
-                    shade_block=256, shade_blocks_per_sm=0)
+                    shade_block=256, shade_blocks_per_sm=0, in_place_factor=1)
         base.update(kw)
         t = Tuning(*(int(base[f]) for f in TUNING_FIELDS))
         check(lib().venu_batch_set_tuning(self.handle, C.byref(t)))

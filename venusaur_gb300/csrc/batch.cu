@@ -462,7 +462,7 @@ struct venu_batch {
     uint64_t next_seq = 0;
     uint32_t* h_interrupt = nullptr;  // mapped host word
     uint32_t* d_interrupt = nullptr;  // its device address
-    venu_tuning tune = {2u, 8u, 256u, 0u, 256u, 0u};
+    venu_tuning tune = {2u, 8u, 256u, 0u, 256u, 0u, 1u};
     int trav_blocks = 0;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;

@@ -276,13 +276,114 @@ __device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Q
     }
 }
 
+// The in-place launch with refills (in_place_factor > 1, its own kernel
+// instantiation, REFILL): a launch with at most in_place_factor rays per
+// thread of the grid finishes every path it takes bounce after bounce
+// instead of appending survivors to the next queue.  A block takes rays from the launch
+// with one atomic per refill (the same dynamic hand-out as the ordinary
+// loop), and at each bounce boundary compacts its surviving paths to its
+// first threads (their state staged through the unused output queue) and
+// gives the threads behind them fresh rays, so its warps stay full while
+// paths end at different bounces.  Each path goes through exactly the same
+// arithmetic as in the ordinary loop; only the thread that runs it changes.
+// A block's staging positions are those of the first rays it took, base0 +
+// [0, blockDim): it never holds more paths than that first chunk had rays
+// (a short first chunk is the launch's last), so they stay inside the queue.
+// The factor is a tuning field (venu_tuning.in_place_factor): finishing in
+// place keeps the warps of a block in step bounce by bounce, which pays on
+// scenes with long, divergent paths and costs on short ones.
+
+template <bool COUNT, int KS, bool WIDE>
+__device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, const Queue& qin, uint32_t n,
+                                                     uint32_t* __restrict__ work, const Queue& qout,
+                                                     float4* __restrict__ slots, const PrimaryGen& gen,
+                                                     const DevCamera& cam, StackSmem sm, bool& overflow,
+                                                     TraceCounters& K, uint32_t& extra) {
+    __shared__ uint32_t warp_live[32];
+    __shared__ uint32_t s_base;
+    const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+    uint32_t base0 = 0xffffffffu;  // the block's staging positions start here (its first chunk)
+    uint32_t held = 0;             // threads [0, held) hold the block's paths
+    bool exhausted = false, live = false, first = false;
+    float4 o4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), d4 = o4;
+    for (;;) {
+        const uint32_t cnt = (uint32_t)__syncthreads_count(live);
+        if (cnt == 0 && exhausted) break;
+        if (cnt < held || (!exhausted && cnt < blockDim.x)) {
+            const uint32_t i = base0 + t;
+            if (cnt < held) {  // the live states to threads [0, cnt)
+                const uint32_t m = __ballot_sync(0xffffffffu, live);
+                if (lane == 0) warp_live[w] = (uint32_t)__popc(m);
+                float4 t4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (live) t4 = qout.t[i];
+                __syncthreads();
+                uint32_t pos = (uint32_t)__popc(m & ((1u << lane) - 1u));
+                for (uint32_t v = 0; v < w; ++v) pos += warp_live[v];
+                if (live) {
+                    qout.o[base0 + pos] = o4;
+                    qout.d[base0 + pos] = d4;
+                    qout.t[base0 + pos] = t4;
+                }
+                __syncthreads();
+                if (t < cnt) {
+                    o4 = qout.o[i];
+                    d4 = qout.d[i];
+                }
+            }
+            uint32_t take = 0, base = 0;
+            if (!exhausted) {  // fresh rays for threads [cnt, blockDim)
+                const uint32_t need = blockDim.x - cnt;
+                if (t == 0) s_base = atomicAdd(work, need);
+                __syncthreads();
+                base = s_base;
+                take = base < n ? min(need, n - base) : 0u;
+                exhausted = take < need;
+                if (base0 == 0xffffffffu) base0 = base;  // the first chunk (cnt == 0 then)
+            }
+            live = t < cnt + take;
+            first = t >= cnt && live;
+            if (first) {
+                const uint32_t ray = base + (t - cnt);
+                const uint32_t j = base0 + t;
+                if (gen.path_seeds) {
+                    uint32_t seed = 0;
+                    gen_primary(gen, cam, ray, o4, d4, seed);
+                    qout.t[j] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
+                } else {
+                    o4 = qin.o[ray];
+                    d4 = qin.d[ray];
+                    qout.t[j] = qin.t[ray];
+                }
+            }
+            held = cnt + take;
+        }
+        if (live) {
+            const uint32_t i = base0 + t;
+            RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+            float th;
+            const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, th, sm, t, blockDim.x, overflow, K);
+            const ShadeOut r = shade_one(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
+            if (!first) ++extra;
+            first = false;
+            if (r.cont) {
+                o4 = r.o;
+                d4 = r.d;
+                qout.t[i] = r.t;
+            } else {
+                slots[(uint32_t)__float_as_int(o4.w)] = r.result;
+                live = false;
+            }
+        }
+    }
+}
+
 // Traverse and shade in one pass: each warp takes 32 rays, traverses them,
 // then shades all 32 together once the warp has reconverged and appends the
 // continuing paths with one ballot and one atomic.  Saves the hit record
 // round trip, the second read of the rays and one launch per bounce.
 // WIDE: the 4-wide tree instead of the binary traversal layout (variant 4,
 // k_trace_shade_wide, with its own register cap).
-template <bool COUNT, int KS, bool WIDE>
+template <bool COUNT, int KS, bool WIDE, bool REFILL>
 __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue& qin,
                                                  const uint32_t* __restrict__ cnt_in, uint32_t* __restrict__ work,
                                                  const Queue& qout, uint32_t* __restrict__ cnt_out,
@@ -303,8 +404,12 @@ __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue
     TraceCounters K{0, 0};
     bool overflow = false;
     uint32_t extra = 0;  // segments traced in place after a ray's first
-    if (n <= gridDim.x * blockDim.x) {
-        trace_shade_in_place<COUNT, KS, WIDE>(S, qin, n, qout, slots, gen, cam, sm, overflow, K, extra);
+    if (n <= (REFILL ? gen.in_place_factor : 1u) * gridDim.x * blockDim.x) {
+        if (REFILL)
+            trace_shade_in_place_refill<COUNT, KS, WIDE>(S, qin, n, work, qout, slots, gen, cam, sm, overflow, K,
+                                                         extra);
+        else
+            trace_shade_in_place<COUNT, KS, WIDE>(S, qin, n, qout, slots, gen, cam, sm, overflow, K, extra);
         for (int off = 16; off > 0; off >>= 1) extra += __shfl_xor_sync(0xffffffffu, extra, off);
         if (lane == 0 && extra) atomicAdd(stats, (unsigned long long)extra);
     } else {
@@ -314,22 +419,25 @@ __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue
     if (COUNT) flush_counters(K, stats);
 }
 
-template <bool COUNT, int KS>
+// REFILL: launches of up to in_place_factor rays per thread finish in place
+// with refills (a separate instantiation, so the ordinary kernel keeps its
+// registers).
+template <bool COUNT, int KS, bool REFILL = false>
 __global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
                                                 uint32_t* __restrict__ work, Queue qout,
                                                 uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                 uint32_t* __restrict__ err, unsigned long long* __restrict__ stats,
                                                 PrimaryGen gen) {
-    trace_shade_body<COUNT, KS, false>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
+    trace_shade_body<COUNT, KS, false, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
 }
 
-template <bool COUNT, int KS>
+template <bool COUNT, int KS, bool REFILL = false>
 __global__ void VENU_WIDE_BOUNDS k_trace_shade_wide(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
                                                     uint32_t* __restrict__ work, Queue qout,
                                                     uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                     uint32_t* __restrict__ err,
                                                     unsigned long long* __restrict__ stats, PrimaryGen gen) {
-    trace_shade_body<COUNT, KS, true>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
+    trace_shade_body<COUNT, KS, true, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
 }
 
 __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
@@ -449,7 +557,7 @@ struct venu_renderer {
     uint32_t* work = nullptr;  // [65]
     uint32_t* err = nullptr;
     unsigned long long* stats = nullptr;  // segments, nodes, spheres
-    venu_tuning tune = {2u, 32u, 128u, 0u, 128u, 0u};
+    venu_tuning tune = {2u, 32u, 128u, 0u, 128u, 0u, 1u};
     int trav_blocks = 0, shade_blocks = 0, fused_blocks = 0;
     venu_render_stats last = {};
     // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
@@ -473,6 +581,11 @@ cudaError_t occupancy_grid(K kernel, int block, size_t smem, uint32_t per_sm_cap
     return cudaSuccess;
 }
 
+template <typename K>
+cudaError_t set_smem_refill(K kernel, size_t smem) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 // Persistent grids: as many resident blocks as fit (or the tuned cap) on every SM.
 cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
@@ -490,6 +603,10 @@ cudaError_t configure(venu_renderer* r) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_trace_shade_wide<true, kSharedShallow>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade_wide<false, kShared, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade_wide<true, kShared, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade_wide<false, kSharedShallow, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade_wide<true, kSharedShallow, true>, sm);
         if (e != cudaSuccess) return e;
         r->trav_blocks = r->fused_blocks;
     } else if (t.traverse_variant >= 2) {  // the fused kernel: every bounce (2), the primary one (3, 5)
@@ -504,6 +621,10 @@ cudaError_t configure(venu_renderer* r) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_trace_shade<true, kSharedShallow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade<false, kShared, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade<true, kShared, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade<false, kSharedShallow, true>, sm);
+        if (e == cudaSuccess) e = set_smem_refill(k_trace_shade<true, kSharedShallow, true>, sm);
         if (e != cudaSuccess) return e;
     }
     if (t.traverse_variant == 4) {
@@ -626,7 +747,7 @@ extern "C" venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tun
     const bool ok = t->traverse_variant <= 5u && t->refill_min >= 1u && t->refill_min <= 32u &&
                     (t->traverse_block == 64u || t->traverse_block == 128u || t->traverse_block == 256u) &&
                     t->shade_block >= 64u && t->shade_block <= 512u && (t->shade_block % 32u) == 0u &&
-                    t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u;
+                    t->traverse_blocks_per_sm <= 32u && t->shade_blocks_per_sm <= 32u && t->in_place_factor <= 16u;
     if (!ok) {
         set_error("venu_renderer_set_tuning: value out of range");
         return VENU_ERR_INVALID;
@@ -744,6 +865,7 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
             pg.depth = (int)maxd - 1;
             pg.div_P = make_fastdiv(PP);
             pg.div_W = make_fastdiv(W);
+            pg.in_place_factor = tu.in_place_factor ? tu.in_place_factor : 1u;
             ++launches;
             for (int b = 0; b < nb; ++b) {
                 const Queue& qi = r->q[b & 1];
@@ -767,9 +889,15 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                 if (v == 2 || v == 4) {
                     pg.path_seeds = (b == 0) ? path_seeds : nullptr;
                     const size_t fsm = shallow ? traverse_smem(tb, kSharedShallow) : tsm;
-#define VENU_FUSED(KERNEL, C, KS)                                                                      \
-    KERNEL<C, KS><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1, \
-                                                    r->slots, r->err, r->stats, pg)
+#define VENU_FUSED(KERNEL, C, KS)                                                                           \
+    do {                                                                                                     \
+        if (pg.in_place_factor > 1u)                                                                         \
+            KERNEL<C, KS, true><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,        \
+                                                                  r->cnt + b + 1, r->slots, r->err, r->stats, pg); \
+        else                                                                                                 \
+            KERNEL<C, KS, false><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,       \
+                                                                   r->cnt + b + 1, r->slots, r->err, r->stats, pg); \
+    } while (0)
                     if (v == 4) {
                         if (shallow) {
                             if (count) VENU_FUSED(k_trace_shade_wide, true, kSharedShallow);
@@ -792,9 +920,10 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                         VENU_CUDA(cudaEventRecord(e3, st));
                     }
                     launches += 1;
-                    // a first bounce with no more paths than the fused grid has
-                    // threads finishes them all in place: no later bounce has rays
-                    if (b == 0 && (uint64_t)PP * kk <= (uint64_t)r->fused_blocks * (uint64_t)tb) break;
+                    // a first bounce that the fused kernel finishes in place
+                    // finishes every path: no later bounce has rays
+                    if (b == 0 && (uint64_t)PP * kk <= (uint64_t)pg.in_place_factor * r->fused_blocks * (uint64_t)tb)
+                        break;
                     continue;
                 }
                 if (v == 0) {

@@ -63,6 +63,7 @@ struct PrimaryGen {
     uint32_t W, H, p0, P;
     int depth;                   // max_depth - 1
     FastDiv div_P, div_W;        // make_fastdiv(P), make_fastdiv(W)
+    uint32_t in_place_factor;    // venu_tuning.in_place_factor (>= 1)
 };
 
 // C: load_camera(g.cam), made once per block

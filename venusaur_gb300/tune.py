@@ -17,22 +17,25 @@ DEFAULT_SPACE = {
     "refill_min": (4, 8, 16),
     "traverse_block": (64, 128, 256),
     "shade_block": (128, 256),
+    "in_place_factor": (1, 8),
 }
 
 
 def candidates(space=None):
     space = dict(DEFAULT_SPACE, **(space or {}))
     seen = set()
-    for v, r, tb, sb in itertools.product(space["traverse_variant"], space["refill_min"],
-                                          space["traverse_block"], space["shade_block"]):
-        # the refill threshold matters to the dynamic-fetch variants only, the
-        # shade block to the variants with a separate shade kernel only
-        key = (v, r if v == 1 else 32, tb, sb if v not in (2, 4) else 256)
+    for v, r, tb, sb, f in itertools.product(space["traverse_variant"], space["refill_min"],
+                                             space["traverse_block"], space["shade_block"],
+                                             space["in_place_factor"]):
+        # the refill threshold matters to the dynamic-fetch variant only, the
+        # shade block to the variants with a separate shade kernel only, the
+        # in-place factor to the variants that are fused on every bounce only
+        key = (v, r if v == 1 else 32, tb, sb if v not in (2, 4) else 256, f if v in (2, 4) else 1)
         if key in seen:
             continue
         seen.add(key)
         yield dict(traverse_variant=v, refill_min=key[1], traverse_block=tb, traverse_blocks_per_sm=0,
-                   shade_block=key[3], shade_blocks_per_sm=0)
+                   shade_block=key[3], shade_blocks_per_sm=0, in_place_factor=key[4])
 
 
 def time_render(wf: Wavefront, scene: DeviceScene, cam, W, H, spp, depth, accum, reps=2):
@@ -54,9 +57,11 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
              reps=2, log=None, finalists=3, final_reps=6):
     """Returns (best_tuning: dict, best_max_paths: int, results: list).
 
-    Every candidate is timed once (reps renders); the `finalists` fastest are
-    timed again with final_reps renders each and the fastest of those wins,
-    so that run-to-run noise between close candidates decides less."""
+    Every candidate is timed once (reps renders) on the reduced copy; the
+    `finalists` fastest are timed again -- on the full workload when one
+    render of it takes at most about 0.3 s, else with final_reps renders of
+    the reduced copy -- and the fastest of those wins, so that run-to-run
+    noise and the reduced copy's smaller waves decide less."""
     tune_spp = tune_spp or max(1, min(spp, 8))
     accum = new_accum(W, H)
     results = []
@@ -69,15 +74,30 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
             if log:
                 log(results[-1])
         wf.close()
-    ranked = sorted(results, key=lambda r: -r["segments_per_s"])[:max(1, finalists)]
+    ranked = sorted(results, key=lambda r: -r["segments_per_s"])
+    # the finalists on the full workload when a render of it is short (the
+    # reduced copy has the same scene but smaller waves, which can favour
+    # other launch shapes: every candidate when a render takes at most
+    # ~50 ms, the `finalists` fastest up to ~300 ms), else on the reduced
+    # copy again
+    full_ms = ranked[0]["ms"] * spp / tune_spp
+    if full_ms <= 50.0:
+        final_spp, reps_final = spp, 3
+    elif full_ms <= 300.0:
+        final_spp, reps_final = spp, 3
+        ranked = ranked[:max(1, finalists)]
+    else:
+        final_spp, reps_final = tune_spp, final_reps
+        ranked = ranked[:max(1, finalists)]
     best = None
     for r in ranked:
         cand = {k: r[k] for k in r if k not in ("max_paths", "segments_per_s", "ms")}
         wf = Wavefront(r["max_paths"])
         wf.set_tuning(**cand)
-        rate, ms = time_render(wf, scene, cam, W, H, tune_spp, depth, accum, final_reps)
+        rate, ms = time_render(wf, scene, cam, W, H, final_spp, depth, accum, reps_final)
         wf.close()
         r["final_segments_per_s"] = rate
+        r["final_spp"] = final_spp
         if best is None or rate > best[0]:
             best = (rate, cand, r["max_paths"])
     return best[1], best[2], results
@@ -151,7 +171,8 @@ def autotune_jobs(jobs, pools=(16 << 20, 32 << 20, 64 << 20), blocks=(64, 128, 2
     return best_plain[1], best_batch[1], results
 
 
-def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5), blocks=(128, 256), reps=3):
+def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5), blocks=(128, 256), reps=3,
+            factors=(1, 8)):
     """Times every traversal variant x block shape on one render (the mean
     of `reps` renders after a warm-up) and, per variant, a counting render:
     box and sphere tests per segment, traversal steps per segment and the
@@ -163,16 +184,18 @@ def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5),
     accum = new_accum(W, H)
     for v in variants:
         for tb in blocks:
-            wf = Wavefront(min(256 << 20, W * H * spp))
-            wf.set_tuning(traverse_variant=v, traverse_block=tb)
-            rate, ms = time_render(wf, scene, cam, W, H, spp, depth, accum, reps)
-            same = None
-            if ref is None:
-                ref = accum.clone()
-            else:
-                same = bool(torch.equal(ref, accum))
-            wf.close()
-            out.append(dict(traverse_variant=v, traverse_block=tb, segments_per_s=rate, ms=ms, identical=same))
+            for f in (factors if v in (2, 4) else (1,)):
+                wf = Wavefront(min(256 << 20, W * H * spp))
+                wf.set_tuning(traverse_variant=v, traverse_block=tb, in_place_factor=f)
+                rate, ms = time_render(wf, scene, cam, W, H, spp, depth, accum, reps)
+                same = None
+                if ref is None:
+                    ref = accum.clone()
+                else:
+                    same = bool(torch.equal(ref, accum))
+                wf.close()
+                out.append(dict(traverse_variant=v, traverse_block=tb, in_place_factor=f, segments_per_s=rate, ms=ms,
+                                identical=same))
         wf = Wavefront(min(256 << 20, W * H * spp), count=True)
         wf.set_tuning(traverse_variant=v, traverse_block=blocks[0])
         wf.render(scene, cam, W, H, spp, accum, subframe=1 + reps, max_depth=depth, reset=True)
@@ -205,6 +228,7 @@ def main(argv=None) -> None:
     ap.add_argument("--depth", type=int, default=50)
     ap.add_argument("--variants", default="2,3,4,5")
     ap.add_argument("--blocks", default="128,256")
+    ap.add_argument("--factors", default="1,8", help="in-place factors tried with the fused variants")
     a = ap.parse_args(argv)
     sp = generate_rtiow(a.seed) if a.scene == "rtiow" else generate_random(a.n, a.seed)
     eye = (13.0, 2.0, 3.0) if a.scene == "rtiow" else (60.0, 15.0, 60.0)
@@ -214,7 +238,7 @@ def main(argv=None) -> None:
     print(json.dumps(dict(scene=a.scene, spheres=len(sp), width=a.width, height=a.height, spp=a.spp,
                           build_ms=info["build_ms"], wide_nodes=info["num_wide_nodes"], wide_ms=info["wide_ms"])))
     for row in compare(ds, cam, a.width, a.height, a.spp, a.depth, [int(x) for x in a.variants.split(",")],
-                       [int(x) for x in a.blocks.split(",")]):
+                       [int(x) for x in a.blocks.split(",")], factors=[int(x) for x in a.factors.split(",")]):
         print(json.dumps(row), flush=True)
 
 
