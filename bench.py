@@ -734,8 +734,13 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     del acc2
     nodes, sph = sc["nodes_visited"], sc["spheres_tested"]
     segs_c, paths_c = sc["segments"], sc["paths"]
-    variant = (tuning or {}).get("traverse_variant", wf.tuning()["traverse_variant"])
-    fused = variant == 2
+    cur = wf.tuning()
+    variant = (tuning or {}).get("traverse_variant", cur["traverse_variant"])
+    factor = (tuning or {}).get("in_place_factor", cur.get("in_place_factor", 1)) or 1
+    # variants 2 and 4 trace and shade in one kernel on every bounce (4 over
+    # the 4-wide tree); 3 and 5 only on the primary bounce, then k_traverse
+    # (5 over the 4-wide tree); 0 and 1 always run k_traverse
+    fused = variant in (2, 4)
     # Algorithmic bytes of the dominant kernel per render, by the per-segment
     # figure: 32 B per node (box) tested + 16 B per sphere tested + the ray
     # state queue traffic: 112 B per segment for the fused traverse+shade
@@ -747,10 +752,10 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     # write after the bounce).
     trav_bytes = nodes * 32 + sph * 16
     if fused:
-        kernel = "k_trace_shade"
+        kernel = "k_trace_shade" if variant == 2 else "k_trace_shade_wide"
         kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 112
-    elif variant == 3:  # fused primary bounce, separate traversal after it
-        kernel = "k_trace_shade (primary) + k_traverse"
+    elif variant in (3, 5):  # fused primary bounce, separate traversal after it
+        kernel = "k_trace_shade (primary) + k_traverse" + (" (4-wide tree)" if variant == 5 else "")
         kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 40
     else:
         kernel = "k_traverse"
@@ -769,7 +774,8 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     fp32_tflops = kflops / (stp["traverse_ms"] / 1000.0) / 1e12
     simd = sc["lane_steps"] / max(1, 32 * sc["warp_steps"])
     sha = kernel_sources_sha()
-    fig = NCU_FIGURES["figures"].get(f"{name}/v{variant}") if NCU_FIGURES["sha"] == sha else None
+    fig_key = f"{name}/v{variant}" + (f"/f{factor}" if fused and factor > 1 else "")
+    fig = NCU_FIGURES["figures"].get(fig_key) if NCU_FIGURES["sha"] == sha else None
     traffic = dram_frac = None
     if fig is not None:
         traffic = fig["dram_b_per_seg"] * segs_c / nl
@@ -790,6 +796,7 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
         "warp_inst_per_segment_ncu": fig["warp_inst_per_seg"] if fig else None,
         "ncu_kernel_sources_sha": NCU_FIGURES["sha"], "ncu_commit": NCU_FIGURES["commit"],
         "kernel_sources_sha": sha,
+        "ncu_figures_key": fig_key,
         "ncu_note": None if fig else ("no ncu figures for these kernel sources and this variant: traffic, "
                                       "dram_frac and lanes_per_inst_ncu are null"),
         "kernel_share": stp["traverse_ms"] / max(1e-9, ms / steps),

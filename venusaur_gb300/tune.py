@@ -57,11 +57,13 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
              reps=2, log=None, finalists=3, final_reps=6):
     """Returns (best_tuning: dict, best_max_paths: int, results: list).
 
-    Every candidate is timed once (reps renders) on the reduced copy; the
-    `finalists` fastest are timed again -- on the full workload when one
-    render of it takes at most about 0.3 s, else with final_reps renders of
-    the reduced copy -- and the fastest of those wins, so that run-to-run
-    noise and the reduced copy's smaller waves decide less."""
+    Every candidate is timed once (reps renders) on the reduced copy; then
+    every candidate (when one render of the full workload takes at most
+    about 50 ms) or the `finalists` fastest are timed again -- on the full
+    workload when one render of it takes at most about 0.3 s, else with
+    final_reps renders of the reduced copy -- and the fastest of those wins,
+    so that run-to-run noise and the reduced copy's smaller waves decide
+    less."""
     tune_spp = tune_spp or max(1, min(spp, 8))
     accum = new_accum(W, H)
     results = []
