@@ -720,8 +720,12 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     wfp = venu.Wavefront(max_paths, profile=True)
     if tuning:
         wfp.set_tuning(**tuning)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
     wfp.render(ds, cam, W, H, spp, acc2, subframe=last_sub, max_depth=depth, reset=True)
+    p1.record(stream)
     torch.cuda.synchronize()
+    prof_ms = p0.elapsed_time(p1)
     stp = wfp.stats()
     wfp.close()
     wfc = venu.Wavefront(max_paths, count=True)
@@ -799,7 +803,10 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
         "ncu_figures_key": fig_key,
         "ncu_note": None if fig else ("no ncu figures for these kernel sources and this variant: traffic, "
                                       "dram_frac and lanes_per_inst_ncu are null"),
-        "kernel_share": stp["traverse_ms"] / max(1e-9, ms / steps),
+        # the kernel's launches over the whole profiled render (the same
+        # render with an event pair around every launch)
+        "kernel_share": stp["traverse_ms"] / max(1e-9, prof_ms),
+        "profiled_render_ms": prof_ms,
         "fp32_tflops": fp32_tflops, "fp32_peak_tflops": fp32_peak, "fp32_frac": fp32_tflops / fp32_peak,
     }
     block = {

@@ -104,7 +104,9 @@ typedef struct venu_scene_info {
     uint64_t device_bytes;   /* resident bytes owned by the scene */
     float bounds[6];         /* centroid bounds used for Morton quantisation */
     float build_ms;          /* device time of the last LBVH build */
-    uint32_t num_wide_nodes; /* nodes of the 4-wide traversal tree collapsed from the LBVH */
+    uint32_t num_wide_nodes; /* nodes of the 4-wide traversal tree collapsed from the LBVH: built
+                                by the first venu_render with traversal variant 4 or 5 (0 until
+                                then; device_bytes grows by its size) */
     float wide_ms;           /* wall time of that collapse (host-driven, level by level) */
 } venu_scene_info;
 
@@ -293,7 +295,9 @@ typedef struct venu_tuning {
                                         3: 2 for the primary rays, 0 for later bounces;
                                         4: as 2, over the 4-wide tree collapsed from the
                                            LBVH (4 child boxes tested per step);
-                                        5: 2 for the primary rays, then 0 over the 4-wide tree */
+                                        5: 2 for the primary rays, then 0 over the 4-wide tree
+                                        (4 and 5: the first such render of a scene builds its
+                                        4-wide tree and blocks until it is built) */
     uint32_t refill_min;             /* variant 1: refill when >= this many lanes are idle (1..32) */
     uint32_t traverse_block;         /* threads per traversal block: 64, 128 or 256 */
     uint32_t traverse_blocks_per_sm; /* 0 = as many as fit */
@@ -301,7 +305,8 @@ typedef struct venu_tuning {
     uint32_t shade_blocks_per_sm;    /* 0 = as many as fit */
     uint32_t in_place_factor;        /* fused variants: a launch with at most this many rays per
                                         thread of its grid finishes its paths in place, bounce
-                                        after bounce, refilling finished threads (1..16; 0 = 1) */
+                                        after bounce, refilling finished threads (1..16; 0 = 1;
+                                        the batch engine ignores it) */
 } venu_tuning;
 VENU_API venu_status venu_renderer_set_tuning(venu_renderer* r, const venu_tuning* t);
 VENU_API venu_status venu_renderer_get_tuning(const venu_renderer* r, venu_tuning* t);

@@ -44,14 +44,22 @@ def test_refit_nodes_and_render(venu, oracle, cuda, case):
         mv = _moved(sp, 2, scale=2.0)
         eye = (60, 15, 60)
     ds = venu.DeviceScene(sp)
+    W, H, spp, depth = 40, 24, 3, 20
+    cam = oracle.camera(eye, (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+    info0 = ds.info()
+    assert info0["num_wide_nodes"] == 0  # the 4-wide tree is built on first use by variant 4 or 5
+    if case == "rtiow":
+        # the update below then refits an existing 4-wide tree; rand20k builds
+        # its 4-wide tree only after the update, from the refit binary tree
+        _render(venu, torch, ds, cam, W, H, 1, 1, depth, variant=4)
+        info1 = ds.info()
+        assert info1["num_wide_nodes"] > 0 and info1["device_bytes"] > info0["device_bytes"]
     before = ds.export_bvh()
     ds.update(mv)
     got = ds.export_bvh()
     assert np.array_equal(got["ids"], before["ids"]) and np.array_equal(got["keys"], before["keys"])
     want_nodes = oracle.lbvh_refit(sp, mv)
     assert np.array_equal(got["nodes"].view(np.uint32), want_nodes.view(np.uint32))
-    W, H, spp, depth = 40, 24, 3, 20
-    cam = oracle.camera(eye, (0, 0, 0), 20.0, W / H, 0.1, 10.0)
     acc, st = _render(venu, torch, ds, cam, W, H, spp, 2, depth)
     want = oracle.render(mv, cam, W, H, spp, subframe=2, max_depth=depth, built_from=sp)
     assert np.array_equal(acc.view(np.uint32), want["accum"].view(np.uint32))
@@ -59,10 +67,12 @@ def test_refit_nodes_and_render(venu, oracle, cuda, case):
     assert st["nodes_visited"] == want["nodes"] and st["spheres_tested"] == want["spheres"]
     fresh = oracle.render(mv, cam, W, H, spp, subframe=2, max_depth=depth)
     assert np.array_equal(acc.view(np.uint32), fresh["accum"].view(np.uint32))
-    # the 8-wide tree is refit with the binary one
+    # the 4-wide tree: refit with the binary one (rtiow) or built from it (rand20k)
+    assert (ds.info()["num_wide_nodes"] > 0) == (case == "rtiow")
     acc4, st4 = _render(venu, torch, ds, cam, W, H, spp, 2, depth, variant=4)
     assert np.array_equal(acc4.view(np.uint32), want["accum"].view(np.uint32))
     assert st4["segments"] == want["segments"]
+    assert ds.info()["num_wide_nodes"] > 0
 
 
 def test_refit_round_trip_and_limits(venu, oracle, cuda):

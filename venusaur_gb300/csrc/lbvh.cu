@@ -881,7 +881,7 @@ void free_scene(venu_scene* s) {
 
 // The wide tree of a built scene (n > 1): the collapse level by level from
 // the root (the host reads each level's size), then one write pass.
-venu_status build_wide(venu_scene* S, cudaStream_t st) {
+venu_status build_wide(const venu_scene* S, cudaStream_t st) {
     const uint32_t n = S->n;
     if (n < 2) return VENU_OK;
     const uint32_t nint = n - 1;
@@ -1031,10 +1031,24 @@ done:
     cudaFree(B.leafbox);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    if (rc == VENU_OK) {
-        const auto t0 = std::chrono::steady_clock::now();
-        rc = build_wide(S, st);
-        S->wide_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+venu_status ensure_wide(const venu_scene* S, cudaStream_t st) {
+    std::lock_guard<std::mutex> lock(S->wide_mu);
+    if (S->n < 2 || S->wide) return VENU_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    const venu_status rc = build_wide(S, st);
+    S->wide_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (rc != VENU_OK) {  // no half-built tree stays behind
+        cudaStreamSynchronize(st);
+        cudaFree(S->wide);
+        cudaFree(S->wide_src);
+        if (S->nwide)
+            S->bytes -= sizeof(float4) * kWideF4 * (size_t)S->nwide + sizeof(int32_t) * kWideChildren * (size_t)S->nwide;
+        S->wide = nullptr;
+        S->wide_src = nullptr;
+        S->nwide = 0;
     }
     return rc;
 }

@@ -809,6 +809,10 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     if (opts->flags & VENU_FLAG_RESET_ACCUM)
         VENU_CUDA(cudaMemsetAsync(accum_dev, 0, sizeof(float) * VENU_ACCUM_FLOATS_PER_PIXEL * npix64, st));
     VENU_CUDA(cudaMemsetAsync(r->stats, 0, sizeof(unsigned long long) * 6, st));
+    if (r->tune.traverse_variant == 4u || r->tune.traverse_variant == 5u) {
+        const venu_status ws = ensure_wide(scene, st);  // the first such render builds it
+        if (ws != VENU_OK) return ws;
+    }
     const SceneView S = view_of(scene);
     const bool count = (r->flags & VENU_RENDERER_COUNT) != 0;
     const bool prof = (r->flags & VENU_RENDERER_PROFILE) != 0;

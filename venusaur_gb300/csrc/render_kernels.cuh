@@ -115,16 +115,20 @@ __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, flo
     bool front = dot(d, outward) < 0.0f;
     f3 n = front ? outward : -outward;
     f3 dir;
-    if (type == 0u) {
-        dir = n + normalize(random_in_unit_sphere(seed));
-        if (near_zero(dir)) dir = n;
-        T = T * mk(m.x, m.y, m.z);
-    } else if (type == 1u) {
-        f3 refl = reflect(normalize(d), n);
-        dir = refl + m.w * random_in_unit_sphere(seed);
-        if (!(dot(dir, n) > 0.0f)) {
-            out.result = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            return out;
+    if (type <= 1u) {
+        // Lambertian and metal draw one point in the unit ball each; one call
+        // serves both, so a warp holding both kinds runs the rejection loop
+        // once instead of once per branch (each ray draws the same values)
+        const f3 u = random_in_unit_sphere(seed);
+        if (type == 0u) {
+            dir = n + normalize(u);
+            if (near_zero(dir)) dir = n;
+        } else {
+            dir = reflect(normalize(d), n) + m.w * u;
+            if (!(dot(dir, n) > 0.0f)) {
+                out.result = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                return out;
+            }
         }
         T = T * mk(m.x, m.y, m.z);
     } else {

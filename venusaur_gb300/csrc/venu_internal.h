@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "../../include/venu.h"
@@ -33,15 +34,19 @@ struct venu_scene {
     uint32_t* meta = nullptr;  // original id | material << 30
     uint32_t* keys = nullptr;  // sorted Morton codes
     int32_t* parents = nullptr;  // [n-1] parent of each internal node, then [n] of each leaf (for refits)
-    float4* wide = nullptr;      // 16 per wide node: the 8-wide traversal tree (lbvh.cu)
-    int32_t* wide_src = nullptr; // 8 per wide node: binary word of each child (for refits)
-    uint32_t nwide = 0;
+    // The 4-wide traversal tree (lbvh.cu), built on first use by a render
+    // with traversal variant 4 or 5 (ensure_wide); a cache of the binary
+    // tree, so it may be filled in through a const scene.
+    mutable float4* wide = nullptr;      // kWideF4 float4 per wide node
+    mutable int32_t* wide_src = nullptr; // kWideChildren per wide node: binary word of each child (for refits)
+    mutable uint32_t nwide = 0;
+    mutable float wide_ms = 0.0f;        // wall time of the wide tree's collapse
+    mutable std::mutex wide_mu;          // serialises that first build
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     uint32_t nhoist = 0;          // huge spheres tested before traversal
     int32_t hoist[4] = {0, 0, 0, 0};
     float build_ms = 0.0f;
-    float wide_ms = 0.0f;         // wall time of the wide tree's collapse
-    uint64_t bytes = 0;
+    mutable uint64_t bytes = 0;   // device bytes held (grows when the wide tree is built)
 };
 
 namespace venu {
@@ -51,4 +56,7 @@ void free_scene(venu_scene* s);
 // Moves the scene's spheres to `spheres_dev` (same count, original order) and
 // refits the boxes on `stream` (asynchronous).
 venu_status update_scene(venu_scene* s, const venu_sphere* spheres_dev, cudaStream_t stream);
+// Builds the scene's 4-wide tree on `stream` unless it exists (blocking: the
+// collapse reads each level's size on the host).  Thread-safe.
+venu_status ensure_wide(const venu_scene* s, cudaStream_t stream);
 }  // namespace venu
