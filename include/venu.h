@@ -270,7 +270,7 @@ VENU_API venu_status venu_trace(const venu_scene* scene, const float* rays_dev, 
 #define VENU_RENDERER_COUNT 1u   /* count nodes visited / spheres tested */
 #define VENU_RENDERER_PROFILE 2u /* CUDA events around every traverse / shade launch */
 
-/* max_paths: paths in flight per wave (0 = default 64 Mi, about 8 GB of queues;
+/* max_paths: paths in flight per wave (0 = default 64 Mi, about 8.6 GB of queues;
  * at most 2^28).  Larger waves mean fewer wave tails -- the last bounces of a
  * wave, when few paths are left -- and are faster: 16 -> 128 Mi gives +24 %
  * on a 1920x1080x256 RTIOW render, 16 -> 64 Mi +22 % on 1M spheres. */
@@ -344,7 +344,7 @@ typedef struct venu_batch_stats {
 
 #define VENU_BATCH_NO_GRAPH 1u /* run the path loop from the host (one launch per stage) */
 
-/* pool_paths: paths in flight (0 = 64 Mi, about 6.5 GB); max_jobs: concurrently admitted jobs (<= 4096). */
+/* pool_paths: paths in flight (0 = 64 Mi, about 7 GB); max_jobs: concurrently admitted jobs (<= 4096). */
 VENU_API venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs, uint32_t flags, venu_batch** out);
 VENU_API venu_status venu_batch_set_tuning(venu_batch* b, const venu_tuning* t);
 /* Bytes venu_batch_submit allocates for a job of this size (seed table + slots). */

@@ -714,16 +714,22 @@ const int32_t kNone = 0x7fffffff;
 // The LBVH walk shared by both arithmetic modes: test-children-at-parent,
 // near child first, far child's child pair pushed with its entry distance;
 // popped entries culled against the current closest hit (best_t, which the
-// leaf callback lowers).  Hoisted huge spheres are tested first.
+// leaf callback lowers).  Tested first: the sphere the ray leaves (`from`,
+// GB300 mode only; -1 for none), then the hoisted huge spheres but that one;
+// neither is tested again during the walk (the kernels' from_first,
+// venusaur_gb300/csrc/venu_device.cuh).
 // Deepest traversal stack of the walks on this thread since it was last reset
 // (the kernels keep the top entries of the same stack in shared memory).
 thread_local int tl_max_stack = 0;
 
 template <class Leaf>
-void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, uint64_t* nv, Leaf leaf) {
-    for (int32_t k : B.hoist) leaf(k);  // huge spheres first (the ground)
+void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, uint64_t* nv, Leaf leaf,
+              int32_t from = -1) {
+    if (from >= 0) leaf(from);
+    for (int32_t k : B.hoist)  // huge spheres (the ground)
+        if (k != from) leaf(k);
     if (B.n == 1) {
-        leaf(0);
+        if (from != 0) leaf(0);
         return;
     }
     float tn;
@@ -738,7 +744,7 @@ void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, ui
         float tn0 = 0, tn1 = 0;
         int32_t c0l = 0, c0r = 0, c1l = 0, c1r = 0;
         if (pl & kLeaf) {
-            if (!(pl & kHoisted)) leaf(pl & kSlotMask);
+            if (!(pl & kHoisted) && (pl & kSlotMask) != from) leaf(pl & kSlotMask);
         } else {
             const vo_node& nd = B.nodes[pl];
             if (nv) ++*nv;
@@ -747,7 +753,7 @@ void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, ui
             c0r = nd.right;
         }
         if (pr & kLeaf) {
-            if (!(pr & kHoisted)) leaf(pr & kSlotMask);
+            if (!(pr & kHoisted) && (pr & kSlotMask) != from) leaf(pr & kSlotMask);
         } else {
             const vo_node& nd = B.nodes[pr];
             if (nv) ++*nv;
@@ -789,8 +795,10 @@ void walk_bvh(const Bvh& B, const RayPre& R, float tmin, const float& best_t, ui
 }
 
 // GB300 closest hit: the LBVH walk with the GB300 sphere test.  Ties on t go
-// to the smaller sorted slot.
-Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, uint64_t* ns) {
+// to the smaller sorted slot.  from: sorted slot of the sphere the ray
+// leaves (-1: none), tested first.
+Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, uint64_t* ns,
+                int32_t from = -1) {
     Hit h{-1, tmax};
     if (B.n == 0) return h;
     RayPre R = prep(o, d);
@@ -804,7 +812,7 @@ Hit trace_gb300(const Bvh& B, f3 o, f3 d, float tmin, float tmax, uint64_t* nv, 
             best_t = t;
             best = k;
         }
-    });
+    }, from);
     if (best != kNone) {
         h.k = best;
         h.t = best_t;
@@ -1019,8 +1027,10 @@ f3 path_ref(const Scene& S, f3 o, f3 d, uint32_t seed, int depth, Counters& K) {
 // One path in GB300 mode: forward throughput, LBVH closest hit.
 f3 path_gb300(const Scene& S, f3 o, f3 d, uint32_t seed, int depth, Counters& K) {
     f3 T = mk(1.0f, 1.0f, 1.0f);
+    int32_t from = -1;  // the sphere the ray leaves
     for (;;) {
-        Hit h = trace_gb300(S.bvh, o, d, 0.001f, 1e16f, &K.nv, &K.ns);
+        Hit h = trace_gb300(S.bvh, o, d, 0.001f, 1e16f, &K.nv, &K.ns, from);
+        from = h.k;
         ++K.segs;
         if (h.k < 0) return T * sky_gb300(d);
         if (!(depth > 0)) return mk(0, 0, 0);

@@ -314,15 +314,18 @@ __device__ __forceinline__ void trace_shade_multi_loop(const DevJob* __restrict_
             const bool fresh = i >= gen_base;
             float4 o4, d4;
             uint32_t seed = 0;
+            int32_t from = -1;
             if (fresh) {
                 gen_primary(jobs, plan_job, plan_start, plan_off, np, i - gen_base, o4, d4, seed);
             } else {
                 o4 = qin.o[i];
                 d4 = qin.d[i];
+                from = qin.from[i];
             }
             job = __float_as_uint(d4.w) >> 8;
             for (bool first = true;; first = false) {
                 RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
+                R.from = from;
                 float t;
                 int32_t k;
                 {
@@ -346,6 +349,7 @@ __device__ __forceinline__ void trace_shade_multi_loop(const DevJob* __restrict_
                 if (!IN_PLACE || !r.cont) break;
                 o4 = r.o;
                 d4 = r.d;
+                from = r.from;
                 qout.t[i] = r.t;
             }
         }
@@ -354,6 +358,7 @@ __device__ __forceinline__ void trace_shade_multi_loop(const DevJob* __restrict_
             qout.o[pos] = r.o;
             qout.d[pos] = r.d;
             qout.t[pos] = r.t;
+            qout.from[pos] = r.from;
         }
         // finished paths per job: one atomic per distinct job in the warp
         const bool fin = valid && !r.cont;
@@ -536,6 +541,7 @@ void free_batch(venu_batch* b) {
         cudaFree(b->q[i].o);
         cudaFree(b->q[i].d);
         cudaFree(b->q[i].t);
+        cudaFree(b->q[i].from);
     }
     cudaFree(b->d_jobs);
     cudaFree(b->d_next);
@@ -601,6 +607,7 @@ extern "C" venu_status venu_batch_create(uint32_t pool_paths, uint32_t max_jobs,
         if (e == cudaSuccess) e = cudaMalloc(&b->q[i].o, sizeof(float4) * Q);
         if (e == cudaSuccess) e = cudaMalloc(&b->q[i].d, sizeof(float4) * Q);
         if (e == cudaSuccess) e = cudaMalloc(&b->q[i].t, sizeof(float4) * Q);
+        if (e == cudaSuccess) e = cudaMalloc(&b->q[i].from, sizeof(int32_t) * Q);
     }
     if (e == cudaSuccess) e = cudaMalloc(&b->d_jobs, sizeof(DevJob) * max_jobs);
     if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned long long) * max_jobs);

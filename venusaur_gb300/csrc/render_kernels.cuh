@@ -18,6 +18,7 @@ __device__ __forceinline__ void write_primary(const Queue& q, uint32_t pos, f3 o
     q.o[pos] = make_float4(o.x, o.y, o.z, __int_as_float((int)slot));
     q.d[pos] = make_float4(d.x, d.y, d.z, __uint_as_float((job << 8) | ((uint32_t)depth & kDepthMask)));
     q.t[pos] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
+    q.from[pos] = -1;
 }
 
 __device__ __forceinline__ DevCamera load_camera(const venu_camera& c) {
@@ -82,6 +83,7 @@ __device__ __forceinline__ void gen_primary(const PrimaryGen& g, const DevCamera
 struct ShadeOut {
     bool cont;
     float4 o, d, t;   // next queue entry when cont
+    int32_t from;     // its Queue::from: the sphere just hit
     float4 result;    // final path radiance when !cont
 };
 
@@ -143,6 +145,7 @@ __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, flo
             dir = refract(ud, n, ratio);
     }
     out.cont = true;
+    out.from = k;
     out.o = make_float4(p.x, p.y, p.z, o4.w);
     out.d = make_float4(dir.x, dir.y, dir.z, __uint_as_float((dbits & ~kDepthMask) | (uint32_t)(depth - 1)));
     out.t = make_float4(T.x, T.y, T.z, __uint_as_float(seed));

@@ -255,16 +255,20 @@ struct SceneView {
 //   for the lo plane, n1_k for the hi plane (the entry plane is lo when
 //   inv_k >= 0).  Such rays are rare (a direction component below ~1e-5 of
 //   the others) and traverse with their own instantiation of the loop.
+//   from: slot of the sphere the ray leaves (its origin lies on that
+//   sphere's surface), or -1 (camera rays, rays from the caller).
 struct RayPre {
     f3 o, d, inv, n0, n1;
     float a, inv_a;
     bool axis;
+    int32_t from;
 };
 
 constexpr float kSharedMarginMax = 1.0f;
 
 __device__ __forceinline__ RayPre prep(f3 o, f3 d) {
     RayPre R;
+    R.from = -1;
     R.o = o;
     R.d = d;
     float dx = fabsf(d.x) < 1e-20f ? copysignf(1e-20f, d.x) : d.x;
@@ -498,6 +502,19 @@ struct Tracer {
         }
     }
 
+    // Tested up front, with the whole warp converged: first the sphere the
+    // ray leaves (R.from; its origin lies within r/16 of that surface, so its
+    // test takes sphere_test's long refined branch, which in the walk would
+    // run at a different step in each lane), then the huge hoisted spheres
+    // (the ground) but that one.  Both are skipped during traversal, and
+    // their hit distances already cull boxes behind them.  The closest hit
+    // does not depend on the order of the tests.
+    __device__ __forceinline__ void from_first(const SceneView& S, TraceCounters& K) {
+        if (R.from >= 0) leaf(R.from, __ldg(S.sph + R.from), K);
+        for (uint32_t h = 0; h < S.nhoist; ++h)
+            if (S.hoist[h] != R.from) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
+    }
+
     // R_ from prep(); its axis flag must equal AXIS.
     __device__ __forceinline__ bool begin(const SceneView& S, const RayPre& R_, float tmin_, float tmax_,
                                           TraceCounters& K) {
@@ -509,12 +526,9 @@ struct Tracer {
         sp = 0;
         const uint32_t n = S.n;
         if (n == 0) return false;
-        // Huge spheres (the ground) are tested by every ray up front, with the
-        // whole warp converged; their leaves are skipped during traversal and
-        // their hit distance already culls boxes behind them.
-        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
+        from_first(S, K);
         if (n == 1) {
-            leaf(0, __ldg(S.sph), K);
+            if (R.from != 0) leaf(0, __ldg(S.sph), K);
             return false;
         }
         float tn;
@@ -550,13 +564,15 @@ struct Tracer {
         bool h0 = false, h1 = false;
         float tn0 = 0.0f, tn1 = 0.0f;
         if (w0 & kLeaf) {
-            if (!(w0 & kHoisted)) leaf(w0 & kSlotMask, make_float4(a0.x, a0.y, a0.z, b0.x), K);
+            if (!(w0 & kHoisted) && (w0 & kSlotMask) != R.from)
+                leaf(w0 & kSlotMask, make_float4(a0.x, a0.y, a0.z, b0.x), K);
         } else {
             if (COUNT) ++K.nodes;
             h0 = box_test<AXIS>(R, a0, b0, tmin, best_t, tn0);
         }
         if (w1 & kLeaf) {
-            if (!(w1 & kHoisted)) leaf(w1 & kSlotMask, make_float4(a1.x, a1.y, a1.z, b1.x), K);
+            if (!(w1 & kHoisted) && (w1 & kSlotMask) != R.from)
+                leaf(w1 & kSlotMask, make_float4(a1.x, a1.y, a1.z, b1.x), K);
         } else {
             if (COUNT) ++K.nodes;
             h1 = box_test<AXIS>(R, a1, b1, tmin, best_t, tn1);
@@ -687,6 +703,13 @@ struct WideTracer {
         }
     }
 
+    // as Tracer::from_first
+    __device__ __forceinline__ void from_first(const SceneView& S, TraceCounters& K) {
+        if (R.from >= 0) leaf(R.from, __ldg(S.sph + R.from), K);
+        for (uint32_t h = 0; h < S.nhoist; ++h)
+            if (S.hoist[h] != R.from) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
+    }
+
     __device__ __forceinline__ bool begin(const SceneView& S, const RayPre& R_, float tmin_, float tmax_,
                                           TraceCounters& K) {
         R = R_;
@@ -697,9 +720,9 @@ struct WideTracer {
         sp = 0;
         const uint32_t n = S.n;
         if (n == 0) return false;
-        for (uint32_t h = 0; h < S.nhoist; ++h) leaf(S.hoist[h], __ldg(S.sph + S.hoist[h]), K);
+        from_first(S, K);
         if (n == 1) {
-            leaf(0, __ldg(S.sph), K);
+            if (R.from != 0) leaf(0, __ldg(S.sph), K);
             return false;
         }
         float tn;
@@ -802,7 +825,7 @@ struct WideTracer {
         // ray and cull the pushed entries and the nearest child
         for (uint32_t lm = lhit; lm; lm &= lm - 1u) {
             const int32_t k = __ldg(words + (__ffs(lm) - 1)) & kSlotMask;
-            leaf(k, __ldg(S.sph + k), K);
+            if (k != R.from) leaf(k, __ldg(S.sph + k), K);
         }
         if (kmin != 0xffffffffu && __uint_as_float(kmin & ~7u) <= best_t) {
             cur = __ldg(words + (kmin & 7u));
@@ -863,15 +886,17 @@ __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPr
 }
 
 // ---------------------------------------------------------------------------
-// Path state in the wavefront queues (48 bytes per path):
+// Path state in the wavefront queues (52 bytes per path):
 //   o4 = {origin.xyz, slot (int bits)}
 //   d4 = {direction.xyz, remaining depth (int bits)}
 //   t4 = {throughput.rgb, bounce seed (uint bits)}
+//   from = slot of the sphere the ray leaves (RayPre::from), -1 for a camera ray
 // ---------------------------------------------------------------------------
 struct Queue {
     float4* o;
     float4* d;
     float4* t;
+    int32_t* from;
 };
 
 }  // namespace venu
