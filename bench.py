@@ -747,24 +747,24 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     fused = variant in (2, 4)
     # Algorithmic bytes of the dominant kernel per render, by the per-segment
     # figure: 32 B per node (box) tested + 16 B per sphere tested + the ray
-    # state queue traffic: 120 B per segment for the fused traverse+shade
-    # kernel (28 B ray write + read, 12 B hit write + read, 16 B
-    # throughput/seed/pixel read + write, 4 B slot of the sphere the ray
-    # leaves write + read), 44 B for the separate traversal kernel (28 B ray
-    # read, 4 B that slot read, 12 B hit write).  The fused kernel makes the
-    # primary rays itself from a 4-byte seed per path: 36 B for those
+    # state queue traffic: 112 B per segment for the fused traverse+shade
+    # kernel (28 B ray write + read -- the depth word also carries the slot
+    # of the sphere the ray leaves --, 12 B hit write + read, 16 B
+    # throughput/seed/pixel read + write), 40 B for the separate traversal
+    # kernel (28 B ray read, 12 B hit write).  The fused kernel makes the
+    # primary rays itself from a 4-byte seed per path: 32 B for those
     # segments (4 B seed write + read, 12 B hit, 16 B throughput/seed/pixel
-    # and 4 B slot written after the bounce).
+    # write after the bounce).
     trav_bytes = nodes * 32 + sph * 16
     if fused:
         kernel = "k_trace_shade" if variant == 2 else "k_trace_shade_wide"
-        kbytes = trav_bytes + paths_c * 36 + (segs_c - paths_c) * 120
+        kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 112
     elif variant in (3, 5):  # fused primary bounce, separate traversal after it
         kernel = "k_trace_shade (primary) + k_traverse" + (" (4-wide tree)" if variant == 5 else "")
-        kbytes = trav_bytes + paths_c * 36 + (segs_c - paths_c) * 44
+        kbytes = trav_bytes + paths_c * 32 + (segs_c - paths_c) * 40
     else:
         kernel = "k_traverse"
-        kbytes = trav_bytes + segs_c * 44
+        kbytes = trav_bytes + segs_c * 40
     nl = max(1, stp["traverse_launches"])
     per_launch_bytes = kbytes / nl
     avg_launch_s = stp["traverse_ms"] / nl / 1000.0

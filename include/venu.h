@@ -270,7 +270,7 @@ VENU_API venu_status venu_trace(const venu_scene* scene, const float* rays_dev, 
 #define VENU_RENDERER_COUNT 1u   /* count nodes visited / spheres tested */
 #define VENU_RENDERER_PROFILE 2u /* CUDA events around every traverse / shade launch */
 
-/* max_paths: paths in flight per wave (0 = default 64 Mi, about 8.6 GB of queues;
+/* max_paths: paths in flight per wave (0 = default 64 Mi, about 8 GB of queues;
  * at most 2^28).  Larger waves mean fewer wave tails -- the last bounces of a
  * wave, when few paths are left -- and are faster: 16 -> 128 Mi gives +24 %
  * on a 1920x1080x256 RTIOW render, 16 -> 64 Mi +22 % on 1M spheres. */

@@ -1030,7 +1030,8 @@ f3 path_gb300(const Scene& S, f3 o, f3 d, uint32_t seed, int depth, Counters& K)
     int32_t from = -1;  // the sphere the ray leaves
     for (;;) {
         Hit h = trace_gb300(S.bvh, o, d, 0.001f, 1e16f, &K.nv, &K.ns, from);
-        from = h.k;
+        // carried for slots up to 2^24 - 2 (the kernels keep 1 + slot in 24 bits)
+        from = (h.k >= 0 && h.k <= (1 << 24) - 2) ? h.k : -1;
         ++K.segs;
         if (h.k < 0) return T * sky_gb300(d);
         if (!(depth > 0)) return mk(0, 0, 0);

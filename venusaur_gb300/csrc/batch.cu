@@ -344,7 +344,7 @@ __device__ __forceinline__ void trace_shade_multi_loop(const DevJob* __restrict_
                                   : fresh                ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed))
                                                          : qin.t[i];
                 const float4 ow = o4;  // .w: the path's slot
-                r = shade_one(S2, o4, d4, t4, make_int2(__float_as_int(t), k));
+                r = shade_one<false>(S2, o4, d4, t4, make_int2(__float_as_int(t), k));
                 if (!r.cont) jobs[job].slots[(uint32_t)__float_as_int(ow.w)] = r.result;
                 if (!IN_PLACE || !r.cont) break;
                 o4 = r.o;

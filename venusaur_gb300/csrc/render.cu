@@ -22,7 +22,7 @@ namespace venu {
 
 // Camera rays of one wave (P pixels from p0, k samples from s0): path
 // pos = s * P + pl.  With path_seeds, only each path's raygen seed is written
-// (4 bytes instead of a 52-byte queue entry) and the fused kernel makes the
+// (4 bytes instead of a 48-byte queue entry) and the fused kernel makes the
 // camera ray itself (PrimaryGen); the pixel's seed still advances through
 // every sample's draws, which is what fixes the next sample's seed.
 __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, uint32_t P, uint32_t s0,
@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
         if (i < n) {
             float4 o4 = q.o[i], d4 = q.d[i];
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            R.from = q.from[i];
+            R.from = packed_from(d4.w);
             float t;
             int32_t k = trace_closest<COUNT, kShared, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x,
                                                            overflow, K);
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                     ray = my;
                     const float4 o4 = q.o[my], d4 = q.d[my];
                     RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-                    R.from = q.from[my];
+                    R.from = packed_from(d4.w);
                     if (R.axis) {
                         // a near-axis-parallel ray (rare): traced to the end now with
                         // the per-axis loop, on this lane's free stack; the lane
@@ -179,29 +179,26 @@ __device__ __forceinline__ void trace_shade_loop(const SceneView& S, const Queue
         if (valid) {
             float4 o4, d4;
             uint32_t seed = 0;
-            int32_t from = -1;
             if (gen.path_seeds) {
                 gen_primary(gen, cam, i, o4, d4, seed);
             } else {
                 o4 = qin.o[i];
                 d4 = qin.d[i];
-                from = qin.from[i];
             }
             slot = (uint32_t)__float_as_int(o4.w);
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            R.from = from;
+            R.from = packed_from(d4.w);
             float t;
             const int32_t k =
                 trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x, overflow, K);
             const float4 t4 = gen.path_seeds ? make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed)) : qin.t[i];
-            r = shade_one(S, o4, d4, t4, make_int2(__float_as_int(t), k));
+            r = shade_one<true>(S, o4, d4, t4, make_int2(__float_as_int(t), k));
         }
         const uint32_t pos = warp_append(r.cont, cnt_out);
         if (r.cont) {
             qout.o[pos] = r.o;
             qout.d[pos] = r.d;
             qout.t[pos] = r.t;
-            qout.from[pos] = r.from;
         } else if (valid) {
             slots[slot] = r.result;
         }
@@ -227,7 +224,6 @@ __device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Q
     const uint32_t i = base + t;  // this thread's state lives at i
     bool live = i < n;
     float4 o4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), d4 = o4;
-    int32_t from = -1;
     if (live) {
         uint32_t seed = 0;
         if (gen.path_seeds) {
@@ -236,7 +232,6 @@ __device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Q
         } else {
             o4 = qin.o[i];
             d4 = qin.d[i];
-            from = qin.from[i];
             qout.t[i] = qin.t[i];
         }
     }
@@ -257,28 +252,25 @@ __device__ __forceinline__ void trace_shade_in_place(const SceneView& S, const Q
                 qout.o[base + pos] = o4;
                 qout.d[base + pos] = d4;
                 qout.t[base + pos] = t4;
-                qout.from[base + pos] = from;
             }
             __syncthreads();
             live = t < cnt;
             if (live) {
                 o4 = qout.o[i];
                 d4 = qout.d[i];
-                from = qout.from[i];
             }
             held = cnt;
         }
         if (live) {
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            R.from = from;
+            R.from = packed_from(d4.w);
             float th;
             const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, th, sm, t, blockDim.x, overflow, K);
-            const ShadeOut r = shade_one(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
+            const ShadeOut r = shade_one<true>(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
             if (!first) ++extra;
             if (r.cont) {
                 o4 = r.o;
                 d4 = r.d;
-                from = r.from;
                 qout.t[i] = r.t;
             } else {
                 slots[(uint32_t)__float_as_int(o4.w)] = r.result;
@@ -318,7 +310,6 @@ __device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, 
     uint32_t held = 0;             // threads [0, held) hold the block's paths
     bool exhausted = false, live = false, first = false;
     float4 o4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f), d4 = o4;
-    int32_t from = -1;
     for (;;) {
         const uint32_t cnt = (uint32_t)__syncthreads_count(live);
         if (cnt == 0 && exhausted) break;
@@ -336,13 +327,11 @@ __device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, 
                     qout.o[base0 + pos] = o4;
                     qout.d[base0 + pos] = d4;
                     qout.t[base0 + pos] = t4;
-                    qout.from[base0 + pos] = from;
                 }
                 __syncthreads();
                 if (t < cnt) {
                     o4 = qout.o[i];
                     d4 = qout.d[i];
-                    from = qout.from[i];
                 }
             }
             uint32_t take = 0, base = 0;
@@ -363,12 +352,10 @@ __device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, 
                 if (gen.path_seeds) {
                     uint32_t seed = 0;
                     gen_primary(gen, cam, ray, o4, d4, seed);
-                    from = -1;
                     qout.t[j] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
                 } else {
                     o4 = qin.o[ray];
                     d4 = qin.d[ray];
-                    from = qin.from[ray];
                     qout.t[j] = qin.t[ray];
                 }
             }
@@ -377,16 +364,15 @@ __device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, 
         if (live) {
             const uint32_t i = base0 + t;
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
-            R.from = from;
+            R.from = packed_from(d4.w);
             float th;
             const int32_t k = trace_closest<COUNT, KS, WIDE>(S, R, 0.001f, 1e16f, th, sm, t, blockDim.x, overflow, K);
-            const ShadeOut r = shade_one(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
+            const ShadeOut r = shade_one<true>(S, o4, d4, qout.t[i], make_int2(__float_as_int(th), k));
             if (!first) ++extra;
             first = false;
             if (r.cont) {
                 o4 = r.o;
                 d4 = r.d;
-                from = r.from;
                 qout.t[i] = r.t;
             } else {
                 slots[(uint32_t)__float_as_int(o4.w)] = r.result;
@@ -474,14 +460,13 @@ __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int
         if (valid) {
             float4 o4 = qin.o[i], d4 = qin.d[i], t4 = qin.t[i];
             slot = (uint32_t)__float_as_int(o4.w);
-            r = shade_one(S, o4, d4, t4, hits[i]);
+            r = shade_one<true>(S, o4, d4, t4, hits[i]);
         }
         const uint32_t pos = warp_append(r.cont, cnt_out);
         if (r.cont) {
             qout.o[pos] = r.o;
             qout.d[pos] = r.d;
             qout.t[pos] = r.t;
-            qout.from[pos] = r.from;
         } else if (valid) {
             slots[slot] = r.result;
         }
@@ -686,7 +671,6 @@ void free_queues(venu_renderer* r) {
         cudaFree(r->q[i].o);
         cudaFree(r->q[i].d);
         cudaFree(r->q[i].t);
-        cudaFree(r->q[i].from);
         r->q[i] = Queue{};
     }
     cudaFree(r->hits);
@@ -696,7 +680,7 @@ void free_queues(venu_renderer* r) {
     r->Q = 0;
 }
 
-// Path queues for waves of Q paths (104 B + 8 B hit + 16 B slot per path).
+// Path queues for waves of Q paths (96 B + 8 B hit + 16 B slot per path).
 cudaError_t alloc_queues(venu_renderer* r, uint32_t Q) {
     free_queues(r);
     cudaError_t e = cudaSuccess;
@@ -704,7 +688,6 @@ cudaError_t alloc_queues(venu_renderer* r, uint32_t Q) {
         if (e == cudaSuccess) e = cudaMalloc(&r->q[i].o, sizeof(float4) * (size_t)Q);
         if (e == cudaSuccess) e = cudaMalloc(&r->q[i].d, sizeof(float4) * (size_t)Q);
         if (e == cudaSuccess) e = cudaMalloc(&r->q[i].t, sizeof(float4) * (size_t)Q);
-        if (e == cudaSuccess) e = cudaMalloc(&r->q[i].from, sizeof(int32_t) * (size_t)Q);
     }
     if (e == cudaSuccess) e = cudaMalloc(&r->hits, sizeof(int2) * (size_t)Q);
     if (e == cudaSuccess) e = cudaMalloc(&r->slots, sizeof(float4) * (size_t)Q);

@@ -10,16 +10,27 @@ namespace venu {
 // optixTrace).  The bounce seed is the raygen seed after the sample's jitter
 // and lens draws; the raygen seed continues from that same state to the next
 // sample (the reference copies it into the PRD and never copies it back).
-// d4.w packs the remaining depth (low 8 bits) and the job index (upper 24
-// bits, 0 for the single-scene renderer).
+// d4.w packs the remaining depth (low 8 bits) and, above it, the job index
+// in the batch engine, or 1 + the slot of the sphere the ray leaves in the
+// single-scene renderer (0 for a camera ray; see packed_from).
 constexpr uint32_t kDepthMask = 0xFFu;
 __device__ __forceinline__ void write_primary(const Queue& q, uint32_t pos, f3 o, f3 d, uint32_t slot,
                                               int depth, uint32_t seed, uint32_t job = 0) {
     q.o[pos] = make_float4(o.x, o.y, o.z, __int_as_float((int)slot));
     q.d[pos] = make_float4(d.x, d.y, d.z, __uint_as_float((job << 8) | ((uint32_t)depth & kDepthMask)));
     q.t[pos] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(seed));
-    q.from[pos] = -1;
 }
+
+// The sphere a continuing ray leaves (RayPre::from) is carried for slots up
+// to kFromMax: 1 + slot fits the 24 bits above the depth in d4.w.  A ray
+// leaving a sphere of a larger slot carries none and meets that sphere in
+// the walk instead (same closest hit).  The single-scene renderer keeps it
+// in d4.w (its queue entry stays 48 bytes; a separate 4-byte array measured
+// 1-4 % slower); the batch engine, whose d4.w holds the job index, in
+// Queue::from.
+constexpr uint32_t kFromMax = (1u << 24) - 2u;
+__device__ __forceinline__ int32_t from_of_hit(int32_t k) { return (uint32_t)k <= kFromMax ? k : -1; }
+__device__ __forceinline__ int32_t packed_from(float d4w) { return (int32_t)(__float_as_uint(d4w) >> 8) - 1; }
 
 __device__ __forceinline__ DevCamera load_camera(const venu_camera& c) {
     DevCamera k;
@@ -83,12 +94,15 @@ __device__ __forceinline__ void gen_primary(const PrimaryGen& g, const DevCamera
 struct ShadeOut {
     bool cont;
     float4 o, d, t;   // next queue entry when cont
-    int32_t from;     // its Queue::from: the sphere just hit
+    int32_t from;     // the sphere the next ray leaves (from_of_hit of the hit)
     float4 result;    // final path radiance when !cont
 };
 
 // One hit/miss record -> scatter (Core/RayTracer.cu:272-449, iterative):
 // forward throughput, black at depth 0 or on metal absorption, sky on miss.
+// PACK_FROM (single-scene renderer): the next ray's d4.w carries `from`
+// above the depth; otherwise it keeps the job index there.
+template <bool PACK_FROM>
 __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, float4 d4, float4 t4, int2 h) {
     ShadeOut out;
     out.cont = false;
@@ -145,9 +159,10 @@ __device__ __forceinline__ ShadeOut shade_one(const SceneView& S, float4 o4, flo
             dir = refract(ud, n, ratio);
     }
     out.cont = true;
-    out.from = k;
+    out.from = from_of_hit(k);
     out.o = make_float4(p.x, p.y, p.z, o4.w);
-    out.d = make_float4(dir.x, dir.y, dir.z, __uint_as_float((dbits & ~kDepthMask) | (uint32_t)(depth - 1)));
+    const uint32_t high = PACK_FROM ? (uint32_t)(out.from + 1) << 8 : (dbits & ~kDepthMask);
+    out.d = make_float4(dir.x, dir.y, dir.z, __uint_as_float(high | (uint32_t)(depth - 1)));
     out.t = make_float4(T.x, T.y, T.z, __uint_as_float(seed));
     return out;
 }

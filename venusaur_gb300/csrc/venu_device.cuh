@@ -886,11 +886,16 @@ __device__ __forceinline__ int32_t trace_closest(const SceneView& S, const RayPr
 }
 
 // ---------------------------------------------------------------------------
-// Path state in the wavefront queues (52 bytes per path):
+// Path state in the wavefront queues (48 bytes per path; 52 in the batch
+// engine):
 //   o4 = {origin.xyz, slot (int bits)}
-//   d4 = {direction.xyz, remaining depth (int bits)}
+//   d4 = {direction.xyz, remaining depth (bits 0-7) | job index (batch
+//         engine) or 1 + slot of the sphere the ray leaves (single-scene
+//         renderer) (bits 8-31)}
 //   t4 = {throughput.rgb, bounce seed (uint bits)}
-//   from = slot of the sphere the ray leaves (RayPre::from), -1 for a camera ray
+//   from = the batch engine's slot of the sphere the ray leaves
+//          (RayPre::from), -1 for a camera ray; null in the single-scene
+//          renderer
 // ---------------------------------------------------------------------------
 struct Queue {
     float4* o;
