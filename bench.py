@@ -81,14 +81,14 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # (c2: 4 spp, c3: 2 spp, c1: its own 16 spp) under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "40d7f87b59d5def3", "commit": "82e234c", "figures": {
-    "c2/v2": {"dram_b_per_seg": 62.4, "lanes_per_inst": 14.25, "warp_inst_per_seg": 89.1},
-    "c2/v4": {"dram_b_per_seg": 64.41, "lanes_per_inst": 16.96, "warp_inst_per_seg": 88.4},
-    "c1/v2": {"dram_b_per_seg": 37.71, "lanes_per_inst": 13.25, "warp_inst_per_seg": 109.2},
-    "c1/v4": {"dram_b_per_seg": 42.27, "lanes_per_inst": 15.0, "warp_inst_per_seg": 110.8},
-    "c3/v3": {"dram_b_per_seg": 59.83, "lanes_per_inst": 6.19, "warp_inst_per_seg": 693.9},
-    "c3/v2": {"dram_b_per_seg": 125.34, "lanes_per_inst": 6.06, "warp_inst_per_seg": 755.2},
-    "c3/v5": {"dram_b_per_seg": 65.63, "lanes_per_inst": 8.1, "warp_inst_per_seg": 664.2},
+NCU_FIGURES = {"sha": "02f3f20253a31d30", "commit": "c716ece", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.64, "lanes_per_inst": 15.73, "warp_inst_per_seg": 82.4},
+    "c2/v4": {"dram_b_per_seg": 63.93, "lanes_per_inst": 17.65, "warp_inst_per_seg": 84.6},
+    "c1/v2": {"dram_b_per_seg": 38.41, "lanes_per_inst": 14.65, "warp_inst_per_seg": 100.4},
+    "c1/v4": {"dram_b_per_seg": 41.52, "lanes_per_inst": 15.84, "warp_inst_per_seg": 104.8},
+    "c3/v3": {"dram_b_per_seg": 64.11, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.4},
+    "c3/v2": {"dram_b_per_seg": 127.42, "lanes_per_inst": 6.39, "warp_inst_per_seg": 722.8},
+    "c3/v5": {"dram_b_per_seg": 65.44, "lanes_per_inst": 8.48, "warp_inst_per_seg": 630.0},
 }}
 
 
