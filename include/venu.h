@@ -279,7 +279,12 @@ VENU_API venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, ve
  * accumulator (VENU_ACCUM_FLOATS_PER_PIXEL floats per pixel, device), then
  * the running mean written to image_f (RGBA32F, may be NULL) and image8
  * (sRGB RGBA8 as Core/RayTracer.cu:16-47, may be NULL).  Asynchronous on
- * `stream`; statistics are final once the stream has been synchronised. */
+ * `stream`; statistics are final once the stream has been synchronised.
+ * With the fused traversal variants (2, 4) each wave's bounce loop is one
+ * CUDA graph launch whose while node stops when no rays are left (the graph
+ * is built by the first such render and rebuilt when the scene, camera,
+ * image size, depth or tuning change); the renderer must not be used from
+ * two streams at once.  Replaces Core/Renderer.h:35-78. */
 VENU_API venu_status venu_render(venu_renderer* r, const venu_scene* scene, const venu_camera* camera,
                         const venu_render_opts* opts, float* accum_dev, float* image_f_dev,
                         uint8_t* image8_dev, void* stream);

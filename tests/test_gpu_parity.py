@@ -414,3 +414,39 @@ def test_in_place_refill_bit_exact(venu, oracle, cuda, scene):
         torch.cuda.synchronize()
         assert np.array_equal(acc.cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
         assert wf.stats()["segments"] == want["segments"]
+
+
+@pytest.mark.parametrize("variant,factor", [(2, 1), (4, 1), (2, 8)])
+def test_wave_graph_matches_host_loop(venu, oracle, cuda, variant, factor):
+    """The fused variants run each wave's bounce loop as one CUDA graph whose
+    while node stops when a bounce leaves no rays; the profiling build
+    launches every bounce from the host.  Both give the oracle's accumulator
+    and segment count, and the graph runs only the bounces that have rays
+    (at most one empty launch per wave) where the host launches all of
+    max_depth.  Waves of part of the pixels keep the host loop."""
+    torch = cuda
+    sp = oracle.scene_rtiow(0)
+    # (W, H, spp, depth, max_paths, launches with the graph against the host loop)
+    cases = [(200, 120, 2, 50, 10_000, "=="),   # waves of 10 k of the 24 k pixels, one sample: host loop
+             (64, 36, 2, 50, 0, "=="),           # 4.6 k paths, all finished in place by the first bounce
+             (1280, 720, 4, 50, 0, "<"),         # one wave of 3.7 M paths: more than 8 per thread of any grid
+             (320, 180, 6, 50, 120_000, "<=")]   # three waves of all pixels x 2 samples
+    for W, H, spp, depth, max_paths, rel in cases:
+        cam = oracle.camera((13, 2, 3), (0, 0, 0), 20.0, W / H, 0.1, 10.0)
+        want = oracle.render(sp, cam, W, H, spp, subframe=2, max_depth=depth, mode=pyoracle.MODE_GB300)
+        ds = venu.DeviceScene(sp)
+        got = {}
+        for profile in (False, True):
+            wf = venu.Wavefront(max_paths, profile=profile)
+            wf.set_tuning(traverse_variant=variant, traverse_block=128, in_place_factor=factor)
+            acc = venu.new_accum(W, H)
+            for _ in range(2):  # the second render reuses the graph
+                wf.render(ds, cam, W, H, spp, acc, subframe=2, max_depth=depth, reset=True)
+            torch.cuda.synchronize()
+            st = wf.stats()
+            assert np.array_equal(acc.cpu().numpy().view(np.uint32), want["accum"].view(np.uint32))
+            assert st["segments"] == want["segments"]
+            got[profile] = st["kernel_launches"]
+        # a wave the first bounce finishes in place stops after it either way
+        ok = {"<": got[False] < got[True], "<=": got[False] <= got[True], "==": got[False] == got[True]}[rel]
+        assert ok, (W, H, spp, got)

@@ -16,9 +16,25 @@
 #include "venu_internal.h"
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 namespace venu {
+
+// The bounce loop of a wave run as one CUDA graph (fused variants): the
+// first bounce's kernel, then a while node over a body of two bounce kernels
+// (odd: queue 1 -> 0, even: queue 0 -> 1), each with its queues and
+// counters as fixed parameters.  The last block of each bounce launch
+// advances the loop: it clears the counters the next bounce writes to,
+// counts the bounce, and keeps the while node going only while the bounce
+// left rays to trace -- so a wave whose paths all finish early (in place, or
+// by depth) launches no empty bounces.
+struct WaveCtl {
+    uint32_t b;            // bounces of the wave traced so far
+    uint32_t nb;           // at most this many (the maximum depth)
+    uint32_t blocks_done;  // blocks of the running bounce launch that finished
+    uint32_t pad;
+};
 
 // Camera rays of one wave (P pixels from p0, k samples from s0): path
 // pos = s * P + pl.  With path_seeds, only each path's raygen seed is written
@@ -28,12 +44,16 @@ namespace venu {
 __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, uint32_t P, uint32_t s0,
                          uint32_t k, uint32_t subframe, int max_depth, uint32_t* __restrict__ seeds,
                          Queue q, uint32_t* __restrict__ path_seeds, uint32_t* __restrict__ cnt,
-                         uint32_t* __restrict__ work, int nbounce) {
+                         uint32_t* __restrict__ work, int nbounce, WaveCtl* __restrict__ ctl) {
     const uint32_t pl = blockIdx.x * blockDim.x + threadIdx.x;
     if (pl == 0) {
         cnt[0] = P * k;
         for (int b = 1; b <= nbounce; ++b) cnt[b] = 0;
         for (int b = 0; b <= nbounce; ++b) work[b] = 0;
+        if (ctl) {
+            ctl->b = 0u;
+            ctl->nb = (uint32_t)nbounce;
+        }
     }
     if (pl >= P) return;
     const DevCamera C = load_camera(cam);
@@ -388,12 +408,34 @@ __device__ __forceinline__ void trace_shade_in_place_refill(const SceneView& S, 
 // round trip, the second read of the rays and one launch per bounce.
 // WIDE: the 4-wide tree instead of the binary traversal layout (variant 4,
 // k_trace_shade_wide, with its own register cap).
+// The end of a bounce launch run inside the wave graph (see WaveCtl).
+__device__ __forceinline__ void wave_advance(WaveCtl* ctl, uint32_t* cnt_in, uint32_t* work,
+                                             const uint32_t* cnt_out, unsigned long long* stats,
+                                             cudaGraphConditionalHandle handle) {
+    __syncthreads();  // every thread of the block is done
+    if (threadIdx.x != 0) return;
+    __threadfence();
+    if (atomicAdd(&ctl->blocks_done, 1u) != gridDim.x - 1u) return;
+    // the last block: every ray of this bounce is traced and shaded, and its
+    // input counters are read by nobody any more
+    __threadfence();
+    ctl->blocks_done = 0u;
+    *cnt_in = 0u;  // the output count of the next bounce
+    *work = 0u;    // the hand-out counter of the bounce after it
+    const uint32_t b = ctl->b + 1u;
+    ctl->b = b;
+    atomicAdd(stats + 5, 1ull);  // bounce launches run
+    const uint32_t more = b < ctl->nb && *reinterpret_cast<const volatile uint32_t*>(cnt_out) > 0u;
+    cudaGraphSetConditional(handle, more);
+}
+
 template <bool COUNT, int KS, bool WIDE, bool REFILL>
 __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue& qin,
-                                                 const uint32_t* __restrict__ cnt_in, uint32_t* __restrict__ work,
+                                                 uint32_t* __restrict__ cnt_in, uint32_t* __restrict__ work,
                                                  const Queue& qout, uint32_t* __restrict__ cnt_out,
                                                  float4* __restrict__ slots, uint32_t* __restrict__ err,
-                                                 unsigned long long* __restrict__ stats, const PrimaryGen& gen) {
+                                                 unsigned long long* __restrict__ stats, const PrimaryGen& gen,
+                                                 WaveCtl* ctl, cudaGraphConditionalHandle handle) {
     extern __shared__ unsigned char smem[];
     StackSmem sm;
     sm.node = reinterpret_cast<int*>(smem);
@@ -422,27 +464,32 @@ __device__ __forceinline__ void trace_shade_body(const SceneView& S, const Queue
     }
     if (overflow) atomicOr(err, 1u);
     if (COUNT) flush_counters(K, stats);
+    if (ctl) wave_advance(ctl, cnt_in, work, cnt_out, stats, handle);
 }
 
 // REFILL: launches of up to in_place_factor rays per thread finish in place
 // with refills (a separate instantiation, so the ordinary kernel keeps its
-// registers).
+// registers).  ctl: the wave graph's loop control (nullptr for a launch
+// from the host's bounce loop).
 template <bool COUNT, int KS, bool REFILL = false>
-__global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+__global__ void VENU_TRACE_BOUNDS k_trace_shade(SceneView S, Queue qin, uint32_t* __restrict__ cnt_in,
                                                 uint32_t* __restrict__ work, Queue qout,
                                                 uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                 uint32_t* __restrict__ err, unsigned long long* __restrict__ stats,
-                                                PrimaryGen gen) {
-    trace_shade_body<COUNT, KS, false, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
+                                                PrimaryGen gen, WaveCtl* ctl, cudaGraphConditionalHandle handle) {
+    trace_shade_body<COUNT, KS, false, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen, ctl,
+                                               handle);
 }
 
 template <bool COUNT, int KS, bool REFILL = false>
-__global__ void VENU_WIDE_BOUNDS k_trace_shade_wide(SceneView S, Queue qin, const uint32_t* __restrict__ cnt_in,
+__global__ void VENU_WIDE_BOUNDS k_trace_shade_wide(SceneView S, Queue qin, uint32_t* __restrict__ cnt_in,
                                                     uint32_t* __restrict__ work, Queue qout,
                                                     uint32_t* __restrict__ cnt_out, float4* __restrict__ slots,
                                                     uint32_t* __restrict__ err,
-                                                    unsigned long long* __restrict__ stats, PrimaryGen gen) {
-    trace_shade_body<COUNT, KS, true, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen);
+                                                    unsigned long long* __restrict__ stats, PrimaryGen gen,
+                                                    WaveCtl* ctl, cudaGraphConditionalHandle handle) {
+    trace_shade_body<COUNT, KS, true, REFILL>(S, qin, cnt_in, work, qout, cnt_out, slots, err, stats, gen, ctl,
+                                              handle);
 }
 
 __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int2* __restrict__ hits,
@@ -549,6 +596,24 @@ size_t traverse_smem(int block) { return traverse_smem(block, kShared); }
 
 using namespace venu;
 
+// Everything the wave graph's kernels take as parameters, and their launch
+// shape: the graph is rebuilt when any of it changes (zero-initialised, so
+// that whole objects compare with memcmp).
+struct WaveGraphKey {
+    SceneView S;
+    PrimaryGen pg;
+    Queue q0, q1;
+    uint32_t* cnt;
+    uint32_t* work;
+    float4* slots;
+    uint32_t* err;
+    unsigned long long* stats;
+    WaveCtl* ctl;
+    size_t fsm;
+    int grid, block;
+    uint32_t kind;  // bits: 4-wide tree, shallow stack, counting build, in-place refills
+};
+
 struct venu_renderer {
     uint32_t Q = 0;     // paths the queues hold now (grown on demand up to Qmax)
     uint32_t Qmax = 0;  // the wave size asked for at creation
@@ -561,10 +626,18 @@ struct venu_renderer {
     uint32_t* cnt = nullptr;   // [65]
     uint32_t* work = nullptr;  // [65]
     uint32_t* err = nullptr;
-    unsigned long long* stats = nullptr;  // segments, nodes, spheres
+    unsigned long long* stats = nullptr;  // segments, nodes, spheres, lane / warp steps, graph bounces
     venu_tuning tune = {2u, 32u, 128u, 0u, 128u, 0u, 1u};
     int trav_blocks = 0, shade_blocks = 0, fused_blocks = 0;
     venu_render_stats last = {};
+    uint32_t host_launches = 0;  // kernels the last render launched from the host
+    bool graph_off = false;      // the wave graph could not be built: host bounce loops only
+    // the wave graph (fused variants): built on first use, kept while its key holds
+    WaveCtl* ctl = nullptr;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t wgraph = nullptr;
+    cudaGraphExec_t wexec = nullptr;
+    WaveGraphKey wkey;
     // VENU_RENDERER_PROFILE: event pairs around traverse (even) / shade (odd) launches
     std::vector<cudaEvent_t> ev;
     size_t ev_used = 0;
@@ -699,9 +772,109 @@ cudaError_t alloc_queues(venu_renderer* r, uint32_t Q) {
     return cudaSuccess;
 }
 
+void destroy_wave_graph(venu_renderer* r);
+constexpr uint32_t kFusedWide = 1u, kFusedShallow = 2u, kFusedCount = 4u, kFusedRefill = 8u;
+
+// One bounce of the fused kernel (variant 2, or 4 over the 4-wide tree)
+// with the renderer's launch shape.  ctl / handle: the wave graph's loop
+// control, or nullptr / 0 for a launch from the host's bounce loop.
+cudaError_t launch_fused(const venu_renderer* r, cudaStream_t st, uint32_t kind, size_t fsm, const SceneView& S,
+                         const Queue& qi, uint32_t* cnt_in, uint32_t* work, const Queue& qo, uint32_t* cnt_out,
+                         const PrimaryGen& pg, WaveCtl* ctl, cudaGraphConditionalHandle h) {
+    const int grid = r->fused_blocks, tb = (int)r->tune.traverse_block;
+#define VENU_FUSED(KERNEL, C, KS, RF)                                                                       \
+    KERNEL<C, KS, RF><<<grid, tb, fsm, st>>>(S, qi, cnt_in, work, qo, cnt_out, r->slots, r->err, r->stats, pg, ctl, h)
+#define VENU_FUSED_RF(KERNEL, C, KS)                  \
+    do {                                              \
+        if (kind & kFusedRefill)                      \
+            VENU_FUSED(KERNEL, C, KS, true);          \
+        else                                          \
+            VENU_FUSED(KERNEL, C, KS, false);         \
+    } while (0)
+#define VENU_FUSED_CS(KERNEL, KS)                     \
+    do {                                              \
+        if (kind & kFusedCount)                       \
+            VENU_FUSED_RF(KERNEL, true, KS);          \
+        else                                          \
+            VENU_FUSED_RF(KERNEL, false, KS);         \
+    } while (0)
+    if (kind & kFusedWide) {
+        if (kind & kFusedShallow) VENU_FUSED_CS(k_trace_shade_wide, kSharedShallow);
+        else VENU_FUSED_CS(k_trace_shade_wide, kShared);
+    } else {
+        if (kind & kFusedShallow) VENU_FUSED_CS(k_trace_shade, kSharedShallow);
+        else VENU_FUSED_CS(k_trace_shade, kShared);
+    }
+#undef VENU_FUSED_CS
+#undef VENU_FUSED_RF
+#undef VENU_FUSED
+    return cudaGetLastError();
+}
+
+// Builds the wave graph for `key` (see WaveCtl): the first bounce (camera
+// rays from the per-path seeds, queue 0 -> 1), then while (rays left) {
+// queue 1 -> 0; queue 0 -> 1 }.  After an odd bounce that leaves no rays the
+// even one still starts and finds none, so a wave runs at most one empty
+// launch.
+venu_status build_wave_graph(venu_renderer* r, const WaveGraphKey& key) {
+    destroy_wave_graph(r);
+    if (!r->cap) VENU_CUDA(cudaStreamCreateWithFlags(&r->cap, cudaStreamNonBlocking));
+    VENU_CUDA(cudaGraphCreate(&r->wgraph, 0));
+    cudaGraph_t g = r->wgraph;
+    cudaGraphConditionalHandle h = 0;
+    VENU_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    PrimaryGen later = key.pg;
+    later.path_seeds = nullptr;  // bounces after the first read their rays from the queue
+    VENU_CUDA(cudaStreamBeginCaptureToGraph(r->cap, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    cudaError_t le = launch_fused(r, r->cap, key.kind, key.fsm, key.S, key.q0, key.cnt, key.work, key.q1,
+                                  key.cnt + 1, key.pg, key.ctl, h);
+    cudaGraph_t captured = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(r->cap, &captured);
+    if (le != cudaSuccess) return cuda_fail(le, "venu_render: capture of the first bounce");
+    if (ee != cudaSuccess) return cuda_fail(ee, "venu_render: cudaStreamEndCapture");
+    cudaGraphNode_t first = nullptr;
+    size_t nn = 1;
+    VENU_CUDA(cudaGraphGetNodes(g, &first, &nn));
+    if (nn != 1) {
+        set_error("venu_render: the first bounce captured as " + std::to_string(nn) + " graph nodes");
+        return VENU_ERR_CUDA;
+    }
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop = nullptr;
+    VENU_CUDA(cudaGraphAddNode(&loop, g, &first, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    VENU_CUDA(cudaStreamBeginCaptureToGraph(r->cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    le = launch_fused(r, r->cap, key.kind, key.fsm, key.S, key.q1, key.cnt + 1, key.work + 1, key.q0, key.cnt,
+                      later, key.ctl, h);
+    if (le == cudaSuccess)
+        le = launch_fused(r, r->cap, key.kind, key.fsm, key.S, key.q0, key.cnt, key.work, key.q1, key.cnt + 1,
+                          later, key.ctl, h);
+    ee = cudaStreamEndCapture(r->cap, &captured);
+    if (le != cudaSuccess) return cuda_fail(le, "venu_render: capture of the bounce loop");
+    if (ee != cudaSuccess) return cuda_fail(ee, "venu_render: cudaStreamEndCapture");
+    VENU_CUDA(cudaGraphInstantiate(&r->wexec, g, 0));
+    r->wkey = key;
+    return VENU_OK;
+}
+
+void destroy_wave_graph(venu_renderer* r) {
+    if (r->wexec) cudaGraphExecDestroy(r->wexec);
+    if (r->wgraph) cudaGraphDestroy(r->wgraph);
+    r->wexec = nullptr;
+    r->wgraph = nullptr;
+}
+
 void free_renderer(venu_renderer* r) {
     for (cudaEvent_t e : r->ev) cudaEventDestroy(e);
     r->ev.clear();
+    destroy_wave_graph(r);
+    if (r->cap) cudaStreamDestroy(r->cap);
+    r->cap = nullptr;
+    cudaFree(r->ctl);
     free_queues(r);
     cudaFree(r->seeds);
     cudaFree(r->cnt);
@@ -733,6 +906,8 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     if (e == cudaSuccess) e = cudaMalloc(&r->stats, sizeof(unsigned long long) * 6);
     if (e == cudaSuccess) e = cudaMemset(r->err, 0, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemset(r->stats, 0, sizeof(unsigned long long) * 6);
+    if (e == cudaSuccess) e = cudaMalloc(&r->ctl, sizeof(WaveCtl));
+    if (e == cudaSuccess) e = cudaMemset(r->ctl, 0, sizeof(WaveCtl));
     if (e == cudaSuccess) e = configure(r);
     if (e != cudaSuccess) {
         free_renderer(r);
@@ -858,24 +1033,74 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     // the SM's memory to L1 (measured: RTIOW +0.5 %; 1M spheres -4.5 %)
     const bool shallow = scene->n <= 4096u;
     uint32_t* const path_seeds = gen0 ? reinterpret_cast<uint32_t*>(r->q[0].t) : nullptr;
+    // the fused variants run each wave's bounce loop as one graph launch
+    // (WaveCtl) when every wave covers all pixels, so that the graph's
+    // parameters are the same for every wave; the profiling build times
+    // every launch from the host
+    const bool fused = tu.traverse_variant == 2u || tu.traverse_variant == 4u;
+    bool use_graph = fused && !prof && P == npix && !r->graph_off;
+    const uint32_t kind = (tu.traverse_variant == 4u ? kFusedWide : 0u) | (shallow ? kFusedShallow : 0u) |
+                          (count ? kFusedCount : 0u) | (tu.in_place_factor > 1u ? kFusedRefill : 0u);
+    const size_t fsm = shallow ? traverse_smem(tb, kSharedShallow) : tsm;
+    // the camera-ray generator of the wave of pixels [p0, p0 + PP)
+    auto primary_gen = [&](uint32_t p0, uint32_t PP) {
+        PrimaryGen pg;
+        std::memset(&pg, 0, sizeof pg);  // the graph key compares whole objects
+        pg.cam = *camera;
+        pg.W = W;
+        pg.H = H;
+        pg.p0 = p0;
+        pg.P = PP;
+        pg.depth = (int)maxd - 1;
+        pg.div_P = make_fastdiv(PP);
+        pg.div_W = make_fastdiv(W);
+        pg.in_place_factor = tu.in_place_factor ? tu.in_place_factor : 1u;
+        return pg;
+    };
+    if (use_graph) {
+        WaveGraphKey key;
+        std::memset(&key, 0, sizeof key);
+        key.S = S;
+        key.pg = primary_gen(0u, npix);
+        key.pg.path_seeds = path_seeds;
+        key.q0 = r->q[0];
+        key.q1 = r->q[1];
+        key.cnt = r->cnt;
+        key.work = r->work;
+        key.slots = r->slots;
+        key.err = r->err;
+        key.stats = r->stats;
+        key.ctl = r->ctl;
+        key.fsm = fsm;
+        key.grid = r->fused_blocks;
+        key.block = tb;
+        key.kind = kind;
+        if (!r->wexec || std::memcmp(&key, &r->wkey, sizeof key) != 0) {
+            if (build_wave_graph(r, key) != VENU_OK) {
+                // graphs unavailable here: the host's bounce loop from now on
+                destroy_wave_graph(r);
+                (void)cudaGetLastError();
+                r->graph_off = true;
+                use_graph = false;
+            }
+        }
+    }
     for (uint32_t s0 = 0; s0 < spp; s0 += k) {
         const uint32_t kk = std::min(k, spp - s0);
         for (uint32_t p0 = 0; p0 < npix; p0 += P) {
             const uint32_t PP = std::min(P, npix - p0);
             k_raygen<<<(PP + 255) / 256, 256, 0, st>>>(*camera, W, H, p0, PP, s0, kk, opts->subframe_index,
                                                        (int)maxd, r->seeds, r->q[0], path_seeds, r->cnt, r->work,
-                                                       nb);
-            PrimaryGen pg{};
-            pg.cam = *camera;
-            pg.W = W;
-            pg.H = H;
-            pg.p0 = p0;
-            pg.P = PP;
-            pg.depth = (int)maxd - 1;
-            pg.div_P = make_fastdiv(PP);
-            pg.div_W = make_fastdiv(W);
-            pg.in_place_factor = tu.in_place_factor ? tu.in_place_factor : 1u;
+                                                       nb, use_graph ? r->ctl : nullptr);
+            PrimaryGen pg = primary_gen(p0, PP);
             ++launches;
+            if (use_graph) {  // the bounce loop of this wave: one graph launch
+                VENU_CUDA(cudaGraphLaunch(r->wexec, st));
+                k_accumulate<<<(PP + 255) / 256, 256, 0, st>>>(r->slots, p0, PP, kk, accum);
+                ++launches;
+                ++waves;
+                continue;
+            }
             for (int b = 0; b < nb; ++b) {
                 const Queue& qi = r->q[b & 1];
                 const Queue& qo = r->q[(b + 1) & 1];
@@ -897,32 +1122,8 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
                 }
                 if (v == 2 || v == 4) {
                     pg.path_seeds = (b == 0) ? path_seeds : nullptr;
-                    const size_t fsm = shallow ? traverse_smem(tb, kSharedShallow) : tsm;
-#define VENU_FUSED(KERNEL, C, KS)                                                                           \
-    do {                                                                                                     \
-        if (pg.in_place_factor > 1u)                                                                         \
-            KERNEL<C, KS, true><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,        \
-                                                                  r->cnt + b + 1, r->slots, r->err, r->stats, pg); \
-        else                                                                                                 \
-            KERNEL<C, KS, false><<<r->fused_blocks, tb, fsm, st>>>(S, qi, r->cnt + b, r->work + b, qo,       \
-                                                                   r->cnt + b + 1, r->slots, r->err, r->stats, pg); \
-    } while (0)
-                    if (v == 4) {
-                        if (shallow) {
-                            if (count) VENU_FUSED(k_trace_shade_wide, true, kSharedShallow);
-                            else VENU_FUSED(k_trace_shade_wide, false, kSharedShallow);
-                        } else {
-                            if (count) VENU_FUSED(k_trace_shade_wide, true, kShared);
-                            else VENU_FUSED(k_trace_shade_wide, false, kShared);
-                        }
-                    } else if (shallow) {
-                        if (count) VENU_FUSED(k_trace_shade, true, kSharedShallow);
-                        else VENU_FUSED(k_trace_shade, false, kSharedShallow);
-                    } else {
-                        if (count) VENU_FUSED(k_trace_shade, true, kShared);
-                        else VENU_FUSED(k_trace_shade, false, kShared);
-                    }
-#undef VENU_FUSED
+                    VENU_CUDA(launch_fused(r, st, kind, fsm, S, qi, r->cnt + b, r->work + b, qo, r->cnt + b + 1,
+                                           pg, nullptr, 0));
                     if (prof) {
                         VENU_CUDA(cudaEventRecord(e1, st));
                         VENU_CUDA(cudaEventRecord(e2, st));
@@ -979,7 +1180,8 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     r->last = venu_render_stats{};
     r->last.paths = (uint64_t)npix * spp;
     r->last.waves = waves;
-    r->last.kernel_launches = launches;
+    r->last.kernel_launches = launches;  // plus the wave graphs' bounces, counted on the device
+    r->host_launches = launches;
     return VENU_OK;
 }
 
@@ -997,6 +1199,7 @@ extern "C" venu_status venu_renderer_stats(venu_renderer* r, venu_render_stats* 
     r->last.spheres_tested = st[2];
     r->last.lane_steps = st[3];
     r->last.warp_steps = st[4];
+    r->last.kernel_launches = r->host_launches + (uint32_t)st[5];
     // event pairs alternate traverse, shade (4 events per bounce)
     float tms = 0.0f, sms = 0.0f;
     uint32_t tn = 0, sn = 0;
