@@ -78,17 +78,20 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # kernel_sources_sha() of the captured build.  Each figure is summed over the
 # k_trace_shade (and, for variant 3, k_traverse) launches of two renders of
 # `bench.py --config <c> --spp <s> --profile-render --tuning <variant>`
-# (c2: 4 spp, c3: 2 spp, c1: its own 16 spp) under ncu --metrics
+# (c2: 4 spp, c3: 2 spp, c1: its own 16 spp; "/f8": in_place_factor 8)
+# under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "02f3f20253a31d30", "commit": "c716ece", "figures": {
-    "c2/v2": {"dram_b_per_seg": 62.64, "lanes_per_inst": 15.73, "warp_inst_per_seg": 82.4},
-    "c2/v4": {"dram_b_per_seg": 63.93, "lanes_per_inst": 17.65, "warp_inst_per_seg": 84.6},
-    "c1/v2": {"dram_b_per_seg": 38.41, "lanes_per_inst": 14.65, "warp_inst_per_seg": 100.4},
-    "c1/v4": {"dram_b_per_seg": 41.52, "lanes_per_inst": 15.84, "warp_inst_per_seg": 104.8},
-    "c3/v3": {"dram_b_per_seg": 64.11, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.4},
-    "c3/v2": {"dram_b_per_seg": 127.42, "lanes_per_inst": 6.39, "warp_inst_per_seg": 722.8},
-    "c3/v5": {"dram_b_per_seg": 65.44, "lanes_per_inst": 8.48, "warp_inst_per_seg": 630.0},
+NCU_FIGURES = {"sha": "3a3685e0ac39279e", "commit": "3eefd47", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.69, "lanes_per_inst": 15.87, "warp_inst_per_seg": 82.1},
+    "c2/v4": {"dram_b_per_seg": 63.99, "lanes_per_inst": 17.82, "warp_inst_per_seg": 84.4},
+    "c1/v2": {"dram_b_per_seg": 38.48, "lanes_per_inst": 14.81, "warp_inst_per_seg": 100.2},
+    "c1/v2/f8": {"dram_b_per_seg": 25.35, "lanes_per_inst": 15.67, "warp_inst_per_seg": 104.9},
+    "c1/v4": {"dram_b_per_seg": 41.56, "lanes_per_inst": 16.0, "warp_inst_per_seg": 104.7},
+    "c1/v4/f8": {"dram_b_per_seg": 26.82, "lanes_per_inst": 16.93, "warp_inst_per_seg": 110.0},
+    "c3/v3": {"dram_b_per_seg": 64.1, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.4},
+    "c3/v2": {"dram_b_per_seg": 127.56, "lanes_per_inst": 6.41, "warp_inst_per_seg": 721.7},
+    "c3/v5": {"dram_b_per_seg": 65.42, "lanes_per_inst": 8.48, "warp_inst_per_seg": 630.0},
 }}
 
 
@@ -346,7 +349,11 @@ def profile_render(venu, torch, cfg, args):
     W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
     ds = venu.DeviceScene(make_scene(venu, cfg["scene"]))
     cam = venu.Camera.look_at(cfg["eye"], (0, 0, 0), 20.0, W / H, 0.1, 10.0)
-    wf = venu.Wavefront(int(min(256 << 20, W * H * spp)))
+    # the profiling build launches every bounce from the host (ncu does not
+    # profile kernels of graphs with conditional nodes, which the fused
+    # variants otherwise run each wave's bounce loop as); the kernels and
+    # their work are the same
+    wf = venu.Wavefront(int(min(256 << 20, W * H * spp)), profile=True)
     wf.set_tuning(**(json.loads(args.tuning) if args.tuning else dict(traverse_variant=2, traverse_block=128)))
     acc = venu.new_accum(W, H)
     out = []
