@@ -284,7 +284,9 @@ VENU_API venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, ve
  * CUDA graph launch whose while node stops when no rays are left (the graph
  * is built by the first such render and rebuilt when the scene, camera,
  * image size, depth or tuning change); the renderer must not be used from
- * two streams at once.  Replaces Core/Renderer.h:35-78. */
+ * two streams at once.  On a stream that is being captured, every bounce is
+ * launched from the host instead, so the render can be captured into the
+ * caller's graph.  Replaces Core/Renderer.h:35-78. */
 VENU_API venu_status venu_render(venu_renderer* r, const venu_scene* scene, const venu_camera* camera,
                         const venu_render_opts* opts, float* accum_dev, float* image_f_dev,
                         uint8_t* image8_dev, void* stream);

@@ -1038,7 +1038,11 @@ extern "C" venu_status venu_render(venu_renderer* r, const venu_scene* scene, co
     // parameters are the same for every wave; the profiling build times
     // every launch from the host
     const bool fused = tu.traverse_variant == 2u || tu.traverse_variant == 4u;
-    bool use_graph = fused && !prof && P == npix && !r->graph_off;
+    // a caller capturing the stream into a graph of its own gets the
+    // host's bounce loop captured (no graph launched inside the capture)
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    VENU_CUDA(cudaStreamIsCapturing(st, &cap_status));
+    bool use_graph = fused && !prof && P == npix && !r->graph_off && cap_status == cudaStreamCaptureStatusNone;
     const uint32_t kind = (tu.traverse_variant == 4u ? kFusedWide : 0u) | (shallow ? kFusedShallow : 0u) |
                           (count ? kFusedCount : 0u) | (tu.in_place_factor > 1u ? kFusedRefill : 0u);
     const size_t fsm = shallow ? traverse_smem(tb, kSharedShallow) : tsm;
