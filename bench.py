@@ -82,15 +82,15 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "3a3685e0ac39279e", "commit": "3eefd47", "figures": {
-    "c2/v2": {"dram_b_per_seg": 62.69, "lanes_per_inst": 15.87, "warp_inst_per_seg": 82.1},
+NCU_FIGURES = {"sha": "474c2a06e6d31f43", "commit": "8a049e4", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.71, "lanes_per_inst": 15.87, "warp_inst_per_seg": 82.1},
     "c2/v4": {"dram_b_per_seg": 63.99, "lanes_per_inst": 17.82, "warp_inst_per_seg": 84.4},
-    "c1/v2": {"dram_b_per_seg": 38.48, "lanes_per_inst": 14.81, "warp_inst_per_seg": 100.2},
-    "c1/v2/f8": {"dram_b_per_seg": 25.35, "lanes_per_inst": 15.67, "warp_inst_per_seg": 104.9},
+    "c1/v2": {"dram_b_per_seg": 38.46, "lanes_per_inst": 14.8, "warp_inst_per_seg": 100.3},
+    "c1/v2/f8": {"dram_b_per_seg": 25.44, "lanes_per_inst": 15.66, "warp_inst_per_seg": 104.9},
     "c1/v4": {"dram_b_per_seg": 41.56, "lanes_per_inst": 16.0, "warp_inst_per_seg": 104.7},
-    "c1/v4/f8": {"dram_b_per_seg": 26.82, "lanes_per_inst": 16.93, "warp_inst_per_seg": 110.0},
-    "c3/v3": {"dram_b_per_seg": 64.1, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.4},
-    "c3/v2": {"dram_b_per_seg": 127.56, "lanes_per_inst": 6.41, "warp_inst_per_seg": 721.7},
+    "c1/v4/f8": {"dram_b_per_seg": 26.79, "lanes_per_inst": 16.92, "warp_inst_per_seg": 110.1},
+    "c3/v3": {"dram_b_per_seg": 64.12, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.4},
+    "c3/v2": {"dram_b_per_seg": 127.53, "lanes_per_inst": 6.41, "warp_inst_per_seg": 721.7},
     "c3/v5": {"dram_b_per_seg": 65.42, "lanes_per_inst": 8.48, "warp_inst_per_seg": 630.0},
 }}
 
