@@ -64,6 +64,10 @@ CPU_SAMPLE = {
 }
 METRIC = "path segments/s on 1 GB300 (batched/served vs plain); p50/p99 render latency"
 UNIT = "segments/s"
+# the renderer's largest wave (venu_renderer_create) and the batch engine's
+# largest pool (venu_batch_create)
+MAX_WAVE_PATHS = 1 << 30
+MAX_POOL_PATHS = 1 << 28
 
 # Sources of the plain renderer's kernels: the ncu figures below hold only
 # while these files are byte-identical to the ones they were taken on.
@@ -353,7 +357,7 @@ def profile_render(venu, torch, cfg, args):
     # profile kernels of graphs with conditional nodes, which the fused
     # variants otherwise run each wave's bounce loop as); the kernels and
     # their work are the same
-    wf = venu.Wavefront(int(min(256 << 20, W * H * spp)), profile=True)
+    wf = venu.Wavefront(int(min(MAX_WAVE_PATHS, W * H * spp)), profile=True)
     wf.set_tuning(**(json.loads(args.tuning) if args.tuning else dict(traverse_variant=2, traverse_block=128)))
     acc = venu.new_accum(W, H)
     out = []
@@ -393,7 +397,7 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
                     subframe=j["subframe"]) for j, c in list(zip(jobs, cams))[::4]]
         tuning, batch_tuning, _ = tune.autotune_jobs(red, pools=(16 << 20, 32 << 20, 64 << 20, 128 << 20))
     else:
-        batch_tuning = {"pool_paths": max_paths, "traverse_block": 256}
+        batch_tuning = {"pool_paths": min(max_paths, MAX_POOL_PATHS), "traverse_block": 256}
     acc_plain = [venu.new_accum(j["W"], j["H"]) for j in jobs]
     acc_batch = [venu.new_accum(j["W"], j["H"]) for j in jobs]
     img_plain = [torch.empty((j["W"] * j["H"], 4), dtype=torch.uint8, device="cuda") for j in jobs]
@@ -675,12 +679,14 @@ def measure_plain(venu, torch, rep, name, cfg, args, steps, warmup, headline):
     stream = torch.cuda.current_stream()
     ds = venu.DeviceScene(spheres)
     tuning, tune_log = None, []
-    # Wave size: every path of the render in flight when it fits, else the
-    # largest wave the renderer takes (2^28 paths, ~29 GB of queues and
-    # slots): fewer waves, fewer tails (measured on RTIOW 1080p x 256: 16 Mi
-    # 8.6, 32 Mi 9.8, 64 Mi 10.3, 128 Mi 10.7 G segments/s; later, with the
-    # primary rays made in the kernel, 128 Mi 11.07, 256 Mi 11.27).
-    max_paths = args.max_paths or int(min(256 << 20, W * H * spp))
+    # Wave size: every path of the render in flight (the renderer takes up
+    # to 2^30 paths, ~120 B each: the 1080p x 256 frame is one wave of
+    # 530.8 M paths, ~64 GB of queues and slots): fewer waves, fewer tails
+    # (measured on RTIOW 1080p x 256: 16 Mi 8.6, 32 Mi 9.8, 64 Mi 10.3,
+    # 128 Mi 10.7 G segments/s; later, with the primary rays made in the
+    # kernel, 128 Mi 11.07, 256 Mi 11.27; two waves of 2^28 against one
+    # 11.94 -> 12.01).
+    max_paths = args.max_paths or int(min(MAX_WAVE_PATHS, W * H * spp))
     if args.tuning:
         tuning = json.loads(args.tuning)
     elif not args.no_autotune:
@@ -940,6 +946,7 @@ def main():
 
     steps, warmup = args.steps, args.warmup
     block, state = measure_plain(venu, torch, rep, args.config, cfg, args, steps, warmup, headline=True)
+    state["wf"].close()  # its queues (~64 GB for the headline) before the next renderer takes its own
     e2e = measure_e2e(venu, torch, rep, cfg, state, steps)
     others = {}
     if not args.no_configs and world == 1:
@@ -979,7 +986,8 @@ def main():
     if not args.no_batched and world == 1:
         ds, cam, tuning = state["ds"], state["cam"], state["tuning"]
         line["batched_single_job"] = run_single_job(venu, torch, tuning, ds, cam, W, H, cfg["spp"], cfg["depth"],
-                                                    state["segs_step"], warmup + steps, state["max_paths"])
+                                                    state["segs_step"], warmup + steps,
+                                                    min(state["max_paths"], 256 << 20))
         retune = not (args.tuning or args.no_autotune)
         line["batched"] = run_batched(venu, torch, tuning, state["max_paths"], autotune=retune)
         line["batched_small_jobs"] = run_batched(venu, torch, tuning, state["max_paths"], small=True,

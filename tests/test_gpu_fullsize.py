@@ -47,6 +47,26 @@ def test_rtiow_1920x1080_256spp(venu, oracle, cuda):
     assert len(b.collect()) == 1
     torch.cuda.synchronize()
     assert torch.equal(acc, acc2)
+    b.close()
+    # the whole frame as one wave (the benchmark's shape, ~64 GB of queues)
+    # against the default waves of 64 Mi paths: the same samples in the same
+    # order, so the same bits
+    wf.close()
+    one = venu.Wavefront(W * H * spp)
+    one.render(ds, cam, W, H, spp, acc2, subframe=1, max_depth=depth, reset=True)
+    torch.cuda.synchronize()
+    st = one.stats()
+    one.close()
+    assert st["waves"] == 1 and st["paths"] == W * H * spp
+    assert torch.equal(acc, acc2)
+
+
+def test_renderer_wave_cap(venu, cuda):
+    """max_paths up to 2^30 (queues are allocated by the first render, so
+    creating the renderer costs nothing); above it, a clear error."""
+    venu.Wavefront(1 << 30).close()
+    with pytest.raises(venu.VenuError, match="2\\^30"):
+        venu.Wavefront((1 << 30) + 1)
 
 
 def test_random_1m_spheres_1080p_64spp(venu, oracle, cuda):

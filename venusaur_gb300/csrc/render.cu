@@ -893,8 +893,10 @@ extern "C" venu_status venu_renderer_create(uint32_t max_paths, uint32_t flags, 
     venu_status ds = require_device();
     if (ds != VENU_OK) return ds;
     if (max_paths == 0) max_paths = 64u << 20;
-    if (max_paths > (1u << 28)) {
-        set_error("venu_renderer_create: max_paths above 2^28");
+    // 2^30 keeps every path position and slot below 2^31 (signed slot words,
+    // FastDiv's range) at ~120 B per path (~129 GB at the maximum)
+    if (max_paths > (1u << 30)) {
+        set_error("venu_renderer_create: max_paths above 2^30");
         return VENU_ERR_TOO_LARGE;
     }
     venu_renderer* r = new venu_renderer();

@@ -187,7 +187,7 @@ def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5),
     for v in variants:
         for tb in blocks:
             for f in (factors if v in (2, 4) else (1,)):
-                wf = Wavefront(min(256 << 20, W * H * spp))
+                wf = Wavefront(min(1 << 30, W * H * spp))
                 wf.set_tuning(traverse_variant=v, traverse_block=tb, in_place_factor=f)
                 rate, ms = time_render(wf, scene, cam, W, H, spp, depth, accum, reps)
                 same = None
@@ -198,7 +198,7 @@ def compare(scene: DeviceScene, cam, W, H, spp, depth=50, variants=(2, 3, 4, 5),
                 wf.close()
                 out.append(dict(traverse_variant=v, traverse_block=tb, in_place_factor=f, segments_per_s=rate, ms=ms,
                                 identical=same))
-        wf = Wavefront(min(256 << 20, W * H * spp), count=True)
+        wf = Wavefront(min(1 << 30, W * H * spp), count=True)
         wf.set_tuning(traverse_variant=v, traverse_block=blocks[0])
         wf.render(scene, cam, W, H, spp, accum, subframe=1 + reps, max_depth=depth, reset=True)
         torch.cuda.synchronize()
