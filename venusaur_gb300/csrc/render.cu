@@ -71,6 +71,11 @@ __global__ void k_raygen(venu_camera cam, uint32_t W, uint32_t H, uint32_t p0, u
 }
 
 // WIDE: over the 4-wide tree (variant 5's later bounces).
+// The separate traversal and shading kernels read each queue entry and hit
+// record once: they load and store them evict-first (ld/st.global.cs), which
+// leaves more of L1 and L2 to the node set (1M spheres, variant 3: +0.5 %).
+// The fused kernel keeps plain accesses: the same hints measured -0.45 % on
+// the RTIOW scene there.
 template <bool COUNT, bool WIDE = false>
 __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const uint32_t* __restrict__ cnt,
                                                   uint32_t* __restrict__ work, int2* __restrict__ hits,
@@ -92,13 +97,13 @@ __global__ void __launch_bounds__(256) k_traverse(SceneView S, Queue q, const ui
         if (base >= n) break;
         const uint32_t i = base + lane;
         if (i < n) {
-            float4 o4 = q.o[i], d4 = q.d[i];
+            float4 o4 = __ldcs(q.o + i), d4 = __ldcs(q.d + i);
             RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
             R.from = packed_from(d4.w);
             float t;
             int32_t k = trace_closest<COUNT, kShared, WIDE>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x, blockDim.x,
                                                            overflow, K);
-            hits[i] = make_int2(__float_as_int(t), k);
+            __stcs(hits + i, make_int2(__float_as_int(t), k));
         }
     }
     if (overflow) atomicOr(err, 1u);
@@ -141,7 +146,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                 const uint32_t my = base + (uint32_t)__popc(idle & lt);
                 if (my < n) {
                     ray = my;
-                    const float4 o4 = q.o[my], d4 = q.d[my];
+                    const float4 o4 = __ldcs(q.o + my), d4 = __ldcs(q.d + my);
                     RayPre R = prep(mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z));
                     R.from = packed_from(d4.w);
                     if (R.axis) {
@@ -151,13 +156,13 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
                         float t;
                         const int32_t kk = trace_closest_as<COUNT, true>(S, R, 0.001f, 1e16f, t, sm, threadIdx.x,
                                                                          blockDim.x, overflow, K);
-                        hits[my] = make_int2(__float_as_int(t), kk);
+                        __stcs(hits + my, make_int2(__float_as_int(t), kk));
                     } else if (T.begin(S, R, 0.001f, 1e16f, K)) {
                         active = true;
                     } else {
                         float t;
                         const int32_t kk = T.result(t);
-                        hits[my] = make_int2(__float_as_int(t), kk);
+                        __stcs(hits + my, make_int2(__float_as_int(t), kk));
                     }
                 }
             }
@@ -170,7 +175,7 @@ __global__ void __launch_bounds__(256) k_traverse_dyn(SceneView S, Queue q, cons
             active = false;
             float t;
             const int32_t kk = T.result(t);
-            hits[ray] = make_int2(__float_as_int(t), kk);
+            __stcs(hits + ray, make_int2(__float_as_int(t), kk));
         }
     }
     if (overflow) atomicOr(err, 1u);
@@ -505,17 +510,17 @@ __global__ void __launch_bounds__(512) k_shade(SceneView S, Queue qin, const int
         uint32_t slot = 0;
         const bool valid = i < n;
         if (valid) {
-            float4 o4 = qin.o[i], d4 = qin.d[i], t4 = qin.t[i];
+            float4 o4 = __ldcs(qin.o + i), d4 = __ldcs(qin.d + i), t4 = __ldcs(qin.t + i);
             slot = (uint32_t)__float_as_int(o4.w);
-            r = shade_one<true>(S, o4, d4, t4, hits[i]);
+            r = shade_one<true>(S, o4, d4, t4, __ldcs(hits + i));
         }
         const uint32_t pos = warp_append(r.cont, cnt_out);
         if (r.cont) {
-            qout.o[pos] = r.o;
-            qout.d[pos] = r.d;
-            qout.t[pos] = r.t;
+            __stcs(qout.o + pos, r.o);
+            __stcs(qout.d + pos, r.d);
+            __stcs(qout.t + pos, r.t);
         } else if (valid) {
-            slots[slot] = r.result;
+            __stcs(slots + slot, r.result);
         }
     }
 }
@@ -527,7 +532,7 @@ __global__ void k_accumulate(const float4* __restrict__ slots, uint32_t p0, uint
     if (pl >= P) return;
     const uint32_t pix = p0 + pl;
     float4 a0 = accum[2 * (size_t)pix], a1 = accum[2 * (size_t)pix + 1];
-    for (uint32_t s = 0; s < k; ++s) kahan_add(a0, a1, slots[(size_t)s * P + pl]);
+    for (uint32_t s = 0; s < k; ++s) kahan_add(a0, a1, __ldcs(slots + (size_t)s * P + pl));
     accum[2 * (size_t)pix] = a0;
     accum[2 * (size_t)pix + 1] = a1;
 }
@@ -664,6 +669,23 @@ cudaError_t set_smem_refill(K kernel, size_t smem) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
+// Shared-memory carveout preference: just what `per_sm` resident blocks of
+// `kernel` need (static + dynamic + the 1 KB the system reserves per block),
+// so that the rest of the SM's unified memory is L1 (RTIOW 1080p x 256:
+// +0.5 %; the node records and spheres stay in L1 longer).
+template <typename K>
+cudaError_t prefer_l1(K kernel, int per_sm, size_t dyn) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return e;
+    int dev = 0, maxsm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+    const size_t need = (size_t)std::max(1, per_sm) * (fa.sharedSizeBytes + dyn + 1024);
+    const int pct = (int)std::min<size_t>(100, (need * 100 + (size_t)maxsm - 1) / (size_t)maxsm + 1);
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
 // Persistent grids: as many resident blocks as fit (or the tuned cap) on every SM.
 cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
@@ -722,6 +744,28 @@ cudaError_t configure(venu_renderer* r) {
             e = cudaFuncSetAttribute(k_traverse_dyn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     }
     if (e == cudaSuccess) e = occupancy_grid(k_shade, (int)t.shade_block, 0, t.shade_blocks_per_sm, r->shade_blocks);
+    if (e != cudaSuccess) return e;
+    {
+        const int nsm = std::max(1, sm_count());
+        const int pf = std::max(1, r->fused_blocks / nsm), pt = std::max(1, r->trav_blocks / nsm);
+        const size_t shallow = traverse_smem((int)t.traverse_block, kSharedShallow);
+        if (t.traverse_variant == 4) {
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade_wide<false, kShared>, pf, sm);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade_wide<false, kSharedShallow>, pf, shallow);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade_wide<false, kShared, true>, pf, sm);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade_wide<false, kSharedShallow, true>, pf, shallow);
+        } else if (t.traverse_variant >= 2) {
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade<false, kShared>, pf, sm);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade<false, kSharedShallow>, pf, shallow);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade<false, kShared, true>, pf, sm);
+            if (e == cudaSuccess) e = prefer_l1(k_trace_shade<false, kSharedShallow, true>, pf, shallow);
+        }
+        if (t.traverse_variant == 5 && e == cudaSuccess) e = prefer_l1(k_traverse<false, true>, pt, sm);
+        if ((t.traverse_variant == 0 || t.traverse_variant == 3) && e == cudaSuccess)
+            e = prefer_l1(k_traverse<false>, pt, sm);
+        if (t.traverse_variant == 1 && e == cudaSuccess) e = prefer_l1(k_traverse_dyn<false>, pt, sm);
+        if (e == cudaSuccess) e = prefer_l1(k_shade, std::max(1, r->shade_blocks / nsm), 0);
+    }
     return e;
 }
 
