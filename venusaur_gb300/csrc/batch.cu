@@ -489,7 +489,7 @@ cudaError_t batch_configure(venu_batch* b) {
     per_sm = std::max(1, per_sm);
     if (b->tune.traverse_blocks_per_sm) per_sm = std::min(per_sm, (int)b->tune.traverse_blocks_per_sm);
     b->trav_blocks = per_sm * sm_count();
-    return cudaSuccess;
+    return prefer_l1(k_trace_shade_multi<false>, per_sm, sm);
 }
 
 // One iteration of the path loop: trace the parity queue and the planned new

@@ -669,23 +669,6 @@ cudaError_t set_smem_refill(K kernel, size_t smem) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-// Shared-memory carveout preference: just what `per_sm` resident blocks of
-// `kernel` need (static + dynamic + the 1 KB the system reserves per block),
-// so that the rest of the SM's unified memory is L1 (RTIOW 1080p x 256:
-// +0.5 %; the node records and spheres stay in L1 longer).
-template <typename K>
-cudaError_t prefer_l1(K kernel, int per_sm, size_t dyn) {
-    cudaFuncAttributes fa;
-    cudaError_t e = cudaFuncGetAttributes(&fa, kernel);
-    if (e != cudaSuccess) return e;
-    int dev = 0, maxsm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
-    const size_t need = (size_t)std::max(1, per_sm) * (fa.sharedSizeBytes + dyn + 1024);
-    const int pct = (int)std::min<size_t>(100, (need * 100 + (size_t)maxsm - 1) / (size_t)maxsm + 1);
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
-}
-
 // Persistent grids: as many resident blocks as fit (or the tuned cap) on every SM.
 cudaError_t configure(venu_renderer* r) {
     const venu_tuning& t = r->tune;
