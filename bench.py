@@ -87,16 +87,16 @@ KERNEL_SOURCES = ("venusaur_gb300/csrc/venu_device.cuh", "venusaur_gb300/csrc/re
 # under ncu --metrics
 # dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum,
 # smsp__inst_executed.sum,smsp__thread_inst_executed.sum.
-NCU_FIGURES = {"sha": "247b625f8a2022b2", "commit": "df1517f", "figures": {
-    "c2/v2": {"dram_b_per_seg": 62.59, "lanes_per_inst": 15.87, "warp_inst_per_seg": 82.1},
-    "c2/v4": {"dram_b_per_seg": 63.86, "lanes_per_inst": 17.82, "warp_inst_per_seg": 84.4},
-    "c1/v2": {"dram_b_per_seg": 38.34, "lanes_per_inst": 14.14, "warp_inst_per_seg": 104.0},
-    "c1/v2/f8": {"dram_b_per_seg": 25.26, "lanes_per_inst": 14.97, "warp_inst_per_seg": 108.5},
-    "c1/v4": {"dram_b_per_seg": 41.28, "lanes_per_inst": 16.01, "warp_inst_per_seg": 104.6},
-    "c1/v4/f8": {"dram_b_per_seg": 26.68, "lanes_per_inst": 16.92, "warp_inst_per_seg": 110.1},
-    "c3/v3": {"dram_b_per_seg": 62.22, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.5},
-    "c3/v2": {"dram_b_per_seg": 127.28, "lanes_per_inst": 6.41, "warp_inst_per_seg": 721.7},
-    "c3/v5": {"dram_b_per_seg": 60.63, "lanes_per_inst": 8.48, "warp_inst_per_seg": 629.9},
+NCU_FIGURES = {"sha": "7ec4d38e57e4d468", "commit": "4264606", "figures": {
+    "c2/v2": {"dram_b_per_seg": 62.6, "lanes_per_inst": 15.87, "warp_inst_per_seg": 82.1},
+    "c2/v4": {"dram_b_per_seg": 63.86, "lanes_per_inst": 17.82, "warp_inst_per_seg": 84.3},
+    "c1/v2": {"dram_b_per_seg": 38.26, "lanes_per_inst": 14.14, "warp_inst_per_seg": 104.0},
+    "c1/v2/f8": {"dram_b_per_seg": 25.28, "lanes_per_inst": 14.96, "warp_inst_per_seg": 108.5},
+    "c1/v4": {"dram_b_per_seg": 41.31, "lanes_per_inst": 16.01, "warp_inst_per_seg": 104.6},
+    "c1/v4/f8": {"dram_b_per_seg": 26.64, "lanes_per_inst": 16.92, "warp_inst_per_seg": 110.1},
+    "c3/v3": {"dram_b_per_seg": 62.21, "lanes_per_inst": 6.58, "warp_inst_per_seg": 657.5},
+    "c3/v2": {"dram_b_per_seg": 127.3, "lanes_per_inst": 6.41, "warp_inst_per_seg": 721.7},
+    "c3/v5": {"dram_b_per_seg": 60.63, "lanes_per_inst": 8.48, "warp_inst_per_seg": 630.0},
 }}
 
 
