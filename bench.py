@@ -459,9 +459,9 @@ def run_batched(venu, torch, tuning, max_paths, n_jobs=64, small=False, autotune
 
 
 def run_served(venu, torch, tuning, n_sessions=40, util=0.8, budget=150 << 30):
-    """Serving, BASELINE config 5: progressive sessions (requests of 8, 8, 16,
-    32, 64 spp, each submitted when the previous image is back, accumulated
-    on the device) on scenes from the 1M-sphere distribution (100..1M
+    """Serving the progressive-session workload: sessions of requests of 8, 8,
+    16, 32, 64 spp (each submitted when the previous image is back,
+    accumulated on the device) on scenes from the 1M-sphere distribution (100..1M
     spheres, one scene per session, its BVH built when its first request is
     admitted and kept resident for the rest), four resolutions, depth 50.
 
