@@ -9,6 +9,7 @@ never change the image (every setting is bit-identical); only speed differs.
 from __future__ import annotations
 
 import itertools
+import math
 
 from .core import DeviceScene, Wavefront, new_accum
 
@@ -60,8 +61,9 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
     Every candidate is timed once (reps renders) on the reduced copy; then
     every candidate (when one render of the full workload takes at most
     about 50 ms) or the `finalists` fastest are timed again -- on the full
-    workload when one render of it takes at most about 0.3 s, else with
-    final_reps renders of the reduced copy -- and the fastest of those wins,
+    workload when one render of it takes at most about 0.3 s (a short
+    render repeated until each timing covers ~20 ms), else with final_reps
+    renders of the reduced copy -- and the fastest of those wins,
     so that run-to-run noise and the reduced copy's smaller waves decide
     less."""
     tune_spp = tune_spp or max(1, min(spp, 8))
@@ -84,7 +86,11 @@ def autotune(scene: DeviceScene, cam, W, H, spp, depth, space=None, max_paths=(8
     # copy again
     full_ms = ranked[0]["ms"] * spp / tune_spp
     if full_ms <= 50.0:
-        final_spp, reps_final = spp, 3
+        # a short render is repeated until each candidate's timing covers
+        # ~20 ms: three renders of a 0.7 ms frame left the pick to launch
+        # jitter (400x225x16: 128- or 256-thread blocks from run to run,
+        # 5.46 against 5.37 G segments/s)
+        final_spp, reps_final = spp, max(3, min(64, int(math.ceil(20.0 / max(full_ms, 1e-3)))))
     elif full_ms <= 300.0:
         final_spp, reps_final = spp, 3
         ranked = ranked[:max(1, finalists)]
