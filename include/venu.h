@@ -490,7 +490,9 @@ VENU_API venu_status venu_server_set_express(venu_server* s, uint64_t max_paths)
 /* Frees a progressive session's accumulator (after its admitted request, if
  * any, completes); a later request with the same id starts a new session. */
 VENU_API venu_status venu_server_end_session(venu_server* s, uint64_t session);
-/* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY). */
+/* Blocks until the request completes or timeout_s passes (VENU_ERR_NOT_READY).
+ * timeout_s <= 0 (or NaN) looks once without waiting; values above 1e9 s,
+ * infinity included, wait 1e9 s (about 32 years). */
 VENU_API venu_status venu_server_wait(venu_server* s, uint64_t request_id, double timeout_s, venu_result* out);
 VENU_API venu_status venu_server_cancel(venu_server* s, uint64_t request_id);
 VENU_API venu_status venu_server_release(venu_server* s, uint64_t request_id);

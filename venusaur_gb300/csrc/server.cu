@@ -625,7 +625,10 @@ extern "C" venu_status venu_server_wait(venu_server* s, uint64_t request_id, dou
         return VENU_ERR_INVALID;
     }
     Request* R = it->second.get();
-    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(timeout_s));
+    // NaN or <= 0: one look; above 1e9 s (infinity included): 1e9 s, whose
+    // count of nanoseconds still fits the clock's 64-bit duration
+    const double tw = timeout_s > 0.0 ? (timeout_s < 1e9 ? timeout_s : 1e9) : 0.0;
+    const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(tw));
     while (!R->done)
         if (s->cv_done.wait_until(lock, deadline) == std::cv_status::timeout && !R->done) {
             set_error("venu_server_wait: timed out");
